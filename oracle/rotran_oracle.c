@@ -1,0 +1,783 @@
+/*
+ * rotran_oracle.c -- CPU restatement of MOLFDIR rotran's Coulomb
+ * four-index transformation.  TEST INFRASTRUCTURE ONLY: this file is the
+ * parity oracle for the GPU library and the timed CPU baseline; no product
+ * code path links or calls it.
+ *
+ * Parity status: the reference is Fortran 77 and no Fortran compiler exists
+ * where this is built, and the reference ships no rotran fixtures, so this
+ * restatement is "parity unpinned" against reference-run outputs.  It is
+ * cross-checked instead against an independent dense formulation of the
+ * same integrals (tests/test_oracle.py).
+ *
+ * Scope: Coulomb integrals (BREIT = .FALSE.), spinors without point-group
+ * symmetry (one fermion irrep, quaternionic: classes 1-4 are written), the
+ * 32-bit LINUX label layout.  Each routine cites the reference lines it
+ * follows (paths relative to the MOLFDIR source tree).  Arithmetic order is
+ * kept where the reference fixes it (netlib ZGEMM summation order, the
+ * newest-first read order of the bucket chains) so that the restatement is
+ * close to the reference at the rounding level too.
+ *
+ * Two places where the reference cannot be followed literally for a
+ * quaternionic group, and what is done instead:
+ *  (1) source/rotran/rotran.F:184 sets NSKSIZ4 = 0 when QUATER is true,
+ *      i.e. exactly when the class-4 pp-interchange buffer is used; OUTPP2
+ *      then writes past a zero-length array.  Here class 4 gets the buffer
+ *      size NSKSIZ4 = MIN(NKR*NKR,16384) that the other classes' formula
+ *      gives.
+ *  (2) source/rotran/skelop.F:42 skips "(i,x|x,x)" rows at the level of
+ *      symmetry subreps; with a single quaternionic subrep both members of
+ *      a Kramers pair pass and TRANS2 (trans2.F:230-311) would write two
+ *      records under every barred label.  Here records are written only for
+ *      barred I (IKRMO(I) < 0), the set the record labels describe.
+ *  (3) source/rotran/outpp2.F:220-251 (ITYP 4) lacks the IKR.EQ.JKR return
+ *      that ITYP 1 has at outpp2.F:186, so a diagonal source record would
+ *      add its (a,a) element twice to class-4 records.  The guard is applied
+ *      here; with it every MDCINT element equals the complete integral.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "rotran_oracle.h"
+
+typedef struct {
+    double re, im;
+} cplx;
+
+static inline cplx cadd(cplx a, cplx b) { cplx r = {a.re + b.re, a.im + b.im}; return r; }
+static inline cplx cmul(cplx a, cplx b) {
+    cplx r = {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+    return r;
+}
+static inline cplx cconj(cplx a) { cplx r = {a.re, -a.im}; return r; }
+static inline cplx cscal(double s, cplx a) { cplx r = {s * a.re, s * a.im}; return r; }
+static inline double cabs_(cplx a) { return hypot(a.re, a.im); }
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+/* GETTW scale factor per integral type (source/rotran/gettw.F:33-45). */
+double orc_gettw_factor(int it) {
+    if (it == 1) return 0.125;
+    if (it == 2) return 0.5;
+    if (it == 3) return 0.25;
+    if (it == 4) return 0.5;
+    if (it <= 8) return 0.5;
+    return 1.0;
+}
+
+/* INTTYP (source/rotran/inttyp.F:1-79). */
+int orc_inttyp(int imm, int jmm, int kmm, int lmm) {
+    if (kmm > jmm) {
+        if (jmm > lmm) return (imm != kmm) ? 13 : 10;
+        if (jmm != lmm) return (kmm != lmm) ? 14 : 8;
+        return (imm != kmm) ? 11 : 2;
+    }
+    if (kmm != lmm) {
+        if (imm != jmm) return (jmm != kmm) ? 12 : 9;
+        return (jmm != kmm) ? 5 : 4;
+    }
+    if (jmm != kmm) return (imm != jmm) ? 7 : 3;
+    return (imm != jmm) ? 6 : 1;
+}
+
+/* Record index of the Kramers-unique pair (source/rotran/unique.F:1-50). */
+static void unique_(int nkr, const int* ikrmo, int i, int j, int* ij, int* conjug, int* is) {
+    int ikr = ikrmo[i - 1], jkr = ikrmo[j - 1];
+    int iikr, jjkr;
+    if (abs(ikr) >= abs(jkr)) {
+        iikr = ikr; jjkr = jkr; *conjug = 0;
+    } else {
+        iikr = jkr; jjkr = ikr; *conjug = 1;
+    }
+    *is = 1;
+    if (iikr > 0) {
+        *is = (iikr * jjkr >= 0) ? 1 : -1; /* ISIGN(1, IIKR*JJKR) */
+        iikr = -iikr; jjkr = -jjkr; *conjug = !*conjug;
+    }
+    int ijbaroff = nkr * (nkr + 1) / 2;
+    if (jjkr > 0)
+        *ij = (jjkr - 1) * (2 * nkr - jjkr) / 2 - iikr;
+    else
+        *ij = ijbaroff - (jjkr + 1) * (2 * nkr + jjkr) / 2 - iikr;
+}
+
+/* The buffer sizes rotran derives from its fixed work array (rotran.F:77-225);
+ * they fix the order in which bucket chains are read back. */
+static void ref_buffer_sizes(int nsc, int nkr, int nsp, int npqbuf_used, int* nijsiz,
+                             int* nsksiz, int* nc2) {
+    const long NWORK = 16000000L, NITR = 2, NRTC = 2, MAXPASS = 10;
+    long nsctr = (long)nsc * (nsc + 1) / 2, nsptr = (long)nkr * (nkr + 1), nspsq = (long)nsp * nsp;
+    long ng = nsctr, nijbuf = nsptr;
+    long npqbuf = nsctr < 16384 ? nsctr : 16384;
+    if (npqbuf_used < npqbuf) npqbuf = npqbuf_used; /* MAKIND (makind.F:277) */
+    long lbrcij = 1;
+    long indpq = lbrcij + ((nsptr + 1) + 1) / NITR;
+    long indpqu = indpq + (nsctr + 1) / NITR;
+    long indpqs = indpqu + (nsctr + 1) / NITR;
+    long ipqmin = indpqs + (nsctr + 1) / NITR;
+    long ipqmax = ipqmin + (MAXPASS + 1) / NITR;
+    long ipsym = ipqmax + (MAXPASS + 1) / NITR;
+    long nij = npqbuf < 16384 ? npqbuf : 16384;
+    long top = ipsym + (nsc * 1 + 1) / NITR;
+    long label1 = top + ((npqbuf + 1) + 1) / NITR;
+    for (;;) {
+        long nbck = label1;
+        long lbck = nbck + (nijbuf + 1) / NITR;
+        long cbck = lbck + (nijbuf * nij + 1) / NITR;
+        long indg = cbck + nijbuf * nij * NRTC;
+        long g = indg + ng * 2;
+        long ha = g + ng;
+        long ri = ha + (long)nsc * nsp * NRTC;
+        long ria = ri + nspsq * NRTC;
+        long rib = ria + nspsq * NRTC;
+        top = rib + nspsq * NRTC;
+        if (top <= NWORK || nij <= 128) break;
+        nij = nij - 128 > 128 ? nij - 128 : 128;
+    }
+    *nijsiz = (int)nij;
+    long k2 = (long)nkr * nkr;
+    nsksiz[0] = (int)(k2 < 16384 ? k2 : 16384);
+    nsksiz[1] = (int)(nsptr / 2 < 16384 ? nsptr / 2 : 16384);
+    nsksiz[2] = nsksiz[1];
+    nsksiz[3] = nsksiz[0]; /* deviation (1) in the file header */
+    long nsk = nsksiz[0];
+    for (int c = 1; c < 4; c++) if (nsksiz[c] > nsk) nsk = nsksiz[c];
+    long lbrcsk4 = lbrcij + ((nsptr + 1) + 1) / NITR + 3 * ((nkr + 2) / NITR);
+    top = lbrcsk4 + (nkr + 2) / NITR;
+    long jkrind = top;
+    long icind = jkrind + (nkr + 1) / NITR;
+    long indkl2 = icind + (nkr + 1) / NITR;
+    long indk2 = indkl2 + (nspsq + 1) / NITR;
+    long indl2 = indk2 + (nspsq + 1) / NITR;
+    long rkl2 = indl2 + (nspsq + 1) / NITR;
+    long lbcks = rkl2 + nspsq * NRTC;
+    long cbcks = lbcks + (2 * nsk) / NITR;
+    top = cbcks + nsk * NRTC;
+    long freew = NWORK - top;
+    long c2 = freew / ((long)nkr * nkr * NRTC);
+    if (c2 < 1) c2 = 1;
+    if (c2 > nkr) c2 = nkr;
+    *nc2 = (int)c2;
+}
+
+/* CSR list whose per-row order is the newest-first chunk order in which a
+ * linked-record bucket file is read back (e.g. getsti.F:252-269). */
+static void chunk_reverse_order(long n, int chunk, long* perm) {
+    /* entries 0..n-1 appended in order; chunks of `chunk`; newest first */
+    if (n == 0) return;
+    long nch = (n + chunk - 1) / chunk, k = 0;
+    for (long c = nch - 1; c >= 0; c--) {
+        long s = c * chunk, e = s + chunk < n ? s + chunk : n;
+        for (long x = s; x < e; x++) perm[k++] = x;
+    }
+}
+
+typedef struct {
+    int lkr, ij;
+    cplx v;
+} ppent;
+
+typedef struct {
+    ppent* e;
+    long n, cap;
+} pplist;
+
+static void pp_push(pplist* l, int lkr, int ij, cplx v) {
+    if (l->n == l->cap) {
+        l->cap = l->cap ? 2 * l->cap : 64;
+        l->e = (ppent*)realloc(l->e, sizeof(ppent) * l->cap);
+    }
+    l->e[l->n].lkr = lkr;
+    l->e[l->n].ij = ij;
+    l->e[l->n].v = v;
+    l->n++;
+}
+
+typedef struct {
+    int ikr, jkr, nz;
+    long off; /* into idx/val of the class store */
+} skrec;
+
+typedef struct {
+    skrec* r;
+    long nr, capr;
+    int* kl;
+    cplx* v;
+    long nv, capv;
+} skfile;
+
+static void sk_begin(skfile* f, int ikr, int jkr) {
+    if (f->nr == f->capr) {
+        f->capr = f->capr ? 2 * f->capr : 64;
+        f->r = (skrec*)realloc(f->r, sizeof(skrec) * f->capr);
+    }
+    f->r[f->nr].ikr = ikr;
+    f->r[f->nr].jkr = jkr;
+    f->r[f->nr].nz = 0;
+    f->r[f->nr].off = f->nv;
+    f->nr++;
+}
+
+static void sk_add(skfile* f, int kl, cplx v) {
+    if (f->nv == f->capv) {
+        f->capv = f->capv ? 2 * f->capv : 1024;
+        f->kl = (int*)realloc(f->kl, sizeof(int) * f->capv);
+        f->v = (cplx*)realloc(f->v, sizeof(cplx) * f->capv);
+    }
+    f->kl[f->nv] = kl;
+    f->v[f->nv] = v;
+    f->nv++;
+    f->r[f->nr - 1].nz++;
+}
+
+/* OUTPP1 (source/rotran/outpp1.F:43-116); rl is NSP x NSP column-major. */
+static void outpp1(int nkr, int nsp, int ityp, skfile* f, double thres, const int* krk,
+                   const int* krl, int ikr, int jkr, const cplx* rl, long* nskel) {
+    sk_begin(f, ikr, jkr);
+    int kkrmax = (ityp == 4) ? nkr : ikr;
+    for (int kkr = 1; kkr <= kkrmax; kkr++) {
+        int k = krk[kkr - 1];
+        int lkrmax = kkr;
+        if (ityp <= 3 && ikr == kkr) lkrmax = jkr;
+        for (int lkr = 1; lkr <= lkrmax; lkr++) {
+            int l = krl[lkr - 1];
+            cplx x = rl[(k - 1) + (long)(l - 1) * nsp];
+            if (cabs_(x) > thres) sk_add(f, (kkr - 1) * nkr + lkr, x);
+        }
+    }
+    if ((ityp == 1 && ikr != jkr) || ityp == 4) {
+        for (int kkr = 1; kkr <= kkrmax; kkr++) {
+            int k = krk[kkr - 1];
+            int lkrmax = kkr;
+            if (ityp <= 3 && ikr == kkr) lkrmax = jkr;
+            if (lkrmax == kkr) lkrmax = lkrmax - 1;
+            for (int lkr = 1; lkr <= lkrmax; lkr++) {
+                int l = krl[lkr - 1];
+                cplx x = rl[(l - 1) + (long)(k - 1) * nsp];
+                if (cabs_(x) > thres) sk_add(f, (lkr - 1) * nkr + kkr, x);
+            }
+        }
+    }
+    *nskel += f->r[f->nr - 1].nz;
+}
+
+/* OUTPP2 (source/rotran/outpp2.F:117-255): pp-interchanged integrals,
+ * bucketed on KKR. */
+static void outpp2(int nkr, int nsp, int ityp, pplist* bk, double thres, const int* krk,
+                   const int* krl, int ikr, int jkr, const cplx* rl) {
+    int ij = (ikr - 1) * nkr + jkr;
+    int kkrmin = (ityp == 4) ? 1 : ikr;
+    for (int kkr = kkrmin; kkr <= nkr; kkr++) {
+        int k = krk[kkr - 1];
+        int lkrmin = 1;
+        if (ityp <= 3 && ikr == kkr) lkrmin = jkr;
+        for (int lkr = lkrmin; lkr <= kkr; lkr++) {
+            int l = krl[lkr - 1];
+            cplx x = rl[(k - 1) + (long)(l - 1) * nsp];
+            if (cabs_(x) > thres) pp_push(&bk[kkr], lkr, ij, x);
+        }
+    }
+    int ji = (jkr - 1) * nkr + ikr;
+    if (ityp == 2 || ityp == 3) return;
+    if (ityp == 1) {
+        if (ikr == jkr) return;
+        for (int kkr = kkrmin; kkr <= nkr; kkr++) {
+            int k = krk[kkr - 1];
+            int lkrmin = 1;
+            if (ikr == kkr) lkrmin = jkr;
+            for (int lkr = lkrmin; lkr <= kkr - 1; lkr++) {
+                int l = krl[lkr - 1];
+                cplx x = rl[(l - 1) + (long)(k - 1) * nsp];
+                if (cabs_(x) > thres) pp_push(&bk[kkr], lkr, ji, cconj(x));
+            }
+        }
+    } else { /* ityp == 4 */
+        if (ikr == jkr) return; /* deviation (3) in the file header */
+        for (int kkr = 1; kkr <= nkr; kkr++) {
+            int k = krk[kkr - 1];
+            for (int lkr = 1; lkr <= kkr - 1; lkr++) {
+                int l = krl[lkr - 1];
+                cplx x = rl[(l - 1) + (long)(k - 1) * nsp];
+                if (cabs_(x) > thres) pp_push(&bk[kkr], lkr, ji, cconj(x));
+            }
+        }
+    }
+}
+
+/* Output record store. */
+typedef struct {
+    int* hdr;
+    long nrec, caprec;
+    int* idx;
+    double* val;
+    long nz, capnz;
+} mdstore;
+
+static void md_rec(mdstore* s, int a, int b) {
+    if (s->nrec == s->caprec) {
+        s->caprec = s->caprec ? 2 * s->caprec : 256;
+        s->hdr = (int*)realloc(s->hdr, sizeof(int) * 3 * s->caprec);
+    }
+    s->hdr[3 * s->nrec] = a;
+    s->hdr[3 * s->nrec + 1] = b;
+    s->hdr[3 * s->nrec + 2] = 0;
+    s->nrec++;
+}
+
+static void md_ent(mdstore* s, int k, int l, cplx v) {
+    if (s->nz == s->capnz) {
+        s->capnz = s->capnz ? 2 * s->capnz : 4096;
+        s->idx = (int*)realloc(s->idx, sizeof(int) * 2 * s->capnz);
+        s->val = (double*)realloc(s->val, sizeof(double) * 2 * s->capnz);
+    }
+    s->idx[2 * s->nz] = k;
+    s->idx[2 * s->nz + 1] = l;
+    s->val[2 * s->nz] = v.re;
+    s->val[2 * s->nz + 1] = v.im;
+    s->nz++;
+    s->hdr[3 * (s->nrec - 1) + 2]++;
+}
+
+/* PPSYM (source/rotran/ppsym.F:1-118), with its NC2-slot buffering. */
+static long ppsym(const skfile* f, const pplist* bk, int nsksiz, int nc2, int nkr, int is,
+                  int js, int ks, int ls, double throut, mdstore* out) {
+    long nfinal = 0;
+    long kk = (long)nkr * nkr;
+    cplx* cb2 = (cplx*)calloc((size_t)(nc2 + 2) * kk, sizeof(cplx)); /* slots 1..nc2(+1) */
+    int* jkrind = (int*)calloc(nkr + 1, sizeof(int));
+    int* icind = (int*)calloc(nc2 + 2, sizeof(int));
+    long* perm = NULL;
+    long permcap = 0;
+    int ic2 = 1, ikrc = 0, jkrn = 0;
+    for (long ir = 0; ir <= f->nr; ir++) {
+        int ikr, jkr, nz;
+        long off;
+        if (ir < f->nr) {
+            ikr = f->r[ir].ikr; jkr = f->r[ir].jkr; nz = f->r[ir].nz; off = f->r[ir].off;
+        } else {
+            ikr = 0; jkr = 0; nz = 0; off = 0; /* OUTPP3 terminator (outpp3.F:266) */
+        }
+        if (ic2 == 1) ikrc = ikr;
+        for (int z = 0; z < nz; z++) cb2[(long)ic2 * kk + f->kl[off + z] - 1] = f->v[off + z];
+        if (ic2 < nc2 && ikrc == ikr) {
+            jkrind[jkr] = ic2;
+            icind[ic2] = jkr;
+        } else {
+            if (ikr != ikrc) {
+                jkrn = jkr;
+                ic2 = ic2 - 1;
+            } else {
+                jkrind[jkr] = ic2;
+                icind[ic2] = jkr;
+            }
+            /* chain of pp-interchanged integrals for IKRC, newest first */
+            if (ikrc >= 1 && ikrc <= nkr) {
+                const pplist* l = &bk[ikrc];
+                if (l->n > permcap) {
+                    permcap = l->n;
+                    perm = (long*)realloc(perm, sizeof(long) * permcap);
+                }
+                chunk_reverse_order(l->n, nsksiz, perm);
+                for (long x = 0; x < l->n; x++) {
+                    const ppent* e = &l->e[perm[x]];
+                    if (jkrind[e->lkr] != 0) {
+                        long p = (long)jkrind[e->lkr] * kk + e->ij - 1;
+                        cb2[p] = cadd(cb2[p], e->v);
+                    }
+                }
+            }
+            for (int jc2 = 1; jc2 <= ic2; jc2++) {
+                int jkra = icind[jc2];
+                md_rec(out, ikrc * is, jkra * js);
+                long ix = 0;
+                for (int kkr = 1; kkr <= nkr; kkr++)
+                    for (int lkr = 1; lkr <= nkr; lkr++) {
+                        cplx v = cb2[(long)jc2 * kk + ix];
+                        ix++;
+                        if (cabs_(v) > throut) md_ent(out, kkr * ks, lkr * ls, v);
+                    }
+                nfinal += out->hdr[3 * (out->nrec - 1) + 2];
+            }
+            if (ikr != ikrc) {
+                memcpy(&cb2[1 * kk], &cb2[(long)(ic2 + 1) * kk], sizeof(cplx) * kk);
+                memset(&cb2[2 * kk], 0, sizeof(cplx) * kk * ic2);
+                memset(jkrind, 0, sizeof(int) * (nkr + 1));
+                memset(icind, 0, sizeof(int) * (nc2 + 2));
+                ic2 = 1;
+                icind[ic2] = jkrn;
+                jkrind[jkrn] = ic2;
+                ikrc = ikr;
+            } else {
+                memset(&cb2[1 * kk], 0, sizeof(cplx) * kk * ic2);
+                memset(jkrind, 0, sizeof(int) * (nkr + 1));
+                memset(icind, 0, sizeof(int) * (nc2 + 2));
+                ic2 = 0;
+            }
+        }
+        ic2 = ic2 + 1;
+    }
+    free(cb2);
+    free(jkrind);
+    free(icind);
+    free(perm);
+    return nfinal;
+}
+
+/* MAKIND's Coulomb selection of pq blocks (makind.F:235-255) for C1. */
+static int pq_included(int p, int q, int nsc1, int mfil) {
+    if (p > nsc1 && q <= nsc1) return 0;
+    if (p > nsc1 && mfil < 3) return 0;
+    return 1;
+}
+
+int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const int* kra,
+            const int* krb, const int* ikrmo, long nrec, const int* rec_file, const int* rec_it,
+            const long* rec_nt, const double* rint, const int* label2, const int* label1,
+            orc_result* out) {
+    memset(out, 0, sizeof(*out));
+    const int n = prm->nsc, nsc1 = prm->nsc1, m = prm->nsp, nkr = prm->nkr;
+    if (n <= 0 || m != 2 * nkr || nsc1 < 0 || nsc1 > n || n > 65535) return 2;
+    const cplx* qa = (const cplx*)qa_in; /* QA(p,i) = qa[p + i*n], 0-based */
+#define QA(p, i) qa[(p) + (long)(i) * n]
+#ifdef _OPENMP
+    if (prm->nthreads > 0) omp_set_num_threads(prm->nthreads);
+#endif
+    double t0 = now_s();
+    const long nsctr = (long)n * (n + 1) / 2;
+    const int nji = nkr * (nkr + 1);
+
+    /* VMX (getmos.F:417-423) */
+    double* vmx = (double*)calloc(n, sizeof(double));
+    for (int p = 0; p < n; p++) {
+        double a = 0.0;
+        for (int i = 0; i < m; i++) {
+            double b = cabs_(QA(p, i));
+            if (a < b) a = b;
+        }
+        vmx[p] = a;
+    }
+
+    /* ---------------- SORT1 (sort1.F:118-221) ---------------- */
+    long* cnt = (long*)calloc(nsctr + 1, sizeof(long));
+    long nincl = 0;
+    for (int p = 1; p <= n; p++)
+        for (int q = 1; q <= p; q++) nincl += pq_included(p, q, nsc1, prm->mfil);
+    long off = 0;
+    for (long r = 0; r < nrec; r++) {
+        if (rec_file[r] < 1 || rec_file[r] > prm->mfil) { off += rec_nt[r]; continue; }
+        for (long x = off; x < off + rec_nt[r]; x++) {
+            int ip = (label1[x] >> 16) & 0xFFFF, iq = label1[x] & 0xFFFF;
+            if (ip < 1 || iq < 1 || ip > n || iq > ip) { free(cnt); free(vmx); return 3; }
+            if (!pq_included(ip, iq, nsc1, prm->mfil)) continue;
+            cnt[(long)ip * (ip - 1) / 2 + iq]++;
+        }
+        off += rec_nt[r];
+    }
+    long* bstart = (long*)calloc(nsctr + 2, sizeof(long));
+    for (long pq = 1; pq <= nsctr; pq++) bstart[pq + 1] = bstart[pq] + cnt[pq];
+    long ntot = bstart[nsctr + 1];
+    double* gval = (double*)malloc(sizeof(double) * (ntot ? ntot : 1));
+    int* gr = (int*)malloc(sizeof(int) * (ntot ? ntot : 1));
+    int* gs = (int*)malloc(sizeof(int) * (ntot ? ntot : 1));
+    memset(cnt, 0, sizeof(long) * (nsctr + 1));
+    off = 0;
+    for (long r = 0; r < nrec; r++) {
+        if (rec_file[r] < 1 || rec_file[r] > prm->mfil) { off += rec_nt[r]; continue; }
+        double fac = orc_gettw_factor(rec_it[r]);
+        for (long x = off; x < off + rec_nt[r]; x++) {
+            int ip = (label1[x] >> 16) & 0xFFFF, iq = label1[x] & 0xFFFF;
+            if (!pq_included(ip, iq, nsc1, prm->mfil)) continue;
+            int ir = (label2[x] >> 16) & 0xFFFF, is = label2[x] & 0xFFFF;
+            if (ir < 1 || is < 1 || ir > n || is > n) { free(cnt); return 3; }
+            long pq = (long)ip * (ip - 1) / 2 + iq;
+            long slot = bstart[pq] + cnt[pq]++;
+            gval[slot] = rint[x] * fac;
+            gr[slot] = ir > is ? ir : is; /* sort1.F:167-170 */
+            gs[slot] = ir > is ? is : ir;
+        }
+        off += rec_nt[r];
+    }
+    free(cnt);
+
+    int nijsiz, nsksiz[4], nc2;
+    ref_buffer_sizes(n, nkr, m, (int)(nincl < 16384 ? nincl : 16384), &nijsiz, nsksiz, &nc2);
+
+    /* ---------------- TRANS1 (trans1.F:48-103) ---------------- */
+    long pq_limit = prm->limit_pq > 0 ? prm->limit_pq : nsctr;
+    cplx* hstore = (cplx*)calloc((size_t)nsctr * nji, sizeof(cplx));
+    unsigned char* hkeep = (unsigned char*)calloc((size_t)nsctr * nji, 1);
+    long npq_done = 0;
+    {
+        long* pqlist = (long*)malloc(sizeof(long) * (nsctr + 1));
+        long npql = 0;
+        for (long pq = 1; pq <= nsctr && npql < pq_limit; pq++)
+            if (bstart[pq + 1] > bstart[pq]) pqlist[npql++] = pq;
+        npq_done = npql;
+#pragma omp parallel
+        {
+            cplx* ha = (cplx*)malloc(sizeof(cplx) * (size_t)n * m);
+            cplx* ri = (cplx*)malloc(sizeof(cplx) * (size_t)m * m);
+            cplx* ria = (cplx*)malloc(sizeof(cplx) * (size_t)m * m);
+            long* perm = (long*)malloc(sizeof(long) * 16);
+            long permcap = 16;
+#pragma omp for schedule(dynamic, 1)
+            for (long t = 0; t < npql; t++) {
+                long pq = pqlist[t];
+                int ip = (int)(0.5 + 0.5 * sqrt((double)(8 * pq - 7)));
+                while ((long)ip * (ip - 1) / 2 >= pq) ip--;
+                while ((long)(ip + 1) * ip / 2 < pq) ip++;
+                int iq = (int)(pq - (long)ip * (ip - 1) / 2);
+                long nb = bstart[pq + 1] - bstart[pq];
+                if (nb > permcap) { permcap = nb; perm = (long*)realloc(perm, sizeof(long) * permcap); }
+                chunk_reverse_order(nb, 512, perm); /* GETSTI read order, NPQSIZ=512 */
+                /* MATMUL1 (matmul1.F:108-138) */
+                memset(ha, 0, sizeof(cplx) * (size_t)n * m);
+                for (long x = 0; x < nb; x++) {
+                    long e = bstart[pq] + perm[x];
+                    int r = gr[e] - 1, s = gs[e] - 1;
+                    double g = gval[e];
+                    for (int i = 0; i < m; i++) {
+                        cplx* h = &ha[r + (long)i * n];
+                        cplx b = QA(s, i);
+                        h->re += g * b.re;
+                        h->im += g * b.im;
+                    }
+                }
+                /* ZGEMM('C','N',NSP,NSP,NSC): RI = QA^H * HA (trans1.F:71-75) */
+                for (int j = 0; j < m; j++)
+                    for (int i = 0; i < m; i++) {
+                        cplx tmp = {0.0, 0.0};
+                        for (int l = 0; l < n; l++) tmp = cadd(tmp, cmul(cconj(QA(l, i)), ha[l + (long)j * n]));
+                        ri[i + (long)j * m] = tmp;
+                    }
+                /* MTIMHER(RIA,RI,+1) (mtimher.F:141-164) */
+                for (int i = 1; i <= m; i++)
+                    for (int j = 1; j <= m; j++) {
+                        int itr = abs(itrmo[i - 1]), jtr = abs(itrmo[j - 1]);
+                        int sg = (itrmo[i - 1] * itrmo[j - 1] >= 0) ? 1 : -1;
+                        cplx a = ri[(j - 1) + (long)(i - 1) * m];
+                        cplx b = ri[(itr - 1) + (long)(jtr - 1) * m];
+                        cplx c = cconj(ri[(i - 1) + (long)(j - 1) * m]);
+                        cplx d = cconj(ri[(jtr - 1) + (long)(itr - 1) * m]);
+                        cplx h = cadd(cadd(cadd(a, cscal(sg, b)), c), cscal(sg, d));
+                        ria[(j - 1) + (long)(i - 1) * m] = h;
+                    }
+                /* TROUT (trout.F:165-227) */
+                double thrsh = vmx[ip - 1] * vmx[iq - 1];
+                if (thrsh < prm->thrgen) continue;
+                thrsh = prm->thrgen / thrsh;
+                int ji = 0;
+                for (int ibar = 1; ibar <= 2; ibar++)
+                    for (int ik = 1; ik <= nkr; ik++) {
+                        int i = (ibar == 1) ? kra[ik - 1] : krb[ik - 1];
+                        for (int jk = ik; jk <= nkr; jk++) {
+                            int j = krb[jk - 1];
+                            ji++;
+                            cplx h = ria[(j - 1) + (long)(i - 1) * m];
+                            if (cabs_(h) < thrsh) continue;
+                            hstore[(pq - 1) * nji + (ji - 1)] = h;
+                            hkeep[(pq - 1) * nji + (ji - 1)] = 1;
+                        }
+                    }
+            }
+            free(ha); free(ri); free(ria); free(perm);
+        }
+        free(pqlist);
+    }
+    /* bucket lists per JI in pq order (INTTWO chains) */
+    long* jcnt = (long*)calloc(nji + 2, sizeof(long));
+    for (long pq = 1; pq <= nsctr; pq++)
+        for (int ji = 0; ji < nji; ji++) jcnt[ji + 2] += hkeep[(pq - 1) * nji + ji];
+    for (int ji = 0; ji <= nji; ji++) jcnt[ji + 1] += jcnt[ji];
+    long nhalft = jcnt[nji + 1];
+    cplx* hval = (cplx*)malloc(sizeof(cplx) * (nhalft ? nhalft : 1));
+    int* hp = (int*)malloc(sizeof(int) * (nhalft ? nhalft : 1));
+    int* hq = (int*)malloc(sizeof(int) * (nhalft ? nhalft : 1));
+    {
+        long* fill = (long*)calloc(nji + 1, sizeof(long));
+        for (long pq = 1; pq <= nsctr; pq++) {
+            int ip = (int)(0.5 + 0.5 * sqrt((double)(8 * pq - 7)));
+            while ((long)ip * (ip - 1) / 2 >= pq) ip--;
+            while ((long)(ip + 1) * ip / 2 < pq) ip++;
+            int iq = (int)(pq - (long)ip * (ip - 1) / 2);
+            for (int ji = 0; ji < nji; ji++) {
+                if (!hkeep[(pq - 1) * nji + ji]) continue;
+                long s = jcnt[ji + 1] + fill[ji]++;
+                hval[s] = hstore[(pq - 1) * nji + ji];
+                hp[s] = ip;
+                hq[s] = iq;
+            }
+        }
+        free(fill);
+    }
+    free(hstore);
+    free(hkeep);
+    double t1 = now_s();
+
+    /* ---------------- TRANS2 (trans2.F:68-326), one quaternionic irrep ---------------- */
+    typedef struct { int i, j; } item;
+    item* items = (item*)malloc(sizeof(item) * (size_t)m * m);
+    long nitems = 0;
+    for (int moi = 1; moi <= m; moi++)
+        for (int moj = 1; moj <= m; moj++) {
+            int ikr = ikrmo[moi - 1], jkr = ikrmo[moj - 1];
+            if (abs(ikr) < abs(jkr)) continue; /* trans2.F:239 */
+            if (ikr > 0) continue;             /* deviation (2) in the file header */
+            items[nitems].i = moi;
+            items[nitems].j = moj;
+            nitems++;
+        }
+    long ij_limit = prm->limit_ij > 0 ? prm->limit_ij : nitems;
+    if (ij_limit > nitems) ij_limit = nitems;
+    skfile sk[4];
+    memset(sk, 0, sizeof(sk));
+    pplist* bk[4];
+    for (int c = 0; c < 4; c++) bk[c] = (pplist*)calloc(nkr + 1, sizeof(pplist));
+    long nskel = 0;
+    long maxmrj = 1;
+    for (int ji = 0; ji < nji; ji++)
+        if (jcnt[ji + 2] - jcnt[ji + 1] > maxmrj) maxmrj = jcnt[ji + 2] - jcnt[ji + 1];
+    const long BATCH = 64;
+    cplx* rlb = (cplx*)malloc(sizeof(cplx) * (size_t)BATCH * m * m);
+    for (long b0 = 0; b0 < ij_limit; b0 += BATCH) {
+        long b1 = b0 + BATCH < ij_limit ? b0 + BATCH : ij_limit;
+#pragma omp parallel
+        {
+            cplx* rj = (cplx*)malloc(sizeof(cplx) * maxmrj);
+            cplx* rk = (cplx*)malloc(sizeof(cplx) * (size_t)n * m);
+            cplx* rlr = (cplx*)malloc(sizeof(cplx) * (size_t)m * m);
+            long* perm = (long*)malloc(sizeof(long) * 16);
+            long permcap = 16;
+#pragma omp for schedule(dynamic, 1)
+            for (long t = b0; t < b1; t++) {
+                int I = items[t].i, J = items[t].j;
+                cplx* rl = &rlb[(t - b0) * (long)m * m];
+                int ji, conjug, is;
+                unique_(nkr, ikrmo, I, J, &ji, &conjug, &is);
+                long s0 = jcnt[ji], mrj = jcnt[ji + 1] - jcnt[ji];
+                if (mrj == 0) { /* GETHTI found nothing: REDME stays zero */
+                    memset(rl, 0, sizeof(cplx) * (size_t)m * m);
+                    continue;
+                }
+                if (mrj > permcap) { permcap = mrj; perm = (long*)realloc(perm, sizeof(long) * permcap); }
+                chunk_reverse_order(mrj, nijsiz, perm); /* GETHTI read order */
+                for (long x = 0; x < mrj; x++) {
+                    cplx v = hval[s0 + perm[x]];
+                    if (conjug) v = cconj(v);
+                    if (is < 0) v = cscal(-1.0, v);
+                    rj[x] = v;
+                }
+                /* MATMUL3 (matmul3.F:53-84) */
+                memset(rk, 0, sizeof(cplx) * (size_t)n * m);
+                for (long x = 0; x < mrj; x++) {
+                    long e = s0 + perm[x];
+                    int p = hp[e] - 1, q = hq[e] - 1;
+                    cplx a = rj[x];
+                    for (int k = 0; k < m; k++) {
+                        rk[p + (long)k * n] = cadd(rk[p + (long)k * n], cmul(a, QA(q, k)));
+                        rk[q + (long)k * n] = cadd(rk[q + (long)k * n], cmul(a, QA(p, k)));
+                    }
+                }
+                /* ZGEMM('C','N') RLR = QA^H RK (trans2.F:116-118) */
+                for (int j = 0; j < m; j++)
+                    for (int i = 0; i < m; i++) {
+                        cplx tmp = {0.0, 0.0};
+                        for (int l = 0; l < n; l++) tmp = cadd(tmp, cmul(cconj(QA(l, i)), rk[l + (long)j * n]));
+                        rlr[i + (long)j * m] = tmp;
+                    }
+                /* MSUMTIM(RL,RLR,+1) (msumtim.F:87-105) */
+                for (int i = 1; i <= m; i++)
+                    for (int j = 1; j <= m; j++) {
+                        int itr = abs(itrmo[i - 1]), jtr = abs(itrmo[j - 1]);
+                        int sg = (itrmo[i - 1] * itrmo[j - 1] >= 0) ? 1 : -1;
+                        rl[(j - 1) + (long)(i - 1) * m] =
+                            cadd(rlr[(j - 1) + (long)(i - 1) * m], cscal(sg, rlr[(itr - 1) + (long)(jtr - 1) * m]));
+                    }
+                /* the reduced-matrix-element gather/scatter (trans2.F:199-265)
+                 * is the identity for a single one-dimensional irrep */
+            }
+            free(rj); free(rk); free(rlr); free(perm);
+        }
+        /* OUTPP1 / OUTPP2 in TRANS2's loop order (trans2.F:272-310) */
+        for (long t = b0; t < b1; t++) {
+            int I = items[t].i, J = items[t].j;
+            int ikra = abs(ikrmo[I - 1]), jkr = ikrmo[J - 1], jkra = abs(jkr);
+            cplx* rl = &rlb[(t - b0) * (long)m * m];
+            long mm = (long)m * m;
+            if (jkr < 0) {
+                outpp1(nkr, m, 1, &sk[0], prm->throut, krb, krb, ikra, jkra, rl, &nskel);
+                outpp2(nkr, m, 1, bk[0], prm->throut, krb, krb, ikra, jkra, rl);
+                if (prm->quater) {
+                    for (long x = 0; x < mm; x++) rl[x] = cscal(-1.0, cconj(rl[x])); /* CJNVEC */
+                    outpp2(nkr, m, 4, bk[3], prm->throut, kra, krb, ikra, jkra, rl);
+                    for (long x = 0; x < mm; x++) rl[x] = cscal(-1.0, cconj(rl[x]));
+                }
+            } else {
+                outpp1(nkr, m, 2, &sk[1], prm->throut, krb, kra, ikra, jkra, rl, &nskel);
+                outpp2(nkr, m, 2, bk[1], prm->throut, krb, kra, ikra, jkra, rl);
+                outpp1(nkr, m, 3, &sk[2], prm->throut, kra, krb, ikra, jkra, rl, &nskel);
+                for (long x = 0; x < mm; x++) rl[x] = cconj(rl[x]); /* CJVEC */
+                outpp2(nkr, m, 3, bk[2], prm->throut, kra, krb, ikra, jkra, rl);
+                for (long x = 0; x < mm; x++) rl[x] = cconj(rl[x]);
+                if (prm->quater) outpp1(nkr, m, 4, &sk[3], prm->throut, kra, kra, ikra, jkra, rl, &nskel);
+            }
+        }
+    }
+    free(rlb);
+    for (int c = 0; c < 4; c++)
+        for (int k = 0; k <= nkr; k++) nskel += bk[c][k].n;
+    double t2 = now_s();
+
+    /* ---------------- PPSYM x3 (x4) (rotran.F:305-331) ---------------- */
+    mdstore md;
+    memset(&md, 0, sizeof(md));
+    static const int sgn[4][4] = {{-1, -1, -1, -1}, {-1, 1, -1, 1}, {-1, 1, 1, -1}, {-1, 1, 1, 1}};
+    int ncls = prm->quater ? 4 : 3;
+    for (int c = 0; c < ncls; c++)
+        out->nfinal[c] = ppsym(&sk[c], bk[c], nsksiz[c], nc2, nkr, sgn[c][0], sgn[c][1], sgn[c][2],
+                               sgn[c][3], prm->throut, &md);
+    double t3 = now_s();
+
+    for (int c = 0; c < 4; c++) {
+        free(sk[c].r); free(sk[c].kl); free(sk[c].v);
+        for (int k = 0; k <= nkr; k++) free(bk[c][k].e);
+        free(bk[c]);
+    }
+    free(items); free(hval); free(hp); free(hq); free(jcnt);
+    free(gval); free(gr); free(gs); free(bstart); free(vmx);
+
+    out->nrec = md.nrec;
+    out->hdr = md.hdr;
+    out->nz_total = md.nz;
+    out->idx = md.idx;
+    out->val = md.val;
+    out->nhalft = nhalft;
+    out->nskel = nskel;
+    out->npq_done = npq_done;
+    out->nij_done = ij_limit;
+    out->nij_total = nitems;
+    out->t_first = t1 - t0;
+    out->t_second = t2 - t1;
+    out->t_pp = t3 - t2;
+    out->nijsiz = nijsiz;
+    out->nc2 = nc2;
+#undef QA
+    return 0;
+}
+
+void orc_free(orc_result* r) {
+    free(r->hdr);
+    free(r->idx);
+    free(r->val);
+    memset(r, 0, sizeof(*r));
+}
