@@ -1,0 +1,159 @@
+/*
+ * rotran_gb300.h -- C-ABI of the GB300 (sm_103a) implementation of MOLFDIR
+ * rotran's Coulomb four-index transformation.
+ *
+ * The calls replace, inside a rotran driver, the sequence
+ *   SR2INI / SORT1 / TRANS1 / SR2FLSH / TRANS2 / INITTWOE / PPSYM / EXITTWOE
+ * of source/rotran/rotran.F:236-333.  The host keeps INIT, READIN, GETMOS
+ * and COMSYM (rotran.F:42-45) and hands over the data those routines leave
+ * in COMMON blocks: the spinor coefficients QA (/VECS/, vecs.inc:7), the
+ * Kramers tables ITRMO/KRA/KRB/IKRMO (/REORD/, vecs.inc:11-12), the MDCINT
+ * header orbital pairs, the /INPT/ sizes and the /TRES/ thresholds.
+ *
+ * Conventions
+ *  - Every array is borrowed for the duration of the call only; the library
+ *    copies what it needs.  A context owns its device memory and one CUDA
+ *    stream and must not be shared between threads.
+ *  - Complex numbers are two consecutive doubles (re, im), the memory layout
+ *    of Fortran COMPLEX*16; matrices are column-major (Fortran order).
+ *  - Spinor, AO and Kramers-pair indices are 1-based, as in the reference.
+ *  - Every call returns an int status: 0 for success, otherwise the error
+ *    class of Q2JOB (source/general/q2job.F:8-23) that the reference would
+ *    have stopped with; rt_last_error() gives the message.  Nothing aborts
+ *    inside the library and no call falls back to a CPU path: without a
+ *    usable sm_103a device, rt_create fails with RT_ERR_PROGRAM.
+ */
+#ifndef ROTRAN_GB300_H
+#define ROTRAN_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes = Q2JOB classes (q2job.F:8-23) */
+#define RT_OK 0
+#define RT_ERR_EOF 1      /* missing or truncated input data */
+#define RT_ERR_USER 2     /* inconsistent input */
+#define RT_ERR_DIM 3      /* a size exceeds what the library supports */
+#define RT_ERR_INTERNAL 4 /* internal dimension error */
+#define RT_ERR_MISMATCH 5 /* non-matching parameters between calls */
+#define RT_ERR_PROGRAM 6  /* any other failure (CUDA error, Kramers check) */
+
+#define RT_PREC_FP64 0       /* plain FP64 arithmetic on the CUDA cores */
+#define RT_PREC_SPLIT_BF16 1 /* BF16 slices on the tensor cores, FP64 recombination */
+
+typedef struct rt_ctx rt_ctx;
+
+/* Sizes and options: /INPT/ (inpt.inc:1-8), /TRES/ (thres.inc:1-2). */
+typedef struct rt_config {
+    int nsc;          /* NSC: scalar AO functions transformed */
+    int nsc1;         /* NSC1: large-component functions, 1..NSC1; S = NSC1+1..NSC */
+    int nsp;          /* NSP: active spinors */
+    int nkr;          /* NKR: Kramers pairs, NSP = 2*NKR */
+    int mfil;         /* MFIL: SRT files read (1 LL, 2 +SS|LL, 3 +SS|SS), readin.F:83-84 */
+    int breit;        /* BREIT: must be 0 (Coulomb); Gaunt is not implemented */
+    double thrgen;    /* THRGEN (readin.F:93) */
+    double throut;    /* THROUT (readin.F:94): |x| > THROUT is written to MDCINT */
+    int precision;    /* RT_PREC_FP64 or RT_PREC_SPLIT_BF16 */
+    int slices;       /* split path: BF16 slices per operand, 2..8 (0: default 7) */
+    int n_irrep;      /* 1, or 4: AO functions carry the labels in ao_irrep and
+                         (pq|rs) vanishes unless irr(p)^irr(q) == irr(r)^irr(s) */
+    const int* ao_irrep; /* NSC labels 0..n_irrep-1 (NULL when n_irrep == 1) */
+    long long mem_budget; /* device bytes the context may use (0: 90% of free) */
+} rt_config;
+
+typedef struct rt_stats {
+    long long nhalft;       /* half-transformed values kept by the THRGEN screen */
+    long long nfinal[4];    /* MDCINT elements per class (NFINAL1..4, rotran.F:345) */
+    long long nrec[4];      /* MDCINT records per class */
+    double ms_upload, ms_scatter, ms_first, ms_second, ms_output, ms_total;
+    double flops_algorithmic; /* algorithmic FLOPs of the transform (dense-block count) */
+    long long device_bytes;   /* peak device memory held by the context */
+    int gpu_launches;         /* kernels launched by the last rt_transform */
+} rt_stats;
+
+/* Sizes of a transformation, computed on the host without a device: the
+ * pq blocks transformed (makind.F:223-277), device bytes of the main arrays,
+ * MDCINT records and an upper bound of their elements per class. */
+typedef struct rt_plan_info {
+    long long npairs;          /* pq blocks transformed */
+    long long nitems;          /* Kramers-unique spinor pairs, NKR*(NKR+1) */
+    long long g3_bytes;        /* AO integrals expanded to G_pq(r,s) */
+    long long hp_bytes;        /* half-transformed integrals */
+    long long nrec[4];         /* MDCINT records per class */
+    long long elem_cap[4];     /* upper bound of MDCINT elements per class */
+    double flops_algorithmic;  /* algorithmic FLOPs (dense-block count) */
+} rt_plan_info;
+
+int rt_plan(const rt_config* cfg, rt_plan_info* out);
+
+/* Create a context on the current CUDA device (replaces the work-array set-up
+ * of rotran.F:74-231).  Fails with RT_ERR_PROGRAM if no sm_103a device. */
+int rt_create(rt_ctx** out, const rt_config* cfg);
+
+/* Spinor coefficients and Kramers tables (GETMOS, getmos.F:191-430;
+ * KRAMERS, kramers.F:3-165).  qa: QA(ld_qa, NSP) COMPLEX*16, rows 1..NSC
+ * used; itrmo/ikrmo: NSP entries; kra/krb: NKR spinor indices of the
+ * unbarred/barred member of each pair; imoras_pairs: 2*NKR orbital numbers
+ * written to the MDCINT header (inittwoe.F:139-141). */
+int rt_set_coefficients(rt_ctx* ctx, const double* qa, int ld_qa, const int* itrmo,
+                        const int* kra, const int* krb, const int* ikrmo,
+                        const int* imoras_pairs);
+
+/* One SRTTW/SRTLB record pair as GETTW reads it (gettw.F:15-29): nt unscaled
+ * integrals of type itype from file file_class (1 = SRTTWLL, 2 = SRTTWSL
+ * (SS|LL), 3 = SRTTWSS); label2 = I<<16|K of the first pair, label1 =
+ * L<<16|N of the second (the pq bucket of sort1.F:136-142).  Records of
+ * files above MFIL are accepted and ignored, as SORT1 does not read them. */
+int rt_add_ao_records(rt_ctx* ctx, int file_class, int nt, int itype, const double* rint,
+                      const int* label2, const int* label1);
+
+/* Many records at once: nrec records, record r holds nt[r] integrals of
+ * type itype[r] from file file_class[r]; rint/label2/label1 are the records
+ * concatenated. */
+int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* file_class, const long long* nt,
+                           const int* itype, const double* rint, const int* label2,
+                           const int* label1);
+
+/* Read SRTTWLL/SRTLBLL, SRTTWSL/SRTLBSL, SRTTWSS/SRTLBSS (gfortran
+ * sequential unformatted, 4-byte markers) from directory dir, files
+ * 1..MFIL, as SORT1 does (sort1.F:118-205). */
+int rt_read_srt_files(rt_ctx* ctx, const char* dir);
+
+/* Drop all records added so far (a new integral set, same sizes). */
+int rt_clear_ao_records(rt_ctx* ctx);
+
+/* Run the transformation: first half (TRANS1), sort/transpose, second half
+ * (TRANS2) and particle-particle completion (PPSYM); the MDCINT records stay
+ * in device memory until copied or written. */
+int rt_transform(rt_ctx* ctx);
+
+/* Sizes of the MDCINT record stream of the last transform (records without
+ * header and terminator; nz = total elements). */
+int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz);
+
+/* Copy the record stream: hdr[3*nrec] = (IKR*IS, JKR*JS, NZ) in file order
+ * (ppsym.F:89-91), idx[2*nz] = (INDK, INDL), val[2*nz] = (re, im). */
+int rt_copy_result(rt_ctx* ctx, int* hdr, int* idx, double* val);
+
+/* Write MDCINT (inittwoe.F:119-143, ppsym.F:89-91, exittwoe.F:144-153) as
+ * a gfortran sequential unformatted file. */
+int rt_write_mdcint(rt_ctx* ctx, const char* path, const char* datex10, const char* timex8);
+
+int rt_get_stats(rt_ctx* ctx, rt_stats* out);
+/* Message of the last failed call on ctx; with ctx == NULL, of the last
+ * failed rt_create or rt_plan of the calling thread. */
+const char* rt_last_error(rt_ctx* ctx);
+void rt_destroy(rt_ctx* ctx);
+
+/* KRAMERS pairing check (kramers.F:26-131) on host data: finds the
+ * time-reversal partner of every spinor (tolerance 1e-10), writes ITRMO and
+ * the largest deviation; returns RT_ERR_PROGRAM, like the reference's
+ * Q2JOB(6,...) stops, if a spinor has no partner or a partner needs a phase. */
+int rt_kramers_check(int nsc, int nsp, const double* qa, const double* qb, int ld, int* itrmo,
+                     double* difmax);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

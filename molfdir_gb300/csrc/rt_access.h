@@ -1,0 +1,10 @@
+// rt_access.h -- accessors the host-only translation units (plain C++,
+// no CUDA headers) use on the opaque context.
+#pragma once
+
+#include "../../include/rotran_gb300.h"
+
+int rt_internal_mfil(rt_ctx* c);
+int rt_internal_nkr(rt_ctx* c);
+const int* rt_internal_imoras(rt_ctx* c);
+void rt_internal_set_error(rt_ctx* c, const char* msg);

@@ -1,0 +1,948 @@
+// rt_api.cu -- C-ABI entry points, planning and orchestration of the
+// GB300 rotran transformation (replaces rotran.F:74-333).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "rt_internal.h"
+#include "rt_kernels.h"
+#include "rt_split.h"
+#include "rt_access.h"
+
+using namespace rt;
+
+namespace {
+
+template <class T>
+T* dalloc(rt_ctx* c, size_t count) {
+    if (count == 0) count = 1;
+    void* p = nullptr;
+    size_t bytes = count * sizeof(T);
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(RT_ERR_DIM, "device allocation of " + std::to_string(bytes) +
+                                    " bytes failed (" + cudaGetErrorString(e) + ")");
+    }
+    c->allocs.push_back({p, bytes});
+    c->dev_bytes += bytes;
+    c->dev_peak = std::max(c->dev_peak, c->dev_bytes);
+    return static_cast<T*>(p);
+}
+
+void dfree(rt_ctx* c, void* p) {
+    if (!p) return;
+    for (size_t i = 0; i < c->allocs.size(); ++i)
+        if (c->allocs[i].first == p) {
+            c->dev_bytes -= c->allocs[i].second;
+            c->allocs.erase(c->allocs.begin() + i);
+            break;
+        }
+    cudaFree(p);
+}
+
+template <class T>
+void upload(rt_ctx* c, T*& dst, const std::vector<T>& v) {
+    dfree(c, dst);
+    dst = dalloc<T>(c, v.size());
+    if (!v.empty())
+        RT_CUDA(cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+}
+
+void check_config(const rt_config* cfg) {
+    if (!cfg) throw Error(RT_ERR_USER, "null configuration");
+    if (cfg->nsc < 1 || cfg->nsc > 65535)
+        throw Error(RT_ERR_DIM, "NSC must be in 1..65535 (16-bit integral labels)");
+    if (cfg->nsc1 < 0 || cfg->nsc1 > cfg->nsc) throw Error(RT_ERR_USER, "NSC1 must be in 0..NSC");
+    if (cfg->nkr < 1 || cfg->nsp != 2 * cfg->nkr)
+        throw Error(RT_ERR_USER, "NSP must equal 2*NKR with NKR >= 1");
+    if (cfg->nkr > cfg->nsc) throw Error(RT_ERR_USER, "more Kramers pairs than scalar functions");
+    if (cfg->mfil < 1 || cfg->mfil > 3) throw Error(RT_ERR_USER, "MFIL must be 1, 2 or 3");
+    if (cfg->mfil == 1 && cfg->nsc != cfg->nsc1)
+        throw Error(RT_ERR_USER, "MFIL=1 transforms the large component only: NSC must equal NSC1");
+    if (cfg->breit) throw Error(RT_ERR_USER, "Breit (Gaunt) integrals are not implemented");
+    if (cfg->precision != RT_PREC_FP64 && cfg->precision != RT_PREC_SPLIT_BF16)
+        throw Error(RT_ERR_USER, "unknown precision");
+    if (cfg->slices != 0 && (cfg->slices < 2 || cfg->slices > 8))
+        throw Error(RT_ERR_USER, "slices must be 0 or 2..8");
+    if (cfg->n_irrep != 1 && cfg->n_irrep != 4) throw Error(RT_ERR_USER, "n_irrep must be 1 or 4");
+    if (cfg->n_irrep == 4) {
+        if (!cfg->ao_irrep) throw Error(RT_ERR_USER, "ao_irrep required when n_irrep == 4");
+        for (int p = 0; p < cfg->nsc; ++p)
+            if (cfg->ao_irrep[p] < 0 || cfg->ao_irrep[p] > 3)
+                throw Error(RT_ERR_USER, "AO irrep labels must be 0..3");
+    }
+}
+
+// AO blocks, pair groups and GEMM1 groups (the pq-block list of
+// makind.F:223-277 and the block structure of the integral files).
+void plan_ao(rt_ctx* c) {
+    Plan& P = c->plan;
+    const rt_config& cfg = c->cfg;
+    P.n = cfg.nsc;
+    P.nL = cfg.nsc1;
+    P.nS = cfg.nsc - cfg.nsc1;
+    P.m = cfg.nsp;
+    P.K = cfg.nkr;
+    const int nirr = cfg.n_irrep;
+    auto irr = [&](int p) { return nirr == 1 ? 0 : c->ao_irrep[p]; };
+    P.blk_start.clear(); P.blk_size.clear(); P.blk_comp.clear(); P.blk_irr.clear();
+    P.ao_sorted.assign(P.n, -1);
+    P.ao_block.assign(P.n, -1);
+    std::vector<int> ao_pos(P.n, 0);
+    int pos = 0;
+    for (int comp = 0; comp < 2; ++comp) {
+        int lo = comp == 0 ? 0 : P.nL, hi = comp == 0 ? P.nL : P.n;
+        for (int g = 0; g < nirr; ++g) {
+            int start = pos, cnt = 0;
+            for (int p = lo; p < hi; ++p)
+                if (irr(p) == g) {
+                    P.ao_sorted[p] = pos++;
+                    P.ao_block[p] = (int)P.blk_start.size();
+                    ao_pos[p] = cnt++;
+                }
+            if (cnt == 0) continue;
+            P.blk_start.push_back(start);
+            P.blk_size.push_back(cnt);
+            P.blk_comp.push_back(comp);
+            P.blk_irr.push_back(g);
+        }
+    }
+    P.nblk = (int)P.blk_start.size();
+    P.ncomp[0] = P.nL;
+    P.ncomp[1] = P.nS;
+    P.comp_off[0] = 0;
+    P.comp_off[1] = P.nL;
+    // pairs: LL always, SS when S functions exist (MFIL >= 2 then)
+    const long long ntri = (long long)P.n * (P.n + 1) / 2;
+    P.pair_of_orig.assign(ntri, -1);
+    struct PK { int cls, gamma; long long orig; int p, q; };
+    std::vector<PK> pk;
+    for (int p = 0; p < P.n; ++p)
+        for (int q = 0; q <= p; ++q) {
+            bool pl = p < P.nL, ql = q < P.nL;
+            if (pl != ql) continue;  // no SL blocks for Coulomb (makind.F:240)
+            pk.push_back({pl ? 0 : 1, irr(p) ^ irr(q), (long long)p * (p + 1) / 2 + q, p, q});
+        }
+    std::stable_sort(pk.begin(), pk.end(), [](const PK& a, const PK& b) {
+        if (a.cls != b.cls) return a.cls < b.cls;
+        if (a.gamma != b.gamma) return a.gamma < b.gamma;
+        return a.orig < b.orig;
+    });
+    P.P = (int)pk.size();
+    P.pair_p.resize(P.P);
+    P.pair_q.resize(P.P);
+    P.pgroups.clear();
+    for (int i = 0; i < P.P; ++i) {
+        P.pair_of_orig[pk[i].orig] = i;
+        P.pair_p[i] = pk[i].p;
+        P.pair_q[i] = pk[i].q;
+        if (P.pgroups.empty() || P.pgroups.back().cls != pk[i].cls || P.pgroups.back().gamma != pk[i].gamma)
+            P.pgroups.push_back({pk[i].cls, pk[i].gamma, i, 0});
+        P.pgroups.back().size++;
+    }
+    // GEMM1 groups: which r blocks meet each pair group, and their partner block
+    P.g1.clear();
+    long long base = 0;
+    for (int g = 0; g < (int)P.pgroups.size(); ++g) {
+        const PairGroup& pg = P.pgroups[g];
+        for (int rb = 0; rb < P.nblk; ++rb) {
+            int comp = P.blk_comp[rb];
+            bool present;
+            if (pg.cls == 0) present = comp == 0 || cfg.mfil >= 2;   // (LL|LL), (LL|SS)
+            else present = comp == 0 ? cfg.mfil >= 2 : cfg.mfil >= 3; // (SS|LL), (SS|SS)
+            if (!present) continue;
+            int kb = -1;
+            for (int b = 0; b < P.nblk; ++b)
+                if (P.blk_comp[b] == comp && P.blk_irr[b] == (P.blk_irr[rb] ^ pg.gamma)) kb = b;
+            if (kb < 0) continue;
+            P.g1.push_back({g, rb, kb, base});
+            base += (long long)P.blk_size[rb] * pg.size * P.blk_size[kb];
+        }
+    }
+    P.g3_doubles = base;
+    // expansion tables per component
+    for (int comp = 0; comp < 2; ++comp) {
+        int nc = P.ncomp[comp], off = P.comp_off[comp];
+        P.pidx[comp].assign((size_t)nc * nc, -1);
+        // sorted position -> reference index
+        std::vector<int> ref_of(P.n);
+        for (int p = 0; p < P.n; ++p) ref_of[P.ao_sorted[p]] = p;
+        for (int a = 0; a < nc; ++a)
+            for (int b = 0; b < nc; ++b) {
+                int p = ref_of[off + a], q = ref_of[off + b];
+                int hi = std::max(p, q), lo = std::min(p, q);
+                P.pidx[comp][(size_t)a * nc + b] = P.pair_of_orig[(long long)hi * (hi + 1) / 2 + lo];
+            }
+    }
+    (void)ao_pos;
+}
+
+// Size of the canonical element set of a record (see in_set in rt_kernels.cu).
+long long set_size(int cls, int i, int j, int K, bool all) {
+    if (all || cls == 3) return (long long)K * K;
+    long long rank = (long long)i * (i - 1) / 2 + j;
+    if (cls == 0) return i == j ? (long long)i * (i + 1) / 2 : 2 * rank - (i - 1);
+    return rank;
+}
+
+struct DeviceTabs {
+    unsigned char* pq_read;
+    int *pair_of_orig, *pair_group, *pg_start, *pg_size, *ao_block, *ao_pos, *blk_size, *g1_of,
+        *g1_kblk;
+    long long* g1_base;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// plan + tables that depend on the coefficients
+// ---------------------------------------------------------------------------
+static Work& W(rt_ctx* c) { return c->work; }
+
+// ---------------------------------------------------------------------------
+// device state
+// ---------------------------------------------------------------------------
+static void build_coef_device(rt_ctx* c) {
+    Plan& P = c->plan;
+    const int n = P.n, m = P.m;
+    // QA in sorted AO order, planar
+    std::vector<double> qr((size_t)n * m), qi((size_t)n * m);  // [sorted p][i]
+    for (int p = 0; p < n; ++p)
+        for (int i = 0; i < m; ++i) {
+            qr[(size_t)P.ao_sorted[p] * m + i] = c->qa[2 * ((size_t)p + (size_t)i * n)];
+            qi[(size_t)P.ao_sorted[p] * m + i] = c->qa[2 * ((size_t)p + (size_t)i * n) + 1];
+        }
+    // GEMM1 B: [s][plane*m + b]
+    std::vector<double> qap((size_t)n * 2 * m);
+    for (int s = 0; s < n; ++s)
+        for (int b = 0; b < m; ++b) {
+            qap[(size_t)s * 2 * m + b] = qr[(size_t)s * m + b];
+            qap[(size_t)s * 2 * m + m + b] = qi[(size_t)s * m + b];
+        }
+    // GEMM2/4 A: [(plane',a)][(plane,r)] = [[QAr^T, QAi^T], [-QAi^T, QAr^T]]
+    std::vector<double> qah((size_t)2 * m * 2 * n);
+    for (int a = 0; a < m; ++a)
+        for (int r = 0; r < n; ++r) {
+            double re = qr[(size_t)r * m + a], im = qi[(size_t)r * m + a];
+            qah[(size_t)a * 2 * n + r] = re;
+            qah[(size_t)a * 2 * n + n + r] = im;
+            qah[(size_t)(m + a) * 2 * n + r] = -im;
+            qah[(size_t)(m + a) * 2 * n + n + r] = re;
+        }
+    upload(c, c->d_qap, qap);
+    upload(c, c->d_qah, qah);
+    // GEMM3 B per component: [(plane,q)][(plane',k)] = [[QAr, QAi], [-QAi, QAr]]
+    for (int comp = 0; comp < 2; ++comp) {
+        int nc = P.ncomp[comp], off = P.comp_off[comp];
+        std::vector<double> q3((size_t)2 * nc * 2 * m);
+        for (int q = 0; q < nc; ++q)
+            for (int k = 0; k < m; ++k) {
+                double re = qr[(size_t)(off + q) * m + k], im = qi[(size_t)(off + q) * m + k];
+                q3[(size_t)q * 2 * m + k] = re;
+                q3[(size_t)q * 2 * m + m + k] = im;
+                q3[(size_t)(nc + q) * 2 * m + k] = -im;
+                q3[(size_t)(nc + q) * 2 * m + m + k] = re;
+            }
+        upload(c, c->d_qar[comp], q3);
+    }
+    // split path: slice the constant operands once
+    if (c->cfg.precision == RT_PREC_SPLIT_BF16) split_prepare_constants(c);
+}
+
+// items of TRANS2's loop (trans2.F:73-74,230-239), records, screening data
+static void plan_items(rt_ctx* c) {
+    Plan& P = c->plan;
+    Work& w = W(c);
+    const int m = P.m, K = P.K;
+    P.items.clear();
+    for (int I = 0; I < m; ++I) {
+        int ikr = c->ikrmo[I];
+        if (ikr > 0) continue;  // records are written for barred I only
+        for (int J = 0; J < m; ++J) {
+            int jkr = c->ikrmo[J];
+            if (std::abs(jkr) > std::abs(ikr)) continue;
+            P.items.push_back({I, J, std::abs(ikr), std::abs(jkr), jkr < 0 ? 1 : 0});
+        }
+    }
+    w.items4.resize(P.items.size());
+    w.isign.resize(P.items.size());
+    for (size_t t = 0; t < P.items.size(); ++t) {
+        const Item& it = P.items[t];
+        int ib = std::abs(c->itrmo[it.I]) - 1, jb = std::abs(c->itrmo[it.J]) - 1;
+        w.items4[t] = make_int4(it.I, it.J, ib, jb);
+        w.isign[t] = ((c->itrmo[it.I] > 0) == (c->itrmo[it.J] > 0)) ? 1.0f : -1.0f;
+    }
+    // records: class streams in item order
+    w.recs.clear();
+    w.item_rec0.assign(P.items.size() + 1, 0);
+    for (int cc = 0; cc < 4; ++cc) { w.cap[cc] = 0; w.nrec[cc] = 0; }
+    const bool all = c->cfg.throut < 0.0;
+    for (size_t t = 0; t < P.items.size(); ++t) {
+        const Item& it = P.items[t];
+        w.item_rec0[t] = (int)w.recs.size();
+        for (int cc = it.cls1 ? 0 : 1; cc <= (it.cls1 ? 0 : 3); ++cc) {
+            EmitRec r;
+            r.ijl = 0;  // filled per chunk
+            r.cls = cc;
+            r.ikr = it.ikr;
+            r.jkr = it.jkr;
+            r.rank = (int)w.nrec[cc]++;
+            w.cap[cc] += set_size(cc, it.ikr, it.jkr, K, all);
+            w.recs.push_back(r);
+        }
+    }
+    w.item_rec0[P.items.size()] = (int)w.recs.size();
+    // VMX (getmos.F:417-423) and the pair screening products
+    std::vector<double> vmx(P.n, 0.0);
+    for (int p = 0; p < P.n; ++p)
+        for (int i = 0; i < m; ++i) {
+            double re = c->qa[2 * ((size_t)p + (size_t)i * P.n)], im = c->qa[2 * ((size_t)p + (size_t)i * P.n) + 1];
+            vmx[p] = std::max(vmx[p], std::hypot(re, im));
+        }
+    w.pair_vmx.resize(P.P);
+    for (int i = 0; i < P.P; ++i) w.pair_vmx[i] = vmx[P.pair_p[i]] * vmx[P.pair_q[i]];
+}
+
+// ---------------------------------------------------------------------------
+// C-ABI
+// ---------------------------------------------------------------------------
+#define API_TRY try {
+#define API_CATCH                                                     \
+    }                                                                 \
+    catch (const rt::Error& e) {                                      \
+        ctx->err = e.msg;                                             \
+        return e.code;                                                \
+    }                                                                 \
+    catch (const std::bad_alloc&) {                                   \
+        ctx->err = "host allocation failed";                          \
+        return RT_ERR_PROGRAM;                                        \
+    }                                                                 \
+    catch (const std::exception& e) {                                 \
+        ctx->err = e.what();                                          \
+        return RT_ERR_PROGRAM;                                        \
+    }                                                                 \
+    return RT_OK;
+
+static thread_local std::string g_create_err;
+
+extern "C" int rt_create(rt_ctx** out, const rt_config* cfg) {
+    if (!out) return RT_ERR_USER;
+    *out = nullptr;
+    rt_ctx* ctx = new (std::nothrow) rt_ctx();
+    if (!ctx) return RT_ERR_PROGRAM;
+    API_TRY
+    check_config(cfg);
+    ctx->cfg = *cfg;
+    if (cfg->n_irrep == 4) ctx->ao_irrep.assign(cfg->ao_irrep, cfg->ao_irrep + cfg->nsc);
+    ctx->cfg.ao_irrep = nullptr;
+    if (ctx->cfg.slices == 0) ctx->cfg.slices = 7;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        throw Error(RT_ERR_PROGRAM, "no CUDA device: the library has no CPU path");
+    }
+    RT_CUDA(cudaGetDevice(&ctx->device));
+    cudaDeviceProp prop;
+    RT_CUDA(cudaGetDeviceProperties(&prop, ctx->device));
+    if (prop.major != 10 || prop.minor != 3)
+        throw Error(RT_ERR_PROGRAM, std::string("the library is built for sm_103a; device is ") +
+                                        prop.name);
+    RT_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    for (auto& e : ctx->ev) RT_CUDA(cudaEventCreate(&e));
+    plan_ao(ctx);
+    *out = ctx;
+    return RT_OK;
+    }
+    catch (const rt::Error& e) {
+        g_create_err = e.msg;
+        rt_destroy(ctx);
+        return e.code;
+    }
+    catch (...) {
+        g_create_err = "rt_create failed";
+        rt_destroy(ctx);
+        return RT_ERR_PROGRAM;
+    }
+}
+
+extern "C" int rt_set_coefficients(rt_ctx* ctx, const double* qa, int ld_qa, const int* itrmo,
+                                   const int* kra, const int* krb, const int* ikrmo,
+                                   const int* imoras_pairs) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    const int n = ctx->plan.n, m = ctx->plan.m, K = ctx->plan.K;
+    if (!qa || !itrmo || !kra || !krb || !ikrmo) throw Error(RT_ERR_USER, "null coefficient table");
+    if (ld_qa < n) throw Error(RT_ERR_USER, "ld_qa < NSC");
+    // consistency of the Kramers tables (getmos.F:354-387, kramers.F:114-115)
+    for (int i = 0; i < m; ++i) {
+        int j = std::abs(itrmo[i]);
+        if (j < 1 || j > m || j == i + 1 || itrmo[j - 1] != -(itrmo[i] > 0 ? 1 : -1) * (i + 1))
+            throw Error(RT_ERR_PROGRAM, "ITRMO does not pair the spinors (Kramers symmetry error)");
+    }
+    for (int k = 0; k < K; ++k) {
+        int a = kra[k], b = krb[k];
+        if (a < 1 || a > m || b < 1 || b > m || itrmo[a - 1] != b || ikrmo[a - 1] != k + 1 ||
+            ikrmo[b - 1] != -(k + 1))
+            throw Error(RT_ERR_PROGRAM, "KRA/KRB/IKRMO inconsistent with ITRMO");
+    }
+    ctx->qa.assign((size_t)2 * n * m, 0.0);
+    for (int i = 0; i < m; ++i)
+        std::memcpy(&ctx->qa[(size_t)2 * i * n], qa + (size_t)2 * i * ld_qa, sizeof(double) * 2 * n);
+    for (double v : ctx->qa)
+        if (!std::isfinite(v)) throw Error(RT_ERR_USER, "non-finite spinor coefficient");
+    ctx->itrmo.assign(itrmo, itrmo + m);
+    ctx->kra.assign(kra, kra + K);
+    ctx->krb.assign(krb, krb + K);
+    ctx->ikrmo.assign(ikrmo, ikrmo + m);
+    ctx->imoras.assign(2 * K, 0);
+    if (imoras_pairs) ctx->imoras.assign(imoras_pairs, imoras_pairs + 2 * K);
+    else
+        for (int k = 0; k < K; ++k) { ctx->imoras[2 * k] = kra[k]; ctx->imoras[2 * k + 1] = krb[k]; }
+    plan_items(ctx);
+    build_coef_device(ctx);
+    RT_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->have_coef = true;
+    API_CATCH
+}
+
+// grow the device record store to hold `need` integrals
+static void ensure_record_capacity(rt_ctx* c, long long need) {
+    if (need <= c->cap_int) return;
+    long long cap = std::max(need, c->cap_int * 2);
+    double* v = dalloc<double>(c, cap);
+    int* a = dalloc<int>(c, cap);
+    int* b = dalloc<int>(c, cap);
+    if (c->n_int > 0) {
+        RT_CUDA(cudaMemcpyAsync(v, c->d_rint, c->n_int * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        RT_CUDA(cudaMemcpyAsync(a, c->d_l2, c->n_int * sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+        RT_CUDA(cudaMemcpyAsync(b, c->d_l1, c->n_int * sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+        RT_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    dfree(c, c->d_rint);
+    dfree(c, c->d_l2);
+    dfree(c, c->d_l1);
+    c->d_rint = v;
+    c->d_l2 = a;
+    c->d_l1 = b;
+    c->cap_int = cap;
+}
+
+static void flush_staged(rt_ctx* c) {
+    long long ns = (long long)c->st_v.size();
+    if (ns == 0) return;
+    ensure_record_capacity(c, c->n_int + ns);
+    RT_CUDA(cudaMemcpyAsync(c->d_rint + c->n_int, c->st_v.data(), ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    RT_CUDA(cudaMemcpyAsync(c->d_l2 + c->n_int, c->st_l2.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    RT_CUDA(cudaMemcpyAsync(c->d_l1 + c->n_int, c->st_l1.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    RT_CUDA(cudaStreamSynchronize(c->stream));
+    c->n_int += ns;
+    c->st_v.clear();
+    c->st_l2.clear();
+    c->st_l1.clear();
+}
+
+static void add_record_meta(rt_ctx* c, int file, int it, long long nt, long long off) {
+    c->rec_file.push_back(file);
+    c->rec_it.push_back(it);
+    c->rec_nt.push_back(nt);
+    c->rec_off.push_back(off);
+}
+
+extern "C" int rt_add_ao_records(rt_ctx* ctx, int file_class, int nt, int itype, const double* rint,
+                                 const int* label2, const int* label1) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    if (nt < 0) throw Error(RT_ERR_USER, "negative record length");
+    if (file_class < 1 || file_class > 4) throw Error(RT_ERR_USER, "file class must be 1..4");
+    if (nt > 0 && (!rint || !label2 || !label1)) throw Error(RT_ERR_USER, "null record arrays");
+    long long off = ctx->n_int + (long long)ctx->st_v.size();
+    add_record_meta(ctx, file_class, itype, nt, off);
+    ctx->st_v.insert(ctx->st_v.end(), rint, rint + nt);
+    ctx->st_l2.insert(ctx->st_l2.end(), label2, label2 + nt);
+    ctx->st_l1.insert(ctx->st_l1.end(), label1, label1 + nt);
+    if (ctx->st_v.size() >= (size_t)(8 << 20)) flush_staged(ctx);
+    ctx->transformed = false;
+    API_CATCH
+}
+
+extern "C" int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* file_class,
+                                      const long long* nt, const int* itype, const double* rint,
+                                      const int* label2, const int* label1) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    if (nrec < 0) throw Error(RT_ERR_USER, "negative record count");
+    long long tot = 0;
+    for (long long r = 0; r < nrec; ++r) {
+        if (nt[r] < 0) throw Error(RT_ERR_USER, "negative record length");
+        if (file_class[r] < 1 || file_class[r] > 4) throw Error(RT_ERR_USER, "file class must be 1..4");
+        tot += nt[r];
+    }
+    flush_staged(ctx);
+    long long off = ctx->n_int;
+    for (long long r = 0; r < nrec; ++r) {
+        add_record_meta(ctx, file_class[r], itype[r], nt[r], off);
+        off += nt[r];
+    }
+    ensure_record_capacity(ctx, ctx->n_int + tot);
+    if (tot > 0) {
+        RT_CUDA(cudaMemcpyAsync(ctx->d_rint + ctx->n_int, rint, tot * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        RT_CUDA(cudaMemcpyAsync(ctx->d_l2 + ctx->n_int, label2, tot * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        RT_CUDA(cudaMemcpyAsync(ctx->d_l1 + ctx->n_int, label1, tot * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    ctx->n_int += tot;
+    ctx->transformed = false;
+    API_CATCH
+}
+
+extern "C" int rt_clear_ao_records(rt_ctx* ctx) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    ctx->n_int = 0;
+    ctx->st_v.clear();
+    ctx->st_l2.clear();
+    ctx->st_l1.clear();
+    ctx->rec_file.clear();
+    ctx->rec_it.clear();
+    ctx->rec_nt.clear();
+    ctx->rec_off.clear();
+    ctx->transformed = false;
+    API_CATCH
+}
+
+// ---------------------------------------------------------------------------
+// the transformation
+// ---------------------------------------------------------------------------
+namespace {
+
+void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk) {
+    Plan& P = c->plan;
+    Work& w = W(c);
+    const int n = P.n, m = P.m;
+    const long long KK1 = (long long)P.items.size();
+    if (!c->d_g3) c->d_g3 = dalloc<double>(c, (size_t)P.g3_doubles);
+    if (!c->d_hp) c->d_hp = dalloc<double>(c, (size_t)2 * KK1 * P.P);
+    for (int cc = 0; cc < 4; ++cc) {
+        if (!c->d_oidx[cc]) {
+            c->d_oidx[cc] = dalloc<int>(c, (size_t)2 * std::max(1LL, w.cap[cc]));
+            c->d_oval[cc] = dalloc<double>(c, (size_t)2 * std::max(1LL, w.cap[cc]));
+            c->d_hdr[cc] = dalloc<int>(c, (size_t)std::max(1LL, w.nrec[cc]));          // counts
+            c->out_cap[cc] = w.cap[cc];
+        }
+    }
+    // work arena from the memory budget
+    size_t freeb = 0, totb = 0;
+    RT_CUDA(cudaMemGetInfo(&freeb, &totb));
+    long long budget = c->cfg.mem_budget > 0 ? c->cfg.mem_budget - (long long)c->dev_bytes
+                                            : (long long)(0.85 * (double)freeb);
+    const int S = c->cfg.precision == RT_PREC_SPLIT_BF16 ? c->cfg.slices : 0;
+    // bytes per pair of stage A and per item of stage B
+    double per_pair = 16.0 * n * m + 16.0 * m * m;
+    int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+    double per_item = 16.0 * ncmax * ncmax + 16.0 * n * m + 16.0 * m * m;
+    if (S) {
+        per_pair += split_stageA_bytes_per_pair(c);
+        per_item += split_stageB_bytes_per_item(c);
+    }
+    int maxpg = 1;
+    for (auto& g : P.pgroups) maxpg = std::max(maxpg, g.size);
+    long long usable = budget - (64LL << 20);
+    if (usable <= 0) throw Error(RT_ERR_DIM, "device memory budget exhausted by the fixed arrays");
+    pair_chunk = (int)std::min<long long>(maxpg, std::max(1LL, (long long)(usable / per_pair)));
+    item_chunk = (int)std::min<long long>(KK1, std::max(1LL, (long long)(usable / per_item)));
+    pair_chunk = std::min(pair_chunk, 16384);
+    item_chunk = std::min(item_chunk, 16384);
+    if (usable < per_pair || usable < per_item)
+        throw Error(RT_ERR_DIM, "device memory budget too small for one pair / one item");
+    size_t need_a = (size_t)((per_pair - (S ? split_stageA_bytes_per_pair(c) : 0)) * pair_chunk / 8) + 64;
+    size_t need_b = (size_t)((per_item - (S ? split_stageB_bytes_per_item(c) : 0)) * item_chunk / 8) + 64;
+    size_t need = std::max(need_a, need_b);
+    if (!c->d_ha || c->stage.pair_chunk != pair_chunk || c->stage.item_chunk != item_chunk) {
+        dfree(c, c->d_ha);
+        c->d_ha = dalloc<double>(c, need);
+        c->stage.pair_chunk = pair_chunk;
+        c->stage.item_chunk = item_chunk;
+        if (S) split_alloc_work(c, pair_chunk, item_chunk);
+    }
+}
+
+}  // namespace
+
+static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
+    Plan& P = c->plan;
+    auto up = [&](auto* hostp, size_t count, auto*& devp) {
+        using TT = std::remove_const_t<std::remove_pointer_t<decltype(hostp)>>;
+        TT* d = dalloc<TT>(c, count);
+        if (count) RT_CUDA(cudaMemcpyAsync(d, hostp, count * sizeof(TT), cudaMemcpyHostToDevice, c->stream));
+        devp = d;
+        tmp.push_back(d);
+    };
+    const long long ntri = (long long)P.n * (P.n + 1) / 2;
+    std::vector<unsigned char> pqr(ntri, 0);
+    for (int p = 0; p < P.n; ++p)
+        for (int q = 0; q <= p; ++q) {
+            bool pl = p < P.nL, ql = q < P.nL;
+            bool inc = !(!pl && ql) && !(!pl && c->cfg.mfil < 3);  // makind.F:240-242
+            pqr[(long long)p * (p + 1) / 2 + q] = inc ? 1 : 0;
+        }
+    std::vector<int> pgroup(P.P), pgs, pgz, aopos(P.n), g1of(P.pgroups.size() * P.nblk, -1), g1k;
+    std::vector<long long> g1b;
+    for (size_t g = 0; g < P.pgroups.size(); ++g) {
+        pgs.push_back(P.pgroups[g].start);
+        pgz.push_back(P.pgroups[g].size);
+        for (int i = 0; i < P.pgroups[g].size; ++i) pgroup[P.pgroups[g].start + i] = (int)g;
+    }
+    for (int p = 0; p < P.n; ++p) aopos[p] = P.ao_sorted[p] - P.blk_start[P.ao_block[p]];
+    for (size_t g = 0; g < P.g1.size(); ++g) {
+        g1of[P.g1[g].pg * P.nblk + P.g1[g].rblk] = (int)g;
+        g1k.push_back(P.g1[g].kblk);
+        g1b.push_back(P.g1[g].base);
+    }
+    up(pqr.data(), pqr.size(), T.pq_read);
+    up(P.pair_of_orig.data(), P.pair_of_orig.size(), T.pair_of_orig);
+    up(pgroup.data(), pgroup.size(), T.pair_group);
+    up(pgs.data(), pgs.size(), T.pg_start);
+    up(pgz.data(), pgz.size(), T.pg_size);
+    up(P.ao_block.data(), P.ao_block.size(), T.ao_block);
+    up(aopos.data(), aopos.size(), T.ao_pos);
+    up(P.blk_size.data(), P.blk_size.size(), T.blk_size);
+    up(g1of.data(), g1of.size(), T.g1_of);
+    up(g1k.data(), g1k.size(), T.g1_kblk);
+    up(g1b.data(), g1b.size(), T.g1_base);
+}
+
+extern "C" int rt_transform(rt_ctx* ctx) {
+    if (!ctx) return RT_ERR_USER;
+    std::vector<void*> tmp;
+    API_TRY
+    if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
+    Plan& P = ctx->plan;
+    Work& w = W(ctx);
+    cudaStream_t st = ctx->stream;
+    const int n = P.n, m = P.m, K = P.K;
+    const int KK1 = (int)P.items.size();
+    const bool split = ctx->cfg.precision == RT_PREC_SPLIT_BF16;
+    int launches = 0;
+    RT_CUDA(cudaEventRecord(ctx->ev[0], st));
+    flush_staged(ctx);
+    RT_CUDA(cudaEventRecord(ctx->ev[1], st));
+    int pair_chunk = 0, item_chunk = 0;
+    ensure_fixed(ctx, pair_chunk, item_chunk);
+    // ---- tables (small) ----
+    DeviceTabs T;
+    upload_tables(ctx, T, tmp);
+    long long* d_roff = dalloc<long long>(ctx, ctx->rec_off.size());
+    tmp.push_back(d_roff);
+    int2* d_rmeta = dalloc<int2>(ctx, ctx->rec_off.size());
+    tmp.push_back(d_rmeta);
+    {
+        std::vector<int2> meta(ctx->rec_off.size());
+        for (size_t r = 0; r < meta.size(); ++r) meta[r] = make_int2(ctx->rec_file[r], ctx->rec_it[r]);
+        if (!meta.empty()) {
+            RT_CUDA(cudaMemcpyAsync(d_roff, ctx->rec_off.data(), meta.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
+            RT_CUDA(cudaMemcpyAsync(d_rmeta, meta.data(), meta.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+        }
+    }
+    int4* d_items = dalloc<int4>(ctx, KK1);
+    tmp.push_back(d_items);
+    float* d_isign = dalloc<float>(ctx, KK1);
+    tmp.push_back(d_isign);
+    double* d_pvmx = dalloc<double>(ctx, P.P);
+    tmp.push_back(d_pvmx);
+    int* d_kra = dalloc<int>(ctx, K);
+    int* d_krb = dalloc<int>(ctx, K);
+    int* d_itrmo = dalloc<int>(ctx, m);
+    tmp.push_back(d_kra); tmp.push_back(d_krb); tmp.push_back(d_itrmo);
+    RT_CUDA(cudaMemcpyAsync(d_items, w.items4.data(), KK1 * sizeof(int4), cudaMemcpyHostToDevice, st));
+    RT_CUDA(cudaMemcpyAsync(d_isign, w.isign.data(), KK1 * sizeof(float), cudaMemcpyHostToDevice, st));
+    RT_CUDA(cudaMemcpyAsync(d_pvmx, w.pair_vmx.data(), P.P * sizeof(double), cudaMemcpyHostToDevice, st));
+    RT_CUDA(cudaMemcpyAsync(d_kra, ctx->kra.data(), K * sizeof(int), cudaMemcpyHostToDevice, st));
+    RT_CUDA(cudaMemcpyAsync(d_krb, ctx->krb.data(), K * sizeof(int), cudaMemcpyHostToDevice, st));
+    RT_CUDA(cudaMemcpyAsync(d_itrmo, ctx->itrmo.data(), m * sizeof(int), cudaMemcpyHostToDevice, st));
+    int* d_pidx[2] = {nullptr, nullptr};
+    for (int cc = 0; cc < 2; ++cc) {
+        d_pidx[cc] = dalloc<int>(ctx, P.pidx[cc].size());
+        tmp.push_back(d_pidx[cc]);
+        if (!P.pidx[cc].empty())
+            RT_CUDA(cudaMemcpyAsync(d_pidx[cc], P.pidx[cc].data(), P.pidx[cc].size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    }
+    unsigned long long* d_stat = dalloc<unsigned long long>(ctx, 8);
+    tmp.push_back(d_stat);
+    RT_CUDA(cudaMemsetAsync(d_stat, 0, 8 * sizeof(unsigned long long), st));
+    long long* d_total = dalloc<long long>(ctx, 4);
+    tmp.push_back(d_total);
+    RT_CUDA(cudaMemsetAsync(d_total, 0, 4 * sizeof(long long), st));
+    long long* d_off[4];
+    for (int cc = 0; cc < 4; ++cc) {
+        d_off[cc] = dalloc<long long>(ctx, std::max(1LL, w.nrec[cc]));
+        tmp.push_back(d_off[cc]);
+    }
+    // ---- scatter the records into G3 (SORT1) ----
+    RT_CUDA(cudaMemsetAsync(ctx->d_g3, 0, P.g3_doubles * sizeof(double), st));
+    ScatterTabs tb{n, ctx->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
+                   T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk, T.g1_base};
+    launch_scatter(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, ctx->n_int, d_roff, d_rmeta,
+                   (int)ctx->rec_off.size(), tb, ctx->d_g3, (unsigned int*)d_stat);
+    launches += ctx->n_int > 0;
+    RT_CUDA(cudaGetLastError());
+    unsigned long long hstat[8];
+    RT_CUDA(cudaMemcpyAsync(hstat, d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
+    RT_CUDA(cudaStreamSynchronize(st));
+    if (hstat[0] & ST_BAD_LABEL)
+        throw Error(RT_ERR_USER, "integral label outside 1..NSC or pq label with q > p");
+    if (hstat[0] & ST_BAD_BLOCK)
+        throw Error(RT_ERR_USER, "integral outside the (LL|LL)/(SS|LL)/(SS|SS) or irrep block structure");
+    RT_CUDA(cudaMemsetAsync(d_stat, 0, 8 * sizeof(unsigned long long), st));
+    RT_CUDA(cudaEventRecord(ctx->ev[2], st));
+    if (split) split_prepare_g3(ctx, &launches);
+    // ---- stage A: first half-transformation (TRANS1) per pair chunk ----
+    double* ha = ctx->d_ha;
+    double* ri = ha + (size_t)2 * n * m * pair_chunk;
+    for (size_t g = 0; g < P.pgroups.size(); ++g) {
+        const PairGroup& pg = P.pgroups[g];
+        // does every r block meet this pair group?
+        int covered = 0;
+        for (auto& gg : P.g1)
+            if (gg.pg == (int)g) covered += P.blk_size[gg.rblk];
+        for (int c0 = 0; c0 < pg.size; c0 += pair_chunk) {
+            const int npc = std::min(pair_chunk, pg.size - c0);
+            const long long plane = (long long)n * m * npc;
+            if (covered < n) RT_CUDA(cudaMemsetAsync(ha, 0, 2 * plane * sizeof(double), st));
+            for (auto& gg : P.g1) {
+                if (gg.pg != (int)g) continue;
+                const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk];
+                const double* A = ctx->d_g3 + gg.base + (long long)c0 * nk;
+                EpiHA epi{ha, P.blk_start[gg.rblk], m, npc, plane};
+                if (split)
+                    split_gemm1(ctx, gg, c0, npc, epi, &launches);
+                else
+                    gemm_f64(st, A, nk, (long long)pg.size * nk, ctx->d_qap + (long long)P.blk_start[gg.kblk] * 2 * m,
+                             2 * m, 0, npc, 2 * m, nk, nr, epi), ++launches;
+            }
+            EpiRowMajor e2{ri, (long long)m * npc, 0};
+            if (split)
+                split_gemm24(ctx, ha, 2 * n, (long long)m * npc, e2, &launches);
+            else
+                gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2), ++launches;
+            launch_tr_select(st, ri, m, npc, pg.start + c0, P.P, d_items, d_isign, KK1, d_pvmx,
+                             ctx->cfg.thrgen, ctx->d_hp, d_stat + 1);
+            launches += (KK1 + 65534) / 65535;
+        }
+    }
+    RT_CUDA(cudaGetLastError());
+    RT_CUDA(cudaEventRecord(ctx->ev[3], st));
+    // ---- stage B: second half-transformation (TRANS2) + PPSYM per item chunk ----
+    double* m3 = ctx->d_ha;
+    int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+    double* rk = m3 + (size_t)2 * ncmax * ncmax * item_chunk;
+    double* rlr = rk + (size_t)2 * n * m * item_chunk;
+    EmitRec* d_recs = dalloc<EmitRec>(ctx, (size_t)3 * item_chunk);
+    tmp.push_back(d_recs);
+    OutStreams os;
+    for (int cc = 0; cc < 4; ++cc) {
+        os.cnt[cc] = ctx->d_hdr[cc];
+        os.off[cc] = d_off[cc];
+        os.idx[cc] = ctx->d_oidx[cc];
+        os.val[cc] = ctx->d_oval[cc];
+    }
+    os.total = d_total;
+    std::vector<EmitRec> chunk_recs;
+    for (int i0 = 0; i0 < KK1; i0 += item_chunk) {
+        const int nij = std::min(item_chunk, KK1 - i0);
+        const long long rkplane = (long long)n * nij * m;
+        for (int cc = 0; cc < 2; ++cc) {
+            const int nc = P.ncomp[cc];
+            if (nc == 0) continue;
+            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, d_pidx[cc], nc, m3);
+            ++launches;
+            EpiRK e3{rk, m, (long long)P.comp_off[cc] * nij, rkplane};
+            if (split)
+                split_gemm3(ctx, cc, m3, nc, nij, e3, &launches);
+            else
+                gemm_f64(st, m3, 2 * nc, 0, ctx->d_qar[cc], 2 * m, 0, nc * nij, 2 * m, 2 * nc, 1, e3), ++launches;
+        }
+        EpiRowMajor e4{rlr, (long long)nij * m, 0};
+        if (split)
+            split_gemm24(ctx, rk, 2 * n, (long long)nij * m, e4, &launches);
+        else
+            gemm_f64(st, ctx->d_qah, 2 * n, 0, rk, (long long)nij * m, 0, 2 * m, nij * m, 2 * n, 1, e4), ++launches;
+        // MDCINT selection for the records of this chunk
+        chunk_recs.assign(w.recs.begin() + w.item_rec0[i0], w.recs.begin() + w.item_rec0[i0 + nij]);
+        for (int t = i0; t < i0 + nij; ++t)
+            for (int r = w.item_rec0[t]; r < w.item_rec0[t + 1]; ++r)
+                chunk_recs[r - w.item_rec0[i0]].ijl = t - i0;
+        RT_CUDA(cudaMemcpyAsync(d_recs, chunk_recs.data(), chunk_recs.size() * sizeof(EmitRec), cudaMemcpyHostToDevice, st));
+        launch_emit(st, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), d_kra, d_krb, d_itrmo,
+                    ctx->cfg.throut, os);
+        launches += 3;
+        // the host copy of chunk_recs must outlive the async copy
+        RT_CUDA(cudaStreamSynchronize(st));
+    }
+    RT_CUDA(cudaGetLastError());
+    RT_CUDA(cudaEventRecord(ctx->ev[4], st));
+    long long tot[4];
+    RT_CUDA(cudaMemcpyAsync(tot, d_total, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    RT_CUDA(cudaMemcpyAsync(hstat, d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
+    RT_CUDA(cudaEventRecord(ctx->ev[5], st));
+    RT_CUDA(cudaStreamSynchronize(st));
+    for (int cc = 0; cc < 4; ++cc) {
+        ctx->out_nz[cc] = tot[cc];
+        ctx->out_nrec[cc] = w.nrec[cc];
+    }
+    float ms[5];
+    for (int e = 0; e < 5; ++e) RT_CUDA(cudaEventElapsedTime(&ms[e], ctx->ev[e], ctx->ev[e + 1]));
+    rt_stats& S = ctx->stats;
+    S.ms_upload = ms[0];
+    S.ms_scatter = ms[1];
+    S.ms_first = ms[2];
+    S.ms_second = ms[3];
+    S.ms_output = ms[4];
+    float tot_ms = 0;
+    RT_CUDA(cudaEventElapsedTime(&tot_ms, ctx->ev[0], ctx->ev[5]));
+    S.ms_total = tot_ms;
+    S.nhalft = (long long)hstat[1];
+    for (int cc = 0; cc < 4; ++cc) {
+        S.nfinal[cc] = tot[cc];
+        S.nrec[cc] = w.nrec[cc];
+    }
+    // algorithmic FLOPs (dense-block count of the reference algorithm)
+    double f1 = 0.0;
+    for (auto& gg : P.g1)
+        f1 += 2.0 * P.blk_size[gg.rblk] * (double)P.pgroups[gg.pg].size * P.blk_size[gg.kblk] * 2.0 * m;
+    f1 += (double)P.P * 8.0 * n * (double)m * m;
+    double f2 = 0.0;
+    for (int cc = 0; cc < 2; ++cc) f2 += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
+    f2 = (double)KK1 * (f2 + 8.0 * n * (double)m * m);
+    S.flops_algorithmic = f1 + f2;
+    S.device_bytes = (long long)ctx->dev_peak;
+    S.gpu_launches = launches;
+    ctx->transformed = true;
+    for (void* p : tmp) dfree(ctx, p);
+    tmp.clear();
+    API_CATCH
+}
+
+extern "C" int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    if (!ctx->transformed) throw Error(RT_ERR_USER, "no transform result");
+    long long a = 0, b = 0;
+    for (int c = 0; c < 4; ++c) { a += ctx->out_nrec[c]; b += ctx->out_nz[c]; }
+    if (nrec) *nrec = a;
+    if (nz) *nz = b;
+    API_CATCH
+}
+
+extern "C" int rt_copy_result(rt_ctx* ctx, int* hdr, int* idx, double* val) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    if (!ctx->transformed) throw Error(RT_ERR_USER, "no transform result");
+    Work& w = W(ctx);
+    long long r0 = 0, z0 = 0;
+    std::vector<int> cnt;
+    for (int c = 0; c < 4; ++c) {
+        const long long nr = ctx->out_nrec[c], nz = ctx->out_nz[c];
+        cnt.resize(std::max(1LL, nr));
+        if (nr) RT_CUDA(cudaMemcpyAsync(cnt.data(), ctx->d_hdr[c], nr * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        if (nz && idx) RT_CUDA(cudaMemcpyAsync(idx + 2 * z0, ctx->d_oidx[c], 2 * nz * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        if (nz && val) RT_CUDA(cudaMemcpyAsync(val + 2 * z0, ctx->d_oval[c], 2 * nz * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (hdr) {
+            long long k = 0;
+            for (const EmitRec& r : w.recs) {
+                if (r.cls != c) continue;
+                int is = -1, js = (c == 0) ? -1 : 1;   // rotran.F:306-328
+                hdr[3 * (r0 + k)] = r.ikr * is;
+                hdr[3 * (r0 + k) + 1] = r.jkr * js;
+                hdr[3 * (r0 + k) + 2] = cnt[k];
+                ++k;
+            }
+        }
+        r0 += nr;
+        z0 += nz;
+    }
+    API_CATCH
+}
+
+extern "C" int rt_get_stats(rt_ctx* ctx, rt_stats* out) {
+    if (!ctx || !out) return RT_ERR_USER;
+    *out = ctx->stats;
+    return RT_OK;
+}
+
+extern "C" const char* rt_last_error(rt_ctx* ctx) {
+    if (!ctx) return g_create_err.c_str();
+    return ctx->err.c_str();
+}
+
+extern "C" void rt_destroy(rt_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto& a : ctx->allocs) cudaFree(a.first);
+    ctx->allocs.clear();
+    split_release(ctx);
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int rt_internal_mfil(rt_ctx* c) { return c->cfg.mfil; }
+int rt_internal_nkr(rt_ctx* c) { return c->cfg.nkr; }
+const int* rt_internal_imoras(rt_ctx* c) { return c->imoras.data(); }
+void rt_internal_set_error(rt_ctx* c, const char* msg) { c->err = msg; }
+
+extern "C" int rt_plan(const rt_config* cfg, rt_plan_info* out) {
+    if (!out) return RT_ERR_USER;
+    std::memset(out, 0, sizeof(*out));
+    rt_ctx tmp;
+    rt_ctx* ctx = &tmp;
+    API_TRY
+    check_config(cfg);
+    tmp.cfg = *cfg;
+    if (cfg->n_irrep == 4) tmp.ao_irrep.assign(cfg->ao_irrep, cfg->ao_irrep + cfg->nsc);
+    plan_ao(&tmp);
+    const Plan& P = tmp.plan;
+    const int K = P.K, m = P.m, n = P.n;
+    const long long KK1 = (long long)K * (K + 1);
+    out->npairs = P.P;
+    out->nitems = KK1;
+    out->g3_bytes = P.g3_doubles * 8;
+    out->hp_bytes = 2 * KK1 * P.P * 8;
+    const bool all = cfg->throut < 0.0;
+    for (int i = 1; i <= K; ++i)
+        for (int j = 1; j <= i; ++j) {
+            out->nrec[0]++;
+            out->elem_cap[0] += set_size(0, i, j, K, all);
+            for (int c = 1; c < 4; ++c) {
+                out->nrec[c]++;
+                out->elem_cap[c] += set_size(c, i, j, K, all);
+            }
+        }
+    double f1 = 0.0;
+    for (auto& gg : P.g1)
+        f1 += 2.0 * P.blk_size[gg.rblk] * (double)P.pgroups[gg.pg].size * P.blk_size[gg.kblk] * 2.0 * m;
+    f1 += (double)P.P * 8.0 * n * (double)m * m;
+    double f2 = 0.0;
+    for (int cc = 0; cc < 2; ++cc) f2 += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
+    f2 = (double)KK1 * (f2 + 8.0 * n * (double)m * m);
+    out->flops_algorithmic = f1 + f2;
+    return RT_OK;
+    }
+    catch (const rt::Error& e) {
+        g_create_err = e.msg;
+        return e.code;
+    }
+    catch (...) {
+        g_create_err = "rt_plan failed";
+        return RT_ERR_PROGRAM;
+    }
+}

@@ -1,0 +1,182 @@
+// rt_internal.h -- internal structures of the GB300 rotran library.
+//
+// Data layout in device memory (planar complex: plane 0 = re, 1 = im):
+//
+//   AO order      AO functions are renumbered block-major ("sorted order"):
+//                 blocks = component (L, S) x irrep (1 or 4), each block in
+//                 increasing reference index.  The L functions occupy sorted
+//                 positions [0, nL) and the S functions [nL, n).
+//   pair order    the pq blocks rotran transforms (LL pairs, and SS pairs
+//                 when S functions exist; makind.F:235-255) grouped by
+//                 (class, pair irrep), inside a group in increasing
+//                 p(p-1)/2+q.  P = number of pairs.
+//   G3            AO integrals expanded per pair-group x r-block:
+//                 G3_g[pq][r][s], r in the r-block, s in the partner block,
+//                 G(pq|rs) with both r<->s orders (the full symmetric
+//                 matrix G_pq(r,s) of the integrals of pair pq).
+//   HA            (stage A, per pair chunk) [plane][r][b][pq]: sum_s G_pq(r,s) QA(s,b)
+//   RI            (stage A) [plane][a][b][pq]: sum_r conj(QA(r,a)) HA(r,b)
+//   Hp            [plane][ij][pq]: (pq| I J) = RI(I,J) + s_IJ RI(Jbar,Ibar)
+//                 for the K(K+1) Kramers-unique spinor pairs (the "sort /
+//                 transpose" between the two halves)
+//   M3            (stage B, per ij chunk, per component block)
+//                 [p][ij][plane][q]: Hp expanded to the symmetric n_c x n_c matrix
+//   RK            [plane][p][ij][k]: sum_q M_ij(p,q) QA(q,k)
+//   RLR           [plane][l][ij][k]: sum_p conj(QA(p,l)) RK(p,k)
+//   RL(K,L) = RLR(K,L) + s_KL RLR(Lbar,Kbar) gives the complete integrals
+//   (I J | K L) from which the MDCINT records are selected.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rotran_gb300.h"
+#include "rt_kernels.h"
+
+namespace rt {
+
+#define RT_CUDA(call)                                                                   \
+    do {                                                                                \
+        cudaError_t e__ = (call);                                                       \
+        if (e__ != cudaSuccess) throw rt::Error(RT_ERR_PROGRAM, std::string("CUDA: ") + \
+                                                cudaGetErrorString(e__) + " at " #call); \
+    } while (0)
+
+struct Error {
+    int code;
+    std::string msg;
+    Error(int c, std::string m) : code(c), msg(std::move(m)) {}
+};
+
+// A GEMM1 group: pairs of one pair-group against one r-block.
+struct G1Group {
+    int pg;          // pair group index
+    int rblk;        // AO block of r
+    int kblk;        // AO block of s (partner block)
+    long long base;  // offset of G3_g in the G3 arena (doubles)
+};
+
+struct PairGroup {
+    int cls;         // 0 = LL, 1 = SS
+    int gamma;       // pair irrep
+    int start, size; // range in pair order
+};
+
+// One transform item of TRANS2's loop (trans2.F:73-74,230-238): barred spinor
+// I of Kramers pair ikr, spinor J of pair jkr (barred: class 1; unbarred:
+// classes 2, 3, 4), jkr <= ikr.
+struct Item {
+    int I, J;        // 0-based spinor indices
+    int ikr, jkr;    // 1-based Kramers-pair indices
+    int cls1;        // 1: J barred (class 1 record), 0: classes 2,3,4
+};
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct Plan {
+    int n = 0, nL = 0, nS = 0, m = 0, K = 0;
+    int nblk = 0;
+    std::vector<int> blk_start, blk_size, blk_comp, blk_irr;
+    std::vector<int> ao_sorted;   // reference AO index (0-based) -> sorted position
+    std::vector<int> ao_block;
+    int P = 0;
+    std::vector<PairGroup> pgroups;
+    std::vector<int> pair_of_orig; // p(p-1)/2+q-1 -> pair order index or -1
+    std::vector<int> pair_p, pair_q; // sorted AO positions of each pair (p >= q in reference order)
+    std::vector<G1Group> g1;
+    long long g3_doubles = 0;
+    std::vector<Item> items;      // K(K+1) items in TRANS2 order
+    std::vector<int> cls1_rank;   // record position of each item within its class stream(s)
+    int n_cls1 = 0, n_cls234 = 0;
+    // expansion tables: per component block c (0 = L, 1 = S) the pair index
+    // of (p, q) in component-local sorted positions, -1 if none
+    std::vector<int> pidx[2];
+    int ncomp[2] = {0, 0};
+    int comp_off[2] = {0, 0};
+};
+
+struct Stage {
+    int pair_chunk = 0;
+    int item_chunk = 0;
+};
+
+// Host tables of the transform derived from the coefficients.
+struct Work {
+    std::vector<int4> items4;     // (I, J, Ibar, Jbar) per item
+    std::vector<float> isign;     // sign(ITRMO(I) ITRMO(J))
+    std::vector<double> pair_vmx; // VMX(p) VMX(q) per pair (trout.F:194)
+    std::vector<EmitRec> recs;    // MDCINT records in item order
+    std::vector<int> item_rec0;   // first record of each item
+    long long cap[4] = {0, 0, 0, 0};   // element capacity per class
+    long long nrec[4] = {0, 0, 0, 0};  // records per class
+};
+
+struct SplitState;  // rt_split.cu
+
+}  // namespace rt
+
+struct rt_ctx {
+    rt_config cfg{};
+    std::vector<int> ao_irrep;
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    bool have_coef = false;
+    // host copies of the tables
+    std::vector<double> qa;   // n x m complex, column-major, interleaved
+    std::vector<int> itrmo, kra, krb, ikrmo, imoras;
+    rt::Plan plan;
+    rt::Stage stage;
+    rt::Work work;
+    rt::SplitState* split = nullptr;
+    // records
+    std::vector<int> rec_file, rec_it;
+    std::vector<long long> rec_off, rec_nt;
+    long long n_int = 0;     // integrals stored on device
+    long long cap_int = 0;
+    double* d_rint = nullptr;
+    int* d_l2 = nullptr;
+    int* d_l1 = nullptr;
+    // staging for per-record calls
+    std::vector<double> st_v;
+    std::vector<int> st_l2, st_l1;
+    double* h_pin_v = nullptr;
+    int* h_pin_l2 = nullptr;
+    int* h_pin_l1 = nullptr;
+    size_t pin_cap = 0;
+    // device arrays
+    double* d_g3 = nullptr;
+    double* d_qap = nullptr;     // [s_sorted][plane*m + b]     (n x 2m)
+    double* d_qah = nullptr;     // [(plane',a)][(plane,r)]     (2m x 2n)
+    double* d_qar[2] = {nullptr, nullptr};  // per component: [(plane,q)][(plane',k)] (2nc x 2m)
+    double* d_ha = nullptr;
+    double* d_ri = nullptr;
+    double* d_hp = nullptr;
+    double* d_m3 = nullptr;
+    double* d_rk = nullptr;
+    double* d_rlr = nullptr;
+    double* d_vmx = nullptr;
+    int* d_tab = nullptr;        // device copies of small index tables
+    size_t tab_bytes = 0;
+    int* d_items = nullptr;
+    // output
+    int* d_cnt = nullptr;        // per record (chunk) counts
+    int* d_pad_idx = nullptr;
+    double* d_pad_val = nullptr;
+    int* d_hdr[4] = {};
+    int* d_oidx[4] = {};
+    double* d_oval[4] = {};
+    long long out_nrec[4] = {}, out_nz[4] = {}, out_cap[4] = {};
+    unsigned long long* d_stat = nullptr;
+    rt_stats stats{};
+    size_t dev_bytes = 0, dev_peak = 0;
+    std::vector<std::pair<void*, size_t>> allocs;
+    bool transformed = false;
+};

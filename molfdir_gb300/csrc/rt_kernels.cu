@@ -1,0 +1,379 @@
+// rt_kernels.cu -- device kernels of the plain transformation path:
+// record scatter, FP64 GEMM, the Kramers selection / transpose between the
+// two half-transformations, the symmetric expansion of the half-transformed
+// integrals, and the MDCINT element selection and compaction.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rt_kernels.h"
+
+namespace rt {
+
+// ---------------------------------------------------------------------------
+// record scatter (replaces GETTW + SORT1 + GETSTI: gettw.F:15-56,
+// sort1.F:128-200, getsti.F:250-269)
+// ---------------------------------------------------------------------------
+
+// GETTW's factor for integral type it (gettw.F:33-45).
+__device__ __forceinline__ double gettw_factor(int it) {
+    if (it == 1) return 0.125;
+    if (it == 2) return 0.5;
+    if (it == 3) return 0.25;
+    if (it <= 8) return 0.5;
+    return 1.0;
+}
+
+// Each stored integral (ab|cd) (label2 = a<<16|b, label1 = c<<16|d) is
+// scaled by GETTW's type factor and by 2^(number of index coincidences);
+// for a consistent type the product is 1 and the element of the symmetric
+// supermatrix is recovered, which the reference's three symmetrisation
+// steps (MTIMHER, MATMUL3, PPSYM) rebuild implicitly.
+__global__ void k_scatter(const double* __restrict__ rint, const int* __restrict__ l2,
+                          const int* __restrict__ l1, long long nint,
+                          const long long* __restrict__ rec_off, const int2* __restrict__ rec_meta,
+                          int nrec, ScatterTabs tb, double* __restrict__ g3,
+                          unsigned int* __restrict__ status) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < nint; x += stride) {
+        // record containing x (records sorted by offset)
+        int lo = 0, hi = nrec - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (rec_off[mid] <= x) lo = mid; else hi = mid - 1;
+        }
+        const int2 meta = rec_meta[lo];
+        const int file = meta.x, it = meta.y;
+        if (file < 1 || file > tb.mfil) continue;  // SORT1 reads files 1..MFIL only
+        int L2 = l2[x], L1 = l1[x];
+        int a = (L2 >> 16) & 0xFFFF, b = L2 & 0xFFFF;
+        int c = (L1 >> 16) & 0xFFFF, d = L1 & 0xFFFF;
+        if (a < 1 || b < 1 || c < 1 || d < 1 || a > tb.n || b > tb.n || c > tb.n || d > tb.n ||
+            d > c) {
+            atomicOr(status, ST_BAD_LABEL);
+            continue;
+        }
+        --a; --b; --c; --d;
+        int pa = a > b ? a : b, pb = a > b ? b : a;
+        // the pq bucket of the reference is label1's pair (sort1.F:139-152)
+        int cdo = c * (c + 1) / 2 + d;
+        if (!tb.pq_read[cdo]) continue;   // INDPQ(pq) == 0: never transformed
+        int coinc = (pa == pb) + (c == d) + (pa == c && pb == d);
+        double v = rint[x] * gettw_factor(it) * (double)(1 << coinc);
+        // direction 1: pair cd against the r,s = a,b indices
+        int abo = pa * (pa + 1) / 2 + pb;
+        for (int dir = 0; dir < 2; ++dir) {
+            int pqo = dir == 0 ? cdo : abo;
+            int r = dir == 0 ? pa : c, s = dir == 0 ? pb : d;
+            if (dir == 1 && abo == cdo) break;
+            int pq = tb.pair_of_orig[pqo];
+            if (pq < 0) { atomicOr(status, ST_BAD_BLOCK); break; }
+            int pg = tb.pair_group[pq];
+            for (int sw = 0; sw < 2; ++sw) {
+                int rr = sw ? s : r, ss = sw ? r : s;
+                if (sw && r == s) break;
+                int rb = tb.ao_block[rr];
+                int g = tb.g1_of[pg * tb.nblk + rb];
+                if (g < 0 || tb.g1_kblk[g] != tb.ao_block[ss]) { atomicOr(status, ST_BAD_BLOCK); break; }
+                long long pql = pq - tb.pg_start[pg];
+                long long off = tb.g1_base[g] +
+                                ((long long)tb.ao_pos[rr] * tb.pg_size[pg] + pql) * tb.blk_size[tb.g1_kblk[g]] +
+                                tb.ao_pos[ss];
+                atomicAdd(&g3[off], v);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 GEMM, C = A(MxK, row-major) * B(KxN, row-major), batched over
+// blockIdx.z; the epilogue functor places each element.
+// ---------------------------------------------------------------------------
+
+template <class Epi>
+__global__ void __launch_bounds__(256) k_gemm_f64(const double* __restrict__ A, long long lda,
+                                                  long long sA, const double* __restrict__ B,
+                                                  long long ldb, long long sB, int M, int N, int K,
+                                                  Epi epi) {
+    __shared__ double As[16][65];
+    __shared__ double Bs[16][64];
+    const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
+    const int bz = blockIdx.z;
+    const double* Ab = A + (long long)bz * sA;
+    const double* Bb = B + (long long)bz * sB;
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    const int ar = t >> 2, ak = (t & 3) * 4;
+    const int bk = t >> 4, bn = (t & 15) * 4;
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        const int row = m0 + ar;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int k = k0 + ak + u;
+            As[ak + u][ar] = (row < M && k < K) ? Ab[(long long)row * lda + k] : 0.0;
+        }
+        const int kk = k0 + bk;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int col = n0 + bn + u;
+            Bs[bk][bn + u] = (kk < K && col < N) ? Bb[(long long)kk * ldb + col] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[q][tx + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[q][ty + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int row = m0 + tx + 16 * i, col = n0 + ty + 16 * j;
+            if (row < M && col < N) epi(bz, row, col, acc[i][j]);
+        }
+}
+
+template <class Epi>
+void gemm_f64(cudaStream_t st, const double* A, long long lda, long long sA, const double* B,
+              long long ldb, long long sB, int M, int N, int K, int batch, Epi epi) {
+    dim3 grid((N + 63) / 64, (M + 63) / 64, batch);
+    k_gemm_f64<Epi><<<grid, 256, 0, st>>>(A, lda, sA, B, ldb, sB, M, N, K, epi);
+}
+
+template void gemm_f64<EpiHA>(cudaStream_t, const double*, long long, long long, const double*,
+                              long long, long long, int, int, int, int, EpiHA);
+template void gemm_f64<EpiRowMajor>(cudaStream_t, const double*, long long, long long,
+                                    const double*, long long, long long, int, int, int, int,
+                                    EpiRowMajor);
+template void gemm_f64<EpiRK>(cudaStream_t, const double*, long long, long long, const double*,
+                              long long, long long, int, int, int, int, EpiRK);
+
+// ---------------------------------------------------------------------------
+// K2: Kramers-unique selection + time-reversal completion + transpose
+// (MTIMHER + TROUT + SR2FLSH + GETHTI + UNIQUE: mtimher.F:141-164,
+// trout.F:165-227, unique.F:1-50).  With the full symmetric G_pq the
+// half-transformed integral of the pair (I, J) is
+//   (pq| I J) = RI(I,J) + s_IJ RI(Jbar, Ibar),   s_IJ = sign(ITRMO(I) ITRMO(J)),
+// RI = QA^H G_pq QA.  The screening test of TROUT (trout.F:194-207) is
+// applied to these values.
+// ---------------------------------------------------------------------------
+__global__ void k_tr_select(const double* __restrict__ ri, int m, int npc, int pq0, int P,
+                            const int4* __restrict__ items, const float* __restrict__ item_sign,
+                            int it0, int nitems, const double* __restrict__ pair_vmx,
+                            double thrgen, double* __restrict__ hp,
+                            unsigned long long* __restrict__ kept) {
+    const int it = it0 + blockIdx.y;
+    const int pql = blockIdx.x * blockDim.x + threadIdx.x;
+    int keep = 0;
+    if (pql < npc && it < nitems) {
+        const int4 w = items[it];  // I, J, Ibar, Jbar (0-based spinors)
+        const double s = item_sign[it];
+        const long long plane = (long long)m * m * npc;
+        const long long a = ((long long)w.x * m + w.y) * npc + pql;
+        const long long b = ((long long)w.w * m + w.z) * npc + pql;
+        double re = ri[a] + s * ri[b];
+        double im = ri[plane + a] + s * ri[plane + b];
+        const int pq = pq0 + pql;
+        double vv = pair_vmx[pq];
+        bool pass;
+        if (vv < thrgen) pass = false;
+        else pass = !(hypot(re, im) < thrgen / vv);
+        if (!pass) { re = 0.0; im = 0.0; }
+        keep = pass && (re != 0.0 || im != 0.0);
+        const long long o = (long long)it * P + pq;
+        hp[o] = re;
+        hp[(long long)nitems * P + o] = im;
+    }
+    keep = __syncthreads_count(keep);
+    if (threadIdx.x == 0 && keep) atomicAdd(kept, (unsigned long long)keep);
+}
+
+// ---------------------------------------------------------------------------
+// Symmetric expansion of the half-transformed integrals of one component
+// block (the role of MATMUL3's two updates, matmul3.F:75-82):
+//   M3[p][ij][plane][q] = Hp[plane][ij][pair(p,q)]
+// ---------------------------------------------------------------------------
+__global__ void k_expand(const double* __restrict__ hp, int P, int nitems, int it0, int nij,
+                         const int* __restrict__ pidx, int nc, double* __restrict__ m3) {
+    const int ijl = blockIdx.x;
+    const int it = it0 + ijl;
+    const double* hr = hp + (long long)it * P;
+    const double* hi = hp + (long long)nitems * P + (long long)it * P;
+    for (int p = blockIdx.y; p < nc; p += gridDim.y) {
+        double* row = m3 + ((long long)p * nij + ijl) * (2LL * nc);
+        for (int q = threadIdx.x; q < nc; q += blockDim.x) {
+            int pq = pidx[p * nc + q];
+            double re = 0.0, im = 0.0;
+            if (pq >= 0) { re = hr[pq]; im = hi[pq]; }
+            row[q] = re;
+            row[nc + q] = im;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// MDCINT element selection (MSUMTIM + OUTPP1/OUTPP2 + PPSYM:
+// msumtim.F:87-105, outpp1.F:43-116, outpp2.F:117-255, ppsym.F:67-91).
+// One block per record; positions (KKR, LKR) in the order PPSYM writes them;
+// an element is written when it belongs to the record's canonical set and
+// |value| > THROUT.  The value is the complete integral
+//   RL(K,L) = RLR(K,L) + s_KL RLR(Lbar,Kbar).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool in_set(int cls, int x, int y, int i, int j) {
+    // x, y, i, j 1-based Kramers indices; cls 0..3 = MDCINT classes 1..4
+    if (cls == 3) return true;
+    if (cls == 0) {
+        if (i == j) return y <= x && x <= i;
+        int a = x > y ? x : y, b = x > y ? y : x;
+        return a < i || (a == i && b <= j);
+    }
+    return y <= x && (x < i || (x == i && y <= j));
+}
+
+// mode 0 counts the elements of each record, mode 1 writes them at the
+// offsets produced by k_scan_records; both evaluate the same expressions.
+__global__ void __launch_bounds__(256) k_emit(const double* __restrict__ rlr, int m, int nij,
+                                              int K, const EmitRec* __restrict__ rec,
+                                              const int* __restrict__ kra,
+                                              const int* __restrict__ krb,
+                                              const int* __restrict__ itrmo, double throut,
+                                              int mode, OutStreams os) {
+    __shared__ int wsum[8];
+    __shared__ int base;
+    const EmitRec R = rec[blockIdx.x];
+    const int ijl = R.ijl, cls = R.cls, i = R.ikr, j = R.jkr;
+    const int ks = (cls == 2 || cls == 3) ? 1 : -1;   // class signs (rotran.F:306-328)
+    const int ls = (cls == 1 || cls == 3) ? 1 : -1;
+    const long long plane = (long long)m * nij * m;
+    long long dst = 0;
+    if (mode == 1) dst = os.off[cls][R.rank];
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int KK = K * K;
+    for (int t0 = 0; t0 < KK; t0 += blockDim.x) {
+        const int pos = t0 + threadIdx.x;
+        bool emit = false;
+        double re = 0.0, im = 0.0;
+        int x = 0, y = 0;
+        if (pos < KK) {
+            x = pos / K + 1;
+            y = pos - (x - 1) * K + 1;
+            if (in_set(cls, x, y, i, j)) {
+                const int Ks = (ks < 0 ? krb[x - 1] : kra[x - 1]) - 1;
+                const int Ls = (ls < 0 ? krb[y - 1] : kra[y - 1]) - 1;
+                const int Kb = abs(itrmo[Ks]) - 1, Lb = abs(itrmo[Ls]) - 1;
+                const double sg = ((itrmo[Ks] > 0) == (itrmo[Ls] > 0)) ? 1.0 : -1.0;
+                const long long a = ((long long)Ks * nij + ijl) * m + Ls;
+                const long long b = ((long long)Lb * nij + ijl) * m + Kb;
+                re = rlr[a] + sg * rlr[b];
+                im = rlr[plane + a] + sg * rlr[plane + b];
+            }
+            emit = hypot(re, im) > throut;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, emit);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        int off = base, tot = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            if (w < warp) off += wsum[w];
+            tot += wsum[w];
+        }
+        off += __popc(bal & ((1u << lane) - 1u));
+        if (emit && mode == 1) {
+            const long long o = dst + off;
+            os.idx[cls][2 * o] = x * ks;
+            os.idx[cls][2 * o + 1] = y * ls;
+            os.val[cls][2 * o] = re;
+            os.val[cls][2 * o + 1] = im;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) base += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && mode == 0) os.cnt[cls][R.rank] = base;
+}
+
+// Exclusive scan of the element counts of one chunk's records, per class,
+// continuing from the running class totals in os.total (single block).
+__global__ void __launch_bounds__(1024) k_scan_records(const EmitRec* __restrict__ rec, int nrec,
+                                                       OutStreams os) {
+    __shared__ long long part[1024][4];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int per = (nrec + nt - 1) / nt;
+    const int r0 = t * per, r1 = min(nrec, r0 + per);
+    long long s[4] = {0, 0, 0, 0};
+    for (int r = r0; r < r1; ++r) s[rec[r].cls] += os.cnt[rec[r].cls][rec[r].rank];
+    for (int c = 0; c < 4; ++c) part[t][c] = s[c];
+    __syncthreads();
+    if (t < 4) {  // serial scan over the 1024 partial sums of class t
+        long long run = os.total[t];
+        for (int q = 0; q < nt; ++q) {
+            long long v = part[q][t];
+            part[q][t] = run;
+            run += v;
+        }
+        os.total[t] = run;
+    }
+    __syncthreads();
+    long long o[4] = {part[t][0], part[t][1], part[t][2], part[t][3]};
+    for (int r = r0; r < r1; ++r) {
+        const int c = rec[r].cls;
+        os.off[c][rec[r].rank] = o[c];
+        o[c] += os.cnt[c][rec[r].rank];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+// ---------------------------------------------------------------------------
+void launch_scatter(cudaStream_t st, const double* rint, const int* l2, const int* l1,
+                    long long nint, const long long* rec_off, const int2* rec_meta, int nrec,
+                    const ScatterTabs& tb, double* g3, unsigned int* status) {
+    if (nint <= 0) return;
+    long long blocks = (nint + 255) / 256;
+    if (blocks > 152LL * 64) blocks = 152LL * 64;
+    k_scatter<<<(unsigned)blocks, 256, 0, st>>>(rint, l2, l1, nint, rec_off, rec_meta, nrec, tb,
+                                                 g3, status);
+}
+
+void launch_tr_select(cudaStream_t st, const double* ri, int m, int npc, int pq0, int P,
+                      const int4* items, const float* item_sign, int nitems,
+                      const double* pair_vmx, double thrgen, double* hp,
+                      unsigned long long* kept) {
+    for (int y0 = 0; y0 < nitems; y0 += 65535) {
+        int ny = nitems - y0 < 65535 ? nitems - y0 : 65535;
+        dim3 grid((npc + 255) / 256, ny);
+        k_tr_select<<<grid, 256, 0, st>>>(ri, m, npc, pq0, P, items, item_sign, y0, nitems,
+                                          pair_vmx, thrgen, hp, kept);
+    }
+}
+
+void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
+                   const int* pidx, int nc, double* m3) {
+    dim3 grid(nij, nc < 64 ? nc : 64);
+    k_expand<<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nc, m3);
+}
+
+void launch_emit(cudaStream_t st, const double* rlr, int m, int nij, int K, const EmitRec* rec,
+                 int nrec, const int* kra, const int* krb, const int* itrmo, double throut,
+                 const OutStreams& os) {
+    if (nrec <= 0) return;
+    k_emit<<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, 0, os);
+    k_scan_records<<<1, 1024, 0, st>>>(rec, nrec, os);
+    k_emit<<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, 1, os);
+}
+
+}  // namespace rt

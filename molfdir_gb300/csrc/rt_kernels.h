@@ -1,0 +1,100 @@
+// rt_kernels.h -- launchers and epilogue functors shared by the transform
+// paths.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace rt {
+
+enum : unsigned int {
+    ST_BAD_LABEL = 1u,   // a label outside 1..NSC or a non-canonical pq pair
+    ST_BAD_BLOCK = 2u,   // an integral outside the (LL|LL),(SS|LL),(SS|SS) / irrep block structure
+};
+
+// Index tables used by the record scatter (device pointers).
+struct ScatterTabs {
+    int n, mfil, nblk;
+    const unsigned char* pq_read;  // [n(n+1)/2] rotran transforms this pq bucket (makind.F:235-255)
+    const int* pair_of_orig;       // [n(n+1)/2] -> pair order or -1
+    const int* pair_group;         // [P] pair group
+    const int* pg_start;           // [npg]
+    const int* pg_size;            // [npg]
+    const int* ao_block;           // [n] AO block
+    const int* ao_pos;             // [n] position inside its block
+    const int* blk_size;           // [nblk]
+    const int* g1_of;              // [npg*nblk] GEMM1 group of (pair group, r block) or -1
+    const int* g1_kblk;            // [ng1] partner block of the group
+    const long long* g1_base;      // [ng1] offset of the group in G3
+};
+
+// One MDCINT record of the current item chunk.
+struct EmitRec {
+    int ijl;   // item inside the chunk
+    int cls;   // 0..3 = MDCINT classes 1..4
+    int ikr, jkr;
+    int rank;  // record number inside its class stream
+};
+
+// The four class streams of the MDCINT record file (device pointers).
+struct OutStreams {
+    int* cnt[4];        // elements per record
+    long long* off[4];  // first element of each record
+    int* idx[4];        // (INDK, INDL) pairs
+    double* val[4];     // (re, im) pairs
+    long long* total;   // [4] running element totals
+};
+
+// GEMM1 (batched over r): row = pq_local, col = plane*m + b
+//   -> HA[plane][r_sorted][b][pq_local]
+struct EpiHA {
+    double* ha;
+    int r0, m, npc;
+    long long plane;  // n*m*npc
+    __device__ __forceinline__ void operator()(int bz, int row, int col, double v) const {
+        int pl = col >= m;
+        int b = col - pl * m;
+        ha[pl * plane + ((long long)(r0 + bz) * m + b) * npc + row] = v;
+    }
+};
+
+// plain row-major C with leading dimension ldc (batch stride sc)
+struct EpiRowMajor {
+    double* c;
+    long long ldc, sc;
+    __device__ __forceinline__ void operator()(int bz, int row, int col, double v) const {
+        c[bz * sc + (long long)row * ldc + col] = v;
+    }
+};
+
+// GEMM3: row = p_local*nij + ijl, col = plane*m + k
+//   -> RK[plane][c0 + p][ijl][k] = plane*PS + (c0*nij + row)*m + k
+struct EpiRK {
+    double* rk;
+    int m;
+    long long rowoff;  // c0*nij
+    long long plane;   // n*nij*m
+    __device__ __forceinline__ void operator()(int, int row, int col, double v) const {
+        int pl = col >= m;
+        int k = col - pl * m;
+        rk[pl * plane + (rowoff + row) * m + k] = v;
+    }
+};
+
+template <class Epi>
+void gemm_f64(cudaStream_t st, const double* A, long long lda, long long sA, const double* B,
+              long long ldb, long long sB, int M, int N, int K, int batch, Epi epi);
+
+void launch_scatter(cudaStream_t st, const double* rint, const int* l2, const int* l1,
+                    long long nint, const long long* rec_off, const int2* rec_meta, int nrec,
+                    const ScatterTabs& tb, double* g3, unsigned int* status);
+void launch_tr_select(cudaStream_t st, const double* ri, int m, int npc, int pq0, int P,
+                      const int4* items, const float* item_sign, int nitems,
+                      const double* pair_vmx, double thrgen, double* hp,
+                      unsigned long long* kept);
+void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
+                   const int* pidx, int nc, double* m3);
+void launch_emit(cudaStream_t st, const double* rlr, int m, int nij, int K, const EmitRec* rec,
+                 int nrec, const int* kra, const int* krb, const int* itrmo, double throut,
+                 const OutStreams& os);
+
+}  // namespace rt

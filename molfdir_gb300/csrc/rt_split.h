@@ -1,0 +1,22 @@
+// rt_split.h -- split-precision (BF16 slices on the tensor cores) variants
+// of the four GEMMs of the transformation.
+#pragma once
+
+#include "rt_internal.h"
+#include "rt_kernels.h"
+
+namespace rt {
+
+void split_prepare_constants(rt_ctx* c);
+double split_stageA_bytes_per_pair(rt_ctx* c);
+double split_stageB_bytes_per_item(rt_ctx* c);
+void split_alloc_work(rt_ctx* c, int pair_chunk, int item_chunk);
+void split_prepare_g3(rt_ctx* c, int* launches);
+void split_gemm1(rt_ctx* c, const G1Group& g, int c0, int npc, const EpiHA& epi, int* launches);
+void split_gemm24(rt_ctx* c, const double* B, int K, long long N, const EpiRowMajor& epi,
+                  int* launches);
+void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& epi,
+                 int* launches);
+void split_release(rt_ctx* c);
+
+}  // namespace rt

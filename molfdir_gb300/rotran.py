@@ -1,0 +1,273 @@
+"""Python mirror of the rotran drop-in C-ABI (``include/rotran_gb300.h``).
+
+``Rotran`` wraps one library context: the calls a rotran driver makes in
+place of SR2INI/SORT1/TRANS1/SR2FLSH/TRANS2/INITTWOE/PPSYM/EXITTWOE
+(``source/rotran/rotran.F:236-333``).  Errors are raised as ``RotranError``
+carrying the Q2JOB class of the failure (``source/general/q2job.F:8-23``).
+The library has no CPU path: loading it or creating a context without a
+usable sm_103a device raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+RT_PREC_FP64 = 0
+RT_PREC_SPLIT_BF16 = 1
+
+ERROR_CLASSES = {
+    1: "end of file / missing data",
+    2: "user error (inconsistent input)",
+    3: "dimension bound exceeded",
+    4: "internal dimension error",
+    5: "non-matching parameters",
+    6: "program error",
+}
+
+
+class RotranError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[Q2JOB class {code}: {ERROR_CLASSES.get(code, '?')}] {msg}")
+        self.code = code
+
+
+class RtConfig(C.Structure):
+    _fields_ = [("nsc", C.c_int), ("nsc1", C.c_int), ("nsp", C.c_int), ("nkr", C.c_int),
+                ("mfil", C.c_int), ("breit", C.c_int), ("thrgen", C.c_double),
+                ("throut", C.c_double), ("precision", C.c_int), ("slices", C.c_int),
+                ("n_irrep", C.c_int), ("ao_irrep", C.POINTER(C.c_int)),
+                ("mem_budget", C.c_longlong)]
+
+
+class RtStats(C.Structure):
+    _fields_ = [("nhalft", C.c_longlong), ("nfinal", C.c_longlong * 4),
+                ("nrec", C.c_longlong * 4), ("ms_upload", C.c_double),
+                ("ms_scatter", C.c_double), ("ms_first", C.c_double),
+                ("ms_second", C.c_double), ("ms_output", C.c_double),
+                ("ms_total", C.c_double), ("flops_algorithmic", C.c_double),
+                ("device_bytes", C.c_longlong), ("gpu_launches", C.c_int)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["nfinal"] = list(self.nfinal)
+        d["nrec"] = list(self.nrec)
+        return d
+
+
+class RtPlanInfo(C.Structure):
+    _fields_ = [("npairs", C.c_longlong), ("nitems", C.c_longlong),
+                ("g3_bytes", C.c_longlong), ("hp_bytes", C.c_longlong),
+                ("nrec", C.c_longlong * 4), ("elem_cap", C.c_longlong * 4),
+                ("flops_algorithmic", C.c_double)]
+
+
+EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
+           "rt_add_ao_records_bulk", "rt_read_srt_files", "rt_clear_ao_records",
+           "rt_transform", "rt_result_sizes", "rt_copy_result", "rt_write_mdcint",
+           "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check"]
+
+_lib = None
+
+
+def load(build: bool = True):
+    """Load (building first if needed) the in-tree shared library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build the sm_103a library first")
+    lib = C.CDLL(path)
+    P = C.POINTER
+    vp = C.c_void_p
+    lib.rt_plan.argtypes = [P(RtConfig), P(RtPlanInfo)]
+    lib.rt_create.argtypes = [P(vp), P(RtConfig)]
+    lib.rt_set_coefficients.argtypes = [vp, P(C.c_double), C.c_int, P(C.c_int), P(C.c_int),
+                                        P(C.c_int), P(C.c_int), P(C.c_int)]
+    lib.rt_add_ao_records.argtypes = [vp, C.c_int, C.c_int, C.c_int, P(C.c_double),
+                                      P(C.c_int), P(C.c_int)]
+    lib.rt_add_ao_records_bulk.argtypes = [vp, C.c_longlong, P(C.c_int), P(C.c_longlong),
+                                           P(C.c_int), P(C.c_double), P(C.c_int), P(C.c_int)]
+    lib.rt_read_srt_files.argtypes = [vp, C.c_char_p]
+    lib.rt_clear_ao_records.argtypes = [vp]
+    lib.rt_transform.argtypes = [vp]
+    lib.rt_result_sizes.argtypes = [vp, P(C.c_longlong), P(C.c_longlong)]
+    lib.rt_copy_result.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
+    lib.rt_write_mdcint.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p]
+    lib.rt_get_stats.argtypes = [vp, P(RtStats)]
+    lib.rt_last_error.argtypes = [vp]
+    lib.rt_last_error.restype = C.c_char_p
+    lib.rt_destroy.argtypes = [vp]
+    lib.rt_destroy.restype = None
+    lib.rt_kramers_check.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_double), C.c_int,
+                                     P(C.c_int), P(C.c_double)]
+    for name in EXPORTS:
+        f = getattr(lib, name)
+        if name not in ("rt_last_error", "rt_destroy"):
+            f.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def make_config(nsc, nsc1, nkr, mfil=3, thrgen=1e-16, throut=1e-16,
+                precision=RT_PREC_FP64, slices=0, ao_irrep=None, mem_budget=0):
+    cfg = RtConfig(nsc, nsc1, 2 * nkr, nkr, mfil, 0, thrgen, throut, precision, slices,
+                   1, None, mem_budget)
+    keep = None
+    if ao_irrep is not None and int(np.max(ao_irrep)) > 0:
+        keep = np.ascontiguousarray(ao_irrep, dtype=np.int32)
+        cfg.n_irrep = 4
+        cfg.ao_irrep = _p(keep, C.c_int)
+    return cfg, keep
+
+
+def plan(cfg: RtConfig) -> RtPlanInfo:
+    lib = load()
+    out = RtPlanInfo()
+    rc = lib.rt_plan(C.byref(cfg), C.byref(out))
+    if rc:
+        raise RotranError(rc, lib.rt_last_error(None).decode())
+    return out
+
+
+def kramers_check(qa: np.ndarray, qb: np.ndarray):
+    """KRAMERS pairing (kramers.F:26-131): returns (ITRMO, max deviation)."""
+    lib = load()
+    n, m = qa.shape
+    a = np.asfortranarray(qa, dtype=np.complex128)
+    b = np.asfortranarray(qb, dtype=np.complex128)
+    itrmo = np.zeros(m, dtype=np.int32)
+    dif = C.c_double(0.0)
+    rc = lib.rt_kramers_check(n, m, a.ctypes.data_as(C.POINTER(C.c_double)),
+                              b.ctypes.data_as(C.POINTER(C.c_double)), n,
+                              _p(itrmo, C.c_int), C.byref(dif))
+    if rc:
+        raise RotranError(rc, "VECTORS SHOULD BE TRUE KRAMERS PAIRS / MOS WITHOUT KRAMERS PARTNER")
+    return itrmo, dif.value
+
+
+class Rotran:
+    """One transformation context on the current CUDA device."""
+
+    def __init__(self, cfg: RtConfig, _keep=None):
+        self.lib = load()
+        self._keep = _keep
+        self.cfg = cfg
+        h = C.c_void_p()
+        rc = self.lib.rt_create(C.byref(h), C.byref(cfg))
+        if rc:
+            raise RotranError(rc, self.lib.rt_last_error(None).decode())
+        self.h = h
+
+    @classmethod
+    def for_problem(cls, problem, **kw):
+        cfg, keep = make_config(problem.n, problem.nsc1, problem.nkr, mfil=problem.mfil,
+                                ao_irrep=problem.model.irrep if problem.model.n_irrep > 1 else None,
+                                **kw)
+        return cls(cfg, keep)
+
+    def _check(self, rc):
+        if rc:
+            raise RotranError(rc, self.lib.rt_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rt_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- inputs ---------------------------------------------------------------
+    def set_coefficients(self, qa, itrmo, kra, krb, ikrmo, imoras_pairs=None):
+        a = np.asfortranarray(qa, dtype=np.complex128)
+        it = np.ascontiguousarray(itrmo, np.int32)
+        ka = np.ascontiguousarray(kra, np.int32)
+        kb = np.ascontiguousarray(krb, np.int32)
+        ik = np.ascontiguousarray(ikrmo, np.int32)
+        im = None if imoras_pairs is None else np.ascontiguousarray(imoras_pairs, np.int32)
+        self._check(self.lib.rt_set_coefficients(
+            self.h, a.ctypes.data_as(C.POINTER(C.c_double)), a.shape[0], _p(it, C.c_int),
+            _p(ka, C.c_int), _p(kb, C.c_int), _p(ik, C.c_int),
+            None if im is None else _p(im, C.c_int)))
+
+    def set_problem_coefficients(self, problem):
+        self.set_coefficients(problem.qa, problem.itrmo, problem.kra, problem.krb,
+                              problem.ikrmo, problem.imoras_pairs())
+
+    def add_record(self, file_class, itype, rint, label2, label1):
+        v = np.ascontiguousarray(rint, np.float64)
+        a = np.ascontiguousarray(label2, np.int32)
+        b = np.ascontiguousarray(label1, np.int32)
+        self._check(self.lib.rt_add_ao_records(self.h, int(file_class), int(v.size), int(itype),
+                                               _p(v, C.c_double), _p(a, C.c_int), _p(b, C.c_int)))
+
+    def add_records_bulk(self, file_class, nt, itype, rint, label2, label1):
+        fc = np.ascontiguousarray(file_class, np.int32)
+        n = np.ascontiguousarray(nt, np.int64)
+        it = np.ascontiguousarray(itype, np.int32)
+        v = np.ascontiguousarray(rint, np.float64)
+        a = np.ascontiguousarray(label2, np.int32)
+        b = np.ascontiguousarray(label1, np.int32)
+        self._check(self.lib.rt_add_ao_records_bulk(
+            self.h, int(fc.size), _p(fc, C.c_int), _p(n, C.c_longlong), _p(it, C.c_int),
+            _p(v, C.c_double), _p(a, C.c_int), _p(b, C.c_int)))
+
+    def add_problem_records(self, problem, bulk=True):
+        if bulk:
+            self.add_records_bulk(*problem.flat_records())
+        else:
+            for cls, r in problem.all_records():
+                self.add_record(cls, r.it, r.rint, r.label2, r.label1)
+
+    def read_srt_files(self, directory):
+        self._check(self.lib.rt_read_srt_files(self.h, os.fsencode(directory)))
+
+    def clear_records(self):
+        self._check(self.lib.rt_clear_ao_records(self.h))
+
+    # -- run ------------------------------------------------------------------
+    def transform(self):
+        self._check(self.lib.rt_transform(self.h))
+
+    def result_sizes(self):
+        nr, nz = C.c_longlong(), C.c_longlong()
+        self._check(self.lib.rt_result_sizes(self.h, C.byref(nr), C.byref(nz)))
+        return nr.value, nz.value
+
+    def result(self, hdr=None, idx=None, val=None):
+        """MDCINT record stream: (hdr (nrec,3), idx (nz,2), val (nz,) complex)."""
+        nr, nz = self.result_sizes()
+        hdr = np.empty((nr, 3), np.int32) if hdr is None else hdr
+        idx = np.empty((nz, 2), np.int32) if idx is None else idx
+        val = np.empty(nz, np.complex128) if val is None else val
+        self._check(self.lib.rt_copy_result(self.h, _p(hdr, C.c_int), _p(idx, C.c_int),
+                                            val.ctypes.data_as(C.POINTER(C.c_double))))
+        return hdr, idx, val
+
+    def write_mdcint(self, path, datex="", timex=""):
+        self._check(self.lib.rt_write_mdcint(self.h, os.fsencode(path), datex.encode()[:10],
+                                             timex.encode()[:8]))
+
+    def stats(self):
+        s = RtStats()
+        self._check(self.lib.rt_get_stats(self.h, C.byref(s)))
+        return s

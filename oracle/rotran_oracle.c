@@ -34,6 +34,10 @@
  *      that ITYP 1 has at outpp2.F:186, so a diagonal source record would
  *      add its (a,a) element twice to class-4 records.  The guard is applied
  *      here; with it every MDCINT element equals the complete integral.
+ *  (4) With a one-slot PPSYM buffer (NC2 = 1, e.g. NKR = 1) the end-of-file
+ *      record of INTSKEL1 lands in a fresh slot and ppsym.F:67-92 writes it
+ *      as a record 0,0,0 inside the class stream, which the readers take for
+ *      the end of MDCINT (goscip/rdtwo.F:31).  That record is not written.
  */
 #include <math.h>
 #include <stdint.h>
@@ -396,7 +400,7 @@ static long ppsym(const skfile* f, const pplist* bk, int nsksiz, int nc2, int nk
                     }
                 }
             }
-            for (int jc2 = 1; jc2 <= ic2; jc2++) {
+            for (int jc2 = 1; jc2 <= ic2 && ikrc != 0; jc2++) { /* deviation (4) */
                 int jkra = icind[jc2];
                 md_rec(out, ikrc * is, jkra * js);
                 long ix = 0;
