@@ -1,0 +1,291 @@
+"""Throughput of the GB300 rotran four-index transformation.
+
+One step = one complete transformation (record scatter, both
+half-transformations, MDCINT selection) of the precision-study workload:
+160 large + 240 small component functions (n = 400), 120 Kramers pairs,
+seeded synthetic integrals (about 8.7e8 unique (LL|LL), (SS|LL) and (SS|SS)
+integrals, 14 GB of records, larger than L2).  ``value`` is the algorithmic
+FLOP rate with the integral records already resident in device memory;
+``e2e`` repeats the step through the public API from pinned host memory,
+host->device copy of the records and device->host copy of the MDCINT
+stream included.  ``--impl reference`` times the CPU restatement of rotran
+(the reference is Fortran 77 and cannot be built here) on a bounded sample of
+the same workload with all host cores.
+
+Multi-GPU: every rank runs an independent replica of the workload (no
+collective on the data path); value = all ranks' work / max rank time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="precision_study_n400_k120", n_l=160, n_s=240, nkr=120, seed=0)
+SMALL = dict(name="c1_n64_k32", n_l=24, n_s=40, nkr=32, seed=0)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    except OSError:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def barrier_max(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(work, steps=1, warmup=0, seconds=15.0):
+    """CPU restatement of rotran on a bounded sample of the workload:
+    TRANS1 over the first pq blocks and TRANS2 over the first items with
+    full-length half-transformed lists; returns (GFLOP/s, cores, sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from molfdir_gb300 import synth
+    cores = os.cpu_count() or 1
+    p = synth.make_spinor_problem(work["n_l"], work["n_s"], work["nkr"], seed=work["seed"])
+    res = pyoracle.time_sample(p, seconds=seconds, nthreads=cores, steps=steps, warmup=warmup)
+    return res, cores
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "split", "fp64"])
+    ap.add_argument("--workload", default="precision", choices=["precision", "c1"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    work = WORKLOAD if args.workload == "precision" else SMALL
+    rank, world, local = dist_env()
+    hbm_peak, bf16_peak, peak_kind = peaks()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        res, cores = cpu_sample(work, steps=args.steps, warmup=args.warmup)
+        line = {"metric": "4-index transform TFLOP/s", "impl": "reference",
+                "value": res["tflops"], "unit": "TFLOP/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": res["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": work["name"], "n": work["n_l"] + work["n_s"],
+                           "nkr": work["nkr"], "seed": work["seed"]},
+                "cpu_baseline": {"value": res["tflops"], "unit": "TFLOP/s", "cores": cores,
+                                 "kind": "port", "sample": res["sample"]},
+                "e2e": {"value": res["tflops"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from molfdir_gb300 import rotran, synth
+
+    prec_name = args.precision
+    if prec_name == "auto":
+        prec_name = "split" if rotran_split_available() else "fp64"
+    prec = rotran.RT_PREC_SPLIT_BF16 if prec_name == "split" else rotran.RT_PREC_FP64
+
+    prob = synth.make_spinor_problem(work["n_l"], work["n_s"], work["nkr"], seed=work["seed"])
+    cls, its, nts, dv, dl2, dl1 = synth.device_records(prob, 3, device="cuda")
+    torch.cuda.synchronize()
+    nint = int(nts.sum())
+
+    def make_ctx():
+        rt = rotran.Rotran.for_problem(prob, precision=prec)
+        rt.set_problem_coefficients(prob)
+        return rt
+
+    # ---- value: records resident in HBM ----
+    rt = make_ctx()
+    rt.add_records_bulk_device(cls, nts, its, dv, dl2, dl1)
+    for _ in range(args.warmup):
+        rt.transform()
+    barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
+    barrier()
+    torch.cuda.synchronize()
+    gemm_ms, step_ms = [], []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rt.transform()
+            st = rt.stats()
+            gemm_ms.append(st.ms_gemm)
+            step_ms.append(st.ms_total)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+    barrier()
+    wall = (t1 - t0) / args.steps
+    dev_ms = statistics.mean(step_ms)
+    sec = barrier_max(max(wall, dev_ms / 1e3), world)
+    flops = st.flops_algorithmic
+    value = flops * world / sec / 1e12
+    nrec, nz = rt.result_sizes()
+    launches = st.gpu_launches * args.steps
+    roof_achieved = st.flops_gemm_executed / (statistics.mean(gemm_ms) / 1e3) / 1e12
+    rt_stats = st.as_dict()
+    rt.close()
+
+    # ---- e2e through the public API with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        hv, h2, h1 = (x.cpu().pin_memory() for x in (dv, dl2, dl1))
+        rt = make_ctx()
+        hdr = np.empty((nrec, 3), np.int32)
+        idx = torch.empty((nz, 2), dtype=torch.int32).pin_memory()
+        val = torch.empty((nz, 2), dtype=torch.float64).pin_memory()
+        idx_np, val_np = idx.numpy(), val.numpy().view(np.complex128).reshape(-1)
+
+        def e2e_step():
+            rt.clear_records()
+            rt.add_records_bulk_ptr(cls, nts, its, hv.data_ptr(), h2.data_ptr(), h1.data_ptr())
+            rt.transform()
+            rt.result(hdr, idx_np, val_np)
+
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        ne = max(1, min(args.steps, 2))
+        for _ in range(ne):
+            e2e_step()
+        t1 = time.perf_counter()
+        esec = barrier_max((t1 - t0) / ne, world)
+        e2e = {"value": flops * world / esec / 1e12, "unit": "TFLOP/s",
+               "h2d_bytes_per_step": nint * 16, "d2h_bytes_per_step": nz * 24 + nrec * 12,
+               "ms_per_step": esec * 1e3}
+        rt.close()
+        del hv, h2, h1
+
+    # ---- CPU baseline (rank 0, N = 1) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        res, cores = cpu_sample(work)
+        cpu = {"value": res["tflops"], "unit": "TFLOP/s", "cores": cores, "kind": "port",
+               "sample": res["sample"]}
+
+    if rank == 0:
+        if prec_name == "split":
+            bound, peak, unit = "tensor", bf16_peak, "TFLOP/s"
+        else:
+            bound, peak, unit = "fp64", None, "TFLOP/s"
+        line = {
+            "metric": "4-index transform TFLOP/s", "value": value, "unit": "TFLOP/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x-split/f64" if prec_name == "split" else "f64",
+            "data": "synthetic",
+            "config": {"workload": work["name"], "n": prob.n, "n_large": work["n_l"],
+                       "n_small": work["n_s"], "nkr": work["nkr"], "seed": work["seed"],
+                       "precision": prec_name, "integrals": nint,
+                       "l2": "inputs larger than L2 (records 16 B x integrals)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": bound, "achieved": roof_achieved, "peak": peak, "unit": unit,
+                         "frac": (roof_achieved / peak) if peak else None, "traffic": None,
+                         "kernel": "half-transformation GEMMs", "peak_kind": peak_kind},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(), "stats": rt_stats,
+            "mdcint": {"records": nrec, "elements": nz},
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def rotran_split_available():
+    return os.environ.get("ROTRAN_BENCH_SPLIT", "0") == "1"
+
+
+if __name__ == "__main__":
+    main()

@@ -70,6 +70,9 @@ typedef struct rt_stats {
     double flops_algorithmic; /* algorithmic FLOPs of the transform (dense-block count) */
     long long device_bytes;   /* peak device memory held by the context */
     int gpu_launches;         /* kernels launched by the last rt_transform */
+    int gemm_launches;        /* of which GEMM (half-transformation) kernels */
+    double ms_gemm;           /* summed device time of the GEMM kernels */
+    double flops_gemm_executed; /* FLOPs the GEMM kernels executed (slice products included) */
 } rt_stats;
 
 /* Sizes of a transformation, computed on the host without a device: the
@@ -110,7 +113,7 @@ int rt_add_ao_records(rt_ctx* ctx, int file_class, int nt, int itype, const doub
 
 /* Many records at once: nrec records, record r holds nt[r] integrals of
  * type itype[r] from file file_class[r]; rint/label2/label1 are the records
- * concatenated. */
+ * concatenated and may be host or device memory of the current device. */
 int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* file_class, const long long* nt,
                            const int* itype, const double* rint, const int* label2,
                            const int* label1);

@@ -93,14 +93,15 @@ template <class Epi>
 __global__ void __launch_bounds__(256) k_gemm_f64(const double* __restrict__ A, long long lda,
                                                   long long sA, const double* __restrict__ B,
                                                   long long ldb, long long sB, int M, int N, int K,
-                                                  Epi epi) {
+                                                  int mx, Epi epi) {
     __shared__ double As[16][65];
     __shared__ double Bs[16][64];
     const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
     const int bz = blockIdx.z;
     const double* Ab = A + (long long)bz * sA;
     const double* Bb = B + (long long)bz * sB;
-    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    // the larger of the two tile counts runs along grid.x (no 65535 limit)
+    const int m0 = (mx ? blockIdx.x : blockIdx.y) * 64, n0 = (mx ? blockIdx.y : blockIdx.x) * 64;
     double acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -148,8 +149,11 @@ __global__ void __launch_bounds__(256) k_gemm_f64(const double* __restrict__ A, 
 template <class Epi>
 void gemm_f64(cudaStream_t st, const double* A, long long lda, long long sA, const double* B,
               long long ldb, long long sB, int M, int N, int K, int batch, Epi epi) {
-    dim3 grid((N + 63) / 64, (M + 63) / 64, batch);
-    k_gemm_f64<Epi><<<grid, 256, 0, st>>>(A, lda, sA, B, ldb, sB, M, N, K, epi);
+    const unsigned tm = (M + 63) / 64, tn = (N + 63) / 64;
+    const int mx = tm > tn;
+    dim3 grid(mx ? tm : tn, mx ? tn : tm, batch);
+    if (grid.y > 65535u || grid.z > 65535u) throw_dim("GEMM grid too large");
+    k_gemm_f64<Epi><<<grid, 256, 0, st>>>(A, lda, sA, B, ldb, sB, M, N, K, mx, epi);
 }
 
 template void gemm_f64<EpiHA>(cudaStream_t, const double*, long long, long long, const double*,

@@ -80,6 +80,9 @@ struct EpiRK {
     }
 };
 
+// raises the library's dimension error (defined in rt_api.cu)
+[[noreturn]] void throw_dim(const char* what);
+
 template <class Epi>
 void gemm_f64(cudaStream_t st, const double* A, long long lda, long long sA, const double* B,
               long long ldb, long long sB, int M, int N, int K, int batch, Epi epi);

@@ -13,5 +13,6 @@ void split_gemm1(rt_ctx*, const G1Group&, int, int, const EpiHA&, int*) { not_bu
 void split_gemm24(rt_ctx*, const double*, int, long long, const EpiRowMajor&, int*) { not_built(); }
 void split_gemm3(rt_ctx*, int, const double*, int, int, const EpiRK&, int*) { not_built(); }
 void split_release(rt_ctx*) {}
+double split_flop_factor(rt_ctx*) { return 1.0; }
 
 }  // namespace rt

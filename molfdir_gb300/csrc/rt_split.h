@@ -18,5 +18,7 @@ void split_gemm24(rt_ctx* c, const double* B, int K, long long N, const EpiRowMa
 void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& epi,
                  int* launches);
 void split_release(rt_ctx* c);
+// executed FLOPs per algorithmic FLOP of a split GEMM (slice products)
+double split_flop_factor(rt_ctx* c);
 
 }  // namespace rt

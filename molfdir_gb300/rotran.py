@@ -50,7 +50,9 @@ class RtStats(C.Structure):
                 ("ms_scatter", C.c_double), ("ms_first", C.c_double),
                 ("ms_second", C.c_double), ("ms_output", C.c_double),
                 ("ms_total", C.c_double), ("flops_algorithmic", C.c_double),
-                ("device_bytes", C.c_longlong), ("gpu_launches", C.c_int)]
+                ("device_bytes", C.c_longlong), ("gpu_launches", C.c_int),
+                ("gemm_launches", C.c_int), ("ms_gemm", C.c_double),
+                ("flops_gemm_executed", C.c_double)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -231,9 +233,26 @@ class Rotran:
             self.h, int(fc.size), _p(fc, C.c_int), _p(n, C.c_longlong), _p(it, C.c_int),
             _p(v, C.c_double), _p(a, C.c_int), _p(b, C.c_int)))
 
+    def add_records_bulk_ptr(self, file_class, nt, itype, p_rint, p_label2, p_label1):
+        """Bulk records from raw host or device pointers (cudaMemcpyDefault)."""
+        fc = np.ascontiguousarray(file_class, np.int32)
+        n = np.ascontiguousarray(nt, np.int64)
+        it = np.ascontiguousarray(itype, np.int32)
+        self._check(self.lib.rt_add_ao_records_bulk(
+            self.h, int(fc.size), _p(fc, C.c_int), _p(n, C.c_longlong), _p(it, C.c_int),
+            C.cast(C.c_void_p(p_rint), C.POINTER(C.c_double)),
+            C.cast(C.c_void_p(p_label2), C.POINTER(C.c_int)),
+            C.cast(C.c_void_p(p_label1), C.POINTER(C.c_int))))
+
+    def add_records_bulk_device(self, file_class, nt, itype, rint, label2, label1):
+        """Bulk records held in torch tensors (device or host)."""
+        self.add_records_bulk_ptr(file_class, nt, itype, rint.data_ptr(), label2.data_ptr(),
+                                  label1.data_ptr())
+
     def add_problem_records(self, problem, bulk=True):
         if bulk:
-            self.add_records_bulk(*problem.flat_records())
+            cls, its, nts, v, l2, l1 = problem.flat_records()
+            self.add_records_bulk(cls, nts, its, v, l2, l1)
         else:
             for cls, r in problem.all_records():
                 self.add_record(cls, r.it, r.rint, r.label2, r.label1)

@@ -390,3 +390,142 @@ def dense_ao_tensor(model: AOModel, mfil: int = 3) -> np.ndarray:
                 for (z, w) in ((c, d), (d, c)):
                     g[x[:, None], y[:, None], z[None, :], w[None, :]] = v
     return g
+
+
+# ---------------------------------------------------------------------------
+# device-side record generation for the large workloads (torch, same model)
+# ---------------------------------------------------------------------------
+
+def _inttyp_torch(i, j, k, l):
+    import torch
+    out = torch.zeros_like(i, dtype=torch.int8)
+    kgj = k > j
+    w = torch.where
+    a = kgj & (j > l)
+    out = w(a & (i != k), 13, out); out = w(a & (i == k), 10, out)
+    b = kgj & ~(j > l)
+    out = w(b & (j != l) & (k != l), 14, out); out = w(b & (j != l) & (k == l), 8, out)
+    out = w(b & (j == l) & (i != k), 11, out); out = w(b & (j == l) & (i == k), 2, out)
+    c = ~kgj & (k != l)
+    out = w(c & (i != j) & (j != k), 12, out); out = w(c & (i != j) & (j == k), 9, out)
+    out = w(c & (i == j) & (j != k), 5, out); out = w(c & (i == j) & (j == k), 4, out)
+    d = ~kgj & (k == l)
+    out = w(d & (j != k) & (i != j), 7, out); out = w(d & (j != k) & (i == j), 3, out)
+    out = w(d & (j == k) & (i != j), 6, out); out = w(d & (j == k) & (i == j), 1, out)
+    return out.to(torch.int8)
+
+
+def device_records(problem_or_model, mfil: int = 3, device="cuda", chunk: int = 4096):
+    """All integral records of a problem generated on a CUDA device.
+
+    Returns ``(file_class, itype, nt)`` host arrays (one record per file and
+    integral type) and device tensors ``(rint, label2, label1)`` holding the
+    records concatenated in that order.  Values equal ``_file_integrals`` up
+    to the summation order of the B B^T products.
+    """
+    import torch
+    model = problem_or_model.model if hasattr(problem_or_model, "model") else problem_or_model
+    irr = torch.as_tensor(model.irrep, device=device, dtype=torch.int32)
+    files = [("LL", 1)]
+    if mfil >= 2 and model.n_s > 0:
+        files.append(("SL", 2))
+    if mfil >= 3 and model.n_s > 0:
+        files.append(("SS", 3))
+    tl = (torch.as_tensor(model.pl, device=device).long(), torch.as_tensor(model.ql, device=device).long(),
+          torch.as_tensor(model.bl, device=device))
+    ts = (torch.as_tensor(model.ps, device=device).long(), torch.as_tensor(model.qs, device=device).long(),
+          torch.as_tensor(model.bs, device=device))
+    cls_l, it_l, nt_l, vs, l2s, l1s = [], [], [], [], [], []
+    for key, fc in files:
+        (pa, qa_, ba), (pc, qc, bc), tri = {
+            "LL": (tl, tl, True), "SL": (ts, tl, False), "SS": (ts, ts, True)}[key]
+        ga = irr[pa - 1] ^ irr[qa_ - 1]
+        gc = irr[pc - 1] ^ irr[qc - 1]
+        fv, f2, f1, ft = [], [], [], []
+        for s0 in range(0, pa.numel(), chunk):
+            s1 = min(pa.numel(), s0 + chunk)
+            ncd = s1 if tri else pc.numel()
+            g = ba[s0:s1] @ bc[:ncd].T
+            mask = torch.ones_like(g, dtype=torch.bool)
+            if tri:
+                rows = torch.arange(s0, s1, device=device)[:, None]
+                cols = torch.arange(ncd, device=device)[None, :]
+                mask &= cols <= rows
+            if model.n_irrep > 1:
+                mask &= ga[s0:s1, None] == gc[None, :ncd]
+            ri, ci = torch.nonzero(mask, as_tuple=True)
+            a, b, c, d = pa[s0 + ri], qa_[s0 + ri], pc[ci], qc[ci]
+            fv.append(g[ri, ci])
+            f2.append(((a << 16) | b).to(torch.int32))
+            f1.append(((c << 16) | d).to(torch.int32))
+            ft.append(_inttyp_torch(a, b, c, d))
+            del g, mask, ri, ci
+        v, l2, l1, it = (torch.cat(x) for x in (fv, f2, f1, ft))
+        order = torch.argsort(it, stable=True)
+        v, l2, l1, it = v[order], l2[order], l1[order], it[order]
+        counts = torch.bincount(it.long(), minlength=15).cpu().numpy()
+        for t in range(1, 15):
+            if counts[t]:
+                cls_l.append(fc); it_l.append(t); nt_l.append(int(counts[t]))
+        vs.append(v); l2s.append(l2); l1s.append(l1)
+        del order, it
+    return (np.asarray(cls_l, np.int32), np.asarray(it_l, np.int32), np.asarray(nt_l, np.int64),
+            torch.cat(vs), torch.cat(l2s), torch.cat(l1s))
+
+
+def make_spinor_problem(n_l: int, n_s: int, nkr: int, seed: int = 0, n_irrep: int = 1,
+                        mfil: int = 3) -> Problem:
+    """Model and spinors of a workload without host-side integral records
+    (for the device-side record generation of large workloads)."""
+    rng = np.random.default_rng(seed)
+    model = make_ao_model(n_l, n_s, rng, n_irrep=n_irrep)
+    qa, qb, itrmo, kra, krb, ikrmo = make_spinors(model.n, nkr, rng)
+    return Problem(model, nkr, qa, qb, itrmo, kra, krb, ikrmo, mfil, {})
+
+
+def bucket_records(model: AOModel, pq_pairs, mfil: int = 3):
+    """The integral records rotran sorts into the given pq buckets.
+
+    Bucket pq (label1) holds (rs|pq) with rs >= pq of the same class
+    ((LL|LL) or (SS|SS)) and, for an LL pair, every (SS|LL) integral
+    (sort1.F:136-200).  Returns flat record arrays like
+    ``Problem.flat_records`` (one record per file and type).
+    """
+    nl = model.n_l
+    lidx = {(int(p), int(q)): i for i, (p, q) in enumerate(zip(model.pl, model.ql))}
+    sidx = {(int(p), int(q)): i for i, (p, q) in enumerate(zip(model.ps, model.qs))}
+    irr = model.irrep
+    out = {}
+    for (p, q) in pq_pairs:
+        cls_pq = "L" if p <= nl else "S"
+        if cls_pq == "L":
+            t = lidx[(p, q)]
+            parts = [(1, model.pl[t:], model.ql[t:], model.bl[t:], model.bl[t])]
+            if mfil >= 2 and model.n_s:
+                parts.append((2, model.ps, model.qs, model.bs, model.bl[t]))
+        else:
+            if mfil < 3:
+                continue
+            t = sidx[(p, q)]
+            parts = [(3, model.ps[t:], model.qs[t:], model.bs[t:], model.bs[t])]
+        for fc, a, b, brs, bpq in parts:
+            v = brs @ bpq
+            keep = np.ones(v.size, dtype=bool)
+            if model.n_irrep > 1:
+                keep = (irr[a - 1] ^ irr[b - 1]) == (irr[p - 1] ^ irr[q - 1])
+            a, b, v = a[keep], b[keep], v[keep]
+            c = np.full(a.size, p, np.int64)
+            d = np.full(a.size, q, np.int64)
+            it = inttyp(a, b, c, d)
+            l2 = ((a.astype(np.int64) << 16) | b).astype(np.int32)
+            l1 = ((c << 16) | d).astype(np.int32)
+            for ty in np.unique(it):
+                m_ = it == ty
+                out.setdefault((fc, int(ty)), []).append((v[m_], l2[m_], l1[m_]))
+    keys = sorted(out)
+    cls = np.asarray([k[0] for k in keys], np.int32)
+    its = np.asarray([k[1] for k in keys], np.int32)
+    nts = np.asarray([sum(x[0].size for x in out[k]) for k in keys], np.int64)
+    cat = lambda j, dt: (np.concatenate([x[j] for k in keys for x in out[k]]).astype(dt)
+                         if keys else np.zeros(0, dt))
+    return cls, its, nts, cat(0, np.float64), cat(1, np.int32), cat(2, np.int32)

@@ -31,7 +31,8 @@ class _Params(C.Structure):
     _fields_ = [("nsc", C.c_int), ("nsc1", C.c_int), ("nsp", C.c_int), ("nkr", C.c_int),
                 ("mfil", C.c_int), ("quater", C.c_int), ("thrgen", C.c_double),
                 ("throut", C.c_double), ("nthreads", C.c_int), ("limit_pq", C.c_long),
-                ("limit_ij", C.c_long)]
+                ("limit_ij", C.c_long), ("pq_select", C.POINTER(C.c_long)),
+                ("n_pq_select", C.c_long), ("fake_list_len", C.c_long)]
 
 
 class _Result(C.Structure):
@@ -77,13 +78,16 @@ def _ptr(a, t):
 
 
 def run(problem, thrgen=1e-16, throut=1e-16, nthreads=0, limit_pq=0, limit_ij=0,
-        quater=True) -> MdcintImage:
+        quater=True, records=None, pq_select=None, fake_list_len=0) -> MdcintImage:
     lib = _load()
-    cls, its, nts, v, l2, l1 = problem.flat_records()
+    cls, its, nts, v, l2, l1 = problem.flat_records() if records is None else records
     qa = np.asfortranarray(problem.qa).astype(np.complex128)
     qa_flat = np.ascontiguousarray(qa.T).reshape(-1)  # column-major QA(p,i)
+    sel = None if pq_select is None else np.ascontiguousarray(pq_select, np.int64)
     prm = _Params(problem.n, problem.nsc1, problem.m, problem.nkr, problem.mfil,
-                  1 if quater else 0, thrgen, throut, nthreads, limit_pq, limit_ij)
+                  1 if quater else 0, thrgen, throut, nthreads, limit_pq, limit_ij,
+                  None if sel is None else _ptr(sel, C.c_long),
+                  0 if sel is None else sel.size, fake_list_len)
     res = _Result()
     itrmo = np.ascontiguousarray(problem.itrmo, np.int32)
     kra = np.ascontiguousarray(problem.kra, np.int32)
@@ -119,3 +123,51 @@ def inttyp(a, b, c, d):
 
 def gettw_factor(it):
     return _load().orc_gettw_factor(it)
+
+
+def time_sample(problem, seconds=15.0, nthreads=0, steps=1, warmup=0):
+    """Time the restatement on a bounded sample of a (large) workload.
+
+    TRANS1 runs over pq blocks spread evenly over the transformed blocks
+    (their integral buckets generated on the host), TRANS2 over the first
+    items with half-transformed lists of the full length (one entry per
+    transformed pq block).  The sample is sized to take about ``seconds``.
+    Returns the algorithmic TFLOP/s of the sample (same per-block and
+    per-item FLOP counts as the GPU library) and a description.
+    """
+    from molfdir_gb300 import synth
+    model = problem.model
+    nl, ns, n, m, k = model.n_l, model.n_s, problem.n, problem.m, problem.nkr
+    pairs = [(p, q) for p in range(1, n + 1) for q in range(1, p + 1)
+             if (p <= nl) == (q <= nl) and (p <= nl or problem.mfil >= 3)]
+    P = len(pairs)
+    blk = nl * nl + ns * ns
+    f_pq = 4.0 * blk * m + 8.0 * n * m * m
+    f_it = 8.0 * blk * m + 8.0 * n * m * m
+    # calibration run
+    npq, nit = 8, 4
+    for attempt in range(3):
+        idx = np.linspace(0, P - 1, npq).round().astype(int)
+        sel_pairs = [pairs[i] for i in idx]
+        recs = synth.bucket_records(model, sel_pairs, problem.mfil)
+        sel = [p * (p - 1) // 2 + q for p, q in sel_pairs]
+        img = run(problem, nthreads=nthreads, records=recs, pq_select=sel, limit_ij=nit,
+                  fake_list_len=P)
+        t1, t2 = img.times[0], img.times[1]
+        if attempt == 2 or t1 + t2 > 0.5 * seconds:
+            break
+        npq = max(npq, int(npq * 0.5 * seconds / max(t1, 1e-3)))
+        nit = max(nit, int(nit * 0.5 * seconds / max(t2, 1e-3)))
+        npq, nit = min(npq, P), min(nit, k * (k + 1))
+    times = []
+    for s in range(warmup + steps):
+        img = run(problem, nthreads=nthreads, records=recs, pq_select=sel, limit_ij=nit,
+                  fake_list_len=P)
+        if s >= warmup:
+            times.append(img.times[0] + img.times[1])
+    t = float(np.mean(times))
+    flops = img.npq_done * f_pq + img.nij_done * f_it
+    return {"tflops": flops / t / 1e12, "ms_per_step": t * 1e3,
+            "sample": (f"TRANS1 over {img.npq_done} of {P} pq blocks (evenly spaced) + TRANS2 over "
+                       f"{img.nij_done} of {k * (k + 1)} Kramers pairs with full-length "
+                       f"half-transformed lists; algorithmic FLOPs {flops:.3e}")}

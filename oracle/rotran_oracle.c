@@ -524,8 +524,15 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     {
         long* pqlist = (long*)malloc(sizeof(long) * (nsctr + 1));
         long npql = 0;
-        for (long pq = 1; pq <= nsctr && npql < pq_limit; pq++)
-            if (bstart[pq + 1] > bstart[pq]) pqlist[npql++] = pq;
+        if (prm->pq_select) {
+            for (long t = 0; t < prm->n_pq_select; t++) {
+                long pq = prm->pq_select[t];
+                if (pq >= 1 && pq <= nsctr && bstart[pq + 1] > bstart[pq]) pqlist[npql++] = pq;
+            }
+        } else {
+            for (long pq = 1; pq <= nsctr && npql < pq_limit; pq++)
+                if (bstart[pq + 1] > bstart[pq]) pqlist[npql++] = pq;
+        }
         npq_done = npql;
 #pragma omp parallel
         {
@@ -626,6 +633,23 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     }
     free(hstore);
     free(hkeep);
+    if (prm->fake_list_len > 0) {
+        /* timing sample: every JI list has fake_list_len entries */
+        long L = prm->fake_list_len;
+        free(hval); free(hp); free(hq);
+        hval = (cplx*)malloc(sizeof(cplx) * L * nji);
+        hp = (int*)malloc(sizeof(int) * L * nji);
+        hq = (int*)malloc(sizeof(int) * L * nji);
+        for (int ji = 0; ji <= nji; ji++) jcnt[ji + 1] = (long)ji * L;
+        jcnt[0] = 0;
+        for (long x = 0; x < L * nji; x++) {
+            long t = x % L;
+            int ip = 1 + (int)(t % n), iq = 1 + (int)((t / n) % ip);
+            hp[x] = ip; hq[x] = iq;
+            hval[x].re = 1e-3 * (double)(x % 7); hval[x].im = -1e-3 * (double)(x % 5);
+        }
+        nhalft = L * nji;
+    }
     double t1 = now_s();
 
     /* ---------------- TRANS2 (trans2.F:68-326), one quaternionic irrep ---------------- */

@@ -18,6 +18,10 @@ typedef struct orc_params {
     int nthreads;          /* OpenMP threads (0: runtime default) */
     long limit_pq;         /* >0: transform only the first limit_pq pq blocks */
     long limit_ij;         /* >0: only the first limit_ij TRANS2 pairs */
+    const long* pq_select; /* optional list of pq blocks (p(p-1)/2+q) to transform */
+    long n_pq_select;
+    long fake_list_len;    /* >0 (timing samples): TRANS2 reads lists of this
+                              length with synthetic values instead of TRANS1's */
 } orc_params;
 
 typedef struct orc_result {

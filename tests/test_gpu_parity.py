@@ -73,7 +73,7 @@ def test_fp64_thresholds(thrgen, throut):
     # screens the complete half-transformed integrals), so only the
     # default-threshold runs are compared element for element
     tol = TOL_FP64 if thrgen <= 1e-16 else 1e-4
-    assert compare_streams(got, ref, tol) <= tol
+    assert compare_streams(got, ref, tol, presence_tol=max(tol, 2 * throut)) <= tol
 
 
 def test_per_record_calls_and_srt_files_match_bulk(tmp_path):

@@ -23,13 +23,17 @@ def permute_spinors(problem, perm):
     return p
 
 
-def compare_streams(got, ref, tol):
+def compare_streams(got, ref, tol, presence_tol=None):
     """Same records in the same order, same element labels, values within tol.
 
-    got/ref: (hdr, idx, val).  Returns the max |difference|.  Elements whose
-    presence differs (a value within rounding of THROUT) are accepted only
-    if both values are below tol.
+    got/ref: (hdr, idx, val).  Returns the max |difference| over elements
+    present in both.  An element present in only one stream is accepted when
+    both its values are at most ``presence_tol`` (default ``tol``): a value
+    within rounding of THROUT, or, for a large THROUT, an integral whose
+    canonical and particle-interchanged halves the reference filters
+    separately (outpp1.F:76, outpp2.F:156) while the GPU filters the sum.
     """
+    presence_tol = tol if presence_tol is None else presence_tol
     gh, gi, gv = got
     rh, ri, rv = ref
     assert gh.shape[0] == rh.shape[0], f"record count {gh.shape[0]} != {rh.shape[0]}"
@@ -45,7 +49,9 @@ def compare_streams(got, ref, tol):
         for k in set(a) | set(b):
             va, vb = a.get(k, 0.0), b.get(k, 0.0)
             if (k in a) != (k in b):
-                assert abs(va) <= tol and abs(vb) <= tol, f"record {r} element {k}: {va} vs {vb}"
+                assert abs(va) <= presence_tol and abs(vb) <= presence_tol, \
+                    f"record {r} element {k}: {va} vs {vb}"
+                continue
             err = max(err, abs(va - vb))
         ka = [k for k in gi[go[r]:go[r + 1]].tolist() if tuple(k) in b]
         kb = [k for k in ri[ro[r]:ro[r + 1]].tolist() if tuple(k) in a]
