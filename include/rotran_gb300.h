@@ -149,6 +149,16 @@ int rt_get_stats(rt_ctx* ctx, rt_stats* out);
 const char* rt_last_error(rt_ctx* ctx);
 void rt_destroy(rt_ctx* ctx);
 
+/* C = A B (row-major FP64 host matrices, M x K times K x N) computed by the
+ * split-precision engine of the transformation (BF16 digit slices on the
+ * tensor cores, exact FP32 accumulation of the two leading slice products,
+ * float-float recombination).  mode 0 slices both operands on the host;
+ * mode 1 rounds A and B to float-float and slices them on the device, as
+ * the intermediate quarter-transforms are; mode 2 slices FP64 rows of A on
+ * the device, as the first quarter-transform does.  K <= 1024. */
+int rt_split_dgemm(int M, int N, int K, const double* A, const double* B, double* C, int slices,
+                   int mode);
+
 /* KRAMERS pairing check (kramers.F:26-131) on host data: finds the
  * time-reversal partner of every spinor (tolerance 1e-10), writes ITRMO and
  * the largest deviation; returns RT_ERR_PROGRAM, like the reference's

@@ -774,7 +774,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             else
                 gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2), ++launches;
             gemm_end(2.0 * 2 * m * (double)m * npc * 2 * n * sfac);
-            launch_tr_select(st, ri, m, npc, pg.start + c0, P.P, d_items, d_isign, KK1, d_pvmx,
+            launch_tr_select(st, split, ri, m, npc, pg.start + c0, P.P, d_items, d_isign, KK1, d_pvmx,
                              ctx->cfg.thrgen, ctx->d_hp, d_stat + 1);
             launches += (KK1 + 65534) / 65535;
         }
@@ -826,7 +826,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             for (int r = w.item_rec0[t]; r < w.item_rec0[t + 1]; ++r)
                 chunk_recs[r - w.item_rec0[i0]].ijl = t - i0;
         RT_CUDA(cudaMemcpyAsync(d_recs, chunk_recs.data(), chunk_recs.size() * sizeof(EmitRec), cudaMemcpyHostToDevice, st));
-        launch_emit(st, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), d_kra, d_krb, d_itrmo,
+        launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), d_kra, d_krb, d_itrmo,
                     ctx->cfg.throut, os);
         launches += 3;
         // the host copy of chunk_recs must outlive the async copy
@@ -839,6 +839,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     RT_CUDA(cudaMemcpyAsync(hstat, d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
     RT_CUDA(cudaEventRecord(ctx->ev[5], st));
     RT_CUDA(cudaStreamSynchronize(st));
+    if (split) split_check(ctx);
     for (int cc = 0; cc < 4; ++cc) {
         ctx->out_nz[cc] = tot[cc];
         ctx->out_nrec[cc] = w.nrec[cc];

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "rt_ff.cuh"
 #include "rt_kernels.h"
 
 namespace rt {
@@ -164,6 +165,21 @@ template void gemm_f64<EpiRowMajor>(cudaStream_t, const double*, long long, long
 template void gemm_f64<EpiRK>(cudaStream_t, const double*, long long, long long, const double*,
                               long long, long long, int, int, int, int, EpiRK);
 
+// Element formats of the intermediate arrays: FP64 (plain path) and
+// float-float (split path).  comb(a, b, sg) = a + sg*b.
+struct F64El {
+    typedef double T;
+    static __device__ __forceinline__ T comb(T a, T b, double sg) { return a + sg * b; }
+    static __device__ __forceinline__ double val(T a) { return a; }
+    static __device__ __forceinline__ T zero() { return 0.0; }
+};
+struct FFEl {
+    typedef float2 T;
+    static __device__ __forceinline__ T comb(T a, T b, double sg) { return ff_add(a, b, (float)sg); }
+    static __device__ __forceinline__ double val(T a) { return ff_to_double(a); }
+    static __device__ __forceinline__ T zero() { return make_float2(0.f, 0.f); }
+};
+
 // ---------------------------------------------------------------------------
 // K2: Kramers-unique selection + time-reversal completion + transpose
 // (MTIMHER + TROUT + SR2FLSH + GETHTI + UNIQUE: mtimher.F:141-164,
@@ -173,11 +189,13 @@ template void gemm_f64<EpiRK>(cudaStream_t, const double*, long long, long long,
 // RI = QA^H G_pq QA.  The screening test of TROUT (trout.F:194-207) is
 // applied to these values.
 // ---------------------------------------------------------------------------
-__global__ void k_tr_select(const double* __restrict__ ri, int m, int npc, int pq0, int P,
+template <class E>
+__global__ void k_tr_select(const typename E::T* __restrict__ ri, int m, int npc, int pq0, int P,
                             const int4* __restrict__ items, const float* __restrict__ item_sign,
                             int it0, int nitems, const double* __restrict__ pair_vmx,
-                            double thrgen, double* __restrict__ hp,
+                            double thrgen, typename E::T* __restrict__ hp,
                             unsigned long long* __restrict__ kept) {
+    typedef typename E::T T;
     const int it = it0 + blockIdx.y;
     const int pql = blockIdx.x * blockDim.x + threadIdx.x;
     int keep = 0;
@@ -187,15 +205,16 @@ __global__ void k_tr_select(const double* __restrict__ ri, int m, int npc, int p
         const long long plane = (long long)m * m * npc;
         const long long a = ((long long)w.x * m + w.y) * npc + pql;
         const long long b = ((long long)w.w * m + w.z) * npc + pql;
-        double re = ri[a] + s * ri[b];
-        double im = ri[plane + a] + s * ri[plane + b];
+        T re = E::comb(ri[a], ri[b], s);
+        T im = E::comb(ri[plane + a], ri[plane + b], s);
         const int pq = pq0 + pql;
-        double vv = pair_vmx[pq];
+        const double vv = pair_vmx[pq];
+        const double vr = E::val(re), vi = E::val(im);
         bool pass;
         if (vv < thrgen) pass = false;
-        else pass = !(hypot(re, im) < thrgen / vv);
-        if (!pass) { re = 0.0; im = 0.0; }
-        keep = pass && (re != 0.0 || im != 0.0);
+        else pass = !(hypot(vr, vi) < thrgen / vv);
+        if (!pass) { re = E::zero(); im = E::zero(); }
+        keep = pass && (vr != 0.0 || vi != 0.0);
         const long long o = (long long)it * P + pq;
         hp[o] = re;
         hp[(long long)nitems * P + o] = im;
@@ -248,7 +267,8 @@ __device__ __forceinline__ bool in_set(int cls, int x, int y, int i, int j) {
 
 // mode 0 counts the elements of each record, mode 1 writes them at the
 // offsets produced by k_scan_records; both evaluate the same expressions.
-__global__ void __launch_bounds__(256) k_emit(const double* __restrict__ rlr, int m, int nij,
+template <class E>
+__global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ rlr, int m, int nij,
                                               int K, const EmitRec* __restrict__ rec,
                                               const int* __restrict__ kra,
                                               const int* __restrict__ krb,
@@ -282,8 +302,8 @@ __global__ void __launch_bounds__(256) k_emit(const double* __restrict__ rlr, in
                 const double sg = ((itrmo[Ks] > 0) == (itrmo[Ls] > 0)) ? 1.0 : -1.0;
                 const long long a = ((long long)Ks * nij + ijl) * m + Ls;
                 const long long b = ((long long)Lb * nij + ijl) * m + Kb;
-                re = rlr[a] + sg * rlr[b];
-                im = rlr[plane + a] + sg * rlr[plane + b];
+                re = E::val(E::comb(rlr[a], rlr[b], sg));
+                im = E::val(E::comb(rlr[plane + a], rlr[plane + b], sg));
             }
             emit = hypot(re, im) > throut;
         }
@@ -353,15 +373,20 @@ void launch_scatter(cudaStream_t st, const double* rint, const int* l2, const in
                                                  g3, status);
 }
 
-void launch_tr_select(cudaStream_t st, const double* ri, int m, int npc, int pq0, int P,
+void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc, int pq0, int P,
                       const int4* items, const float* item_sign, int nitems,
                       const double* pair_vmx, double thrgen, double* hp,
                       unsigned long long* kept) {
     for (int y0 = 0; y0 < nitems; y0 += 65535) {
         int ny = nitems - y0 < 65535 ? nitems - y0 : 65535;
         dim3 grid((npc + 255) / 256, ny);
-        k_tr_select<<<grid, 256, 0, st>>>(ri, m, npc, pq0, P, items, item_sign, y0, nitems,
-                                          pair_vmx, thrgen, hp, kept);
+        if (ff)
+            k_tr_select<FFEl><<<grid, 256, 0, st>>>((const float2*)ri, m, npc, pq0, P, items,
+                                                   item_sign, y0, nitems, pair_vmx, thrgen,
+                                                   (float2*)hp, kept);
+        else
+            k_tr_select<F64El><<<grid, 256, 0, st>>>(ri, m, npc, pq0, P, items, item_sign, y0,
+                                                    nitems, pair_vmx, thrgen, hp, kept);
     }
 }
 
@@ -371,13 +396,19 @@ void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0
     k_expand<<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nc, m3);
 }
 
-void launch_emit(cudaStream_t st, const double* rlr, int m, int nij, int K, const EmitRec* rec,
-                 int nrec, const int* kra, const int* krb, const int* itrmo, double throut,
-                 const OutStreams& os) {
+void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, int K,
+                 const EmitRec* rec, int nrec, const int* kra, const int* krb, const int* itrmo,
+                 double throut, const OutStreams& os) {
     if (nrec <= 0) return;
-    k_emit<<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, 0, os);
-    k_scan_records<<<1, 1024, 0, st>>>(rec, nrec, os);
-    k_emit<<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, 1, os);
+    for (int mode = 0; mode < 2; ++mode) {
+        if (mode == 1) k_scan_records<<<1, 1024, 0, st>>>(rec, nrec, os);
+        if (ff)
+            k_emit<FFEl><<<nrec, 256, 0, st>>>((const float2*)rlr, m, nij, K, rec, kra, krb, itrmo,
+                                              throut, mode, os);
+        else
+            k_emit<F64El><<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, mode,
+                                               os);
+    }
 }
 
 }  // namespace rt

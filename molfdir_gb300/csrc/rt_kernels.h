@@ -90,14 +90,14 @@ void gemm_f64(cudaStream_t st, const double* A, long long lda, long long sA, con
 void launch_scatter(cudaStream_t st, const double* rint, const int* l2, const int* l1,
                     long long nint, const long long* rec_off, const int2* rec_meta, int nrec,
                     const ScatterTabs& tb, double* g3, unsigned int* status);
-void launch_tr_select(cudaStream_t st, const double* ri, int m, int npc, int pq0, int P,
+void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc, int pq0, int P,
                       const int4* items, const float* item_sign, int nitems,
                       const double* pair_vmx, double thrgen, double* hp,
                       unsigned long long* kept);
 void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
                    const int* pidx, int nc, double* m3);
-void launch_emit(cudaStream_t st, const double* rlr, int m, int nij, int K, const EmitRec* rec,
-                 int nrec, const int* kra, const int* krb, const int* itrmo, double throut,
-                 const OutStreams& os);
+void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, int K,
+                 const EmitRec* rec, int nrec, const int* kra, const int* krb, const int* itrmo,
+                 double throut, const OutStreams& os);
 
 }  // namespace rt

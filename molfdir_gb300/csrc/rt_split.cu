@@ -1,18 +1,804 @@
-// rt_split.cu -- split-precision GEMMs (under construction).
+// rt_split.cu -- split-precision GEMMs of the four quarter-transformations.
+//
+// C = A B with A (M x K) and B (K x N) given as FP64 or float-float values is
+// computed from s BF16 digit slices per operand (row scales for A, column
+// scales for B; see rt_ff.cuh) on the tcgen05 tensor cores:
+//
+//   acc0 = sum_k a_1 b_1                       exact in FP32 (K <= 1024)
+//   acc1 = sum_k a_1 b_2 + a_2 b_1             exact in FP32 (K <= 1024)
+//   acc2 = sum_k a_1 b_3 + a_2 b_2 + a_3 b_1   exact in FP32 (K <= 1024)
+//   acc3 = sum_k sum_{t+u>=5} a_t b_u          FP32 (relative weight 2^-21)
+//
+// (the tensor cores' FP32 accumulation of rounded sums behaves like about
+// 20 significant bits, so every product diagonal whose error would show
+// above 2^-40 is kept in an exactly summed accumulator)
+// (digit products with t+u > s+1 are dropped).  The epilogue recombines
+// acc0+acc1+acc2 without rounding into a float-float number, applies the
+// power-of-two scales and writes it; the next stage re-slices float-float
+// values directly.  FP64 arithmetic, which runs at about 1/70 of the FP32
+// rate on GB300, is used nowhere on this path except the final conversion
+// of the MDCINT elements.
+//
+// GEMM kernel: persistent, one CTA per SM, 128x128 output tiles, K in steps
+// of 32 (64-byte swizzled TMA tiles), two shared-memory stages holding all s
+// slices of A and B; warp 0 issues TMA loads, warp 1 issues tcgen05.mma into
+// four TMEM accumulators (all 512 columns), warps 2-5 drain TMEM and run the
+// epilogue.  Every wait is bounded (2 s); on a timeout the kernel sets an
+// error flag, stops all roles, waits for its own TMA copies and frees TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "rt_ff.cuh"
 #include "rt_split.h"
+#include "rt_umma.cuh"
 
 namespace rt {
 
-static void not_built() { throw Error(RT_ERR_USER, "split-BF16 path not available in this build"); }
-void split_prepare_constants(rt_ctx*) { not_built(); }
-double split_stageA_bytes_per_pair(rt_ctx*) { return 0.0; }
-double split_stageB_bytes_per_item(rt_ctx*) { return 0.0; }
-void split_alloc_work(rt_ctx*, int, int) { not_built(); }
-void split_prepare_g3(rt_ctx*, int*) { not_built(); }
-void split_gemm1(rt_ctx*, const G1Group&, int, int, const EpiHA&, int*) { not_built(); }
-void split_gemm24(rt_ctx*, const double*, int, long long, const EpiRowMajor&, int*) { not_built(); }
-void split_gemm3(rt_ctx*, int, const double*, int, int, const EpiRK&, int*) { not_built(); }
-void split_release(rt_ctx*) {}
-double split_flop_factor(rt_ctx*) { return 1.0; }
+constexpr int SBM = 128, SBN = 128, SBK = 32, NSTAGE = 2, MAX_SLICES = 7;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr unsigned long long WAIT_NS = 2000000000ull;
+
+enum : int { ERR_TIMEOUT_EMPTY = 1, ERR_TIMEOUT_FULL = 2, ERR_TIMEOUT_TMEM = 3 };
+
+// ---------------------------------------------------------------------------
+// slicing kernels
+// ---------------------------------------------------------------------------
+
+// Source rows of the A operand.
+struct RowsF64Batched {  // GEMM1: row = r*npc + pql -> G3 row (r, c0+pql)
+    const double* g3;    // group base
+    long long pg_size, c0;
+    int npc, nk;
+    __device__ const double* row(long long i) const {
+        long long r = i / npc, q = i - r * npc;
+        return g3 + (r * pg_size + c0 + q) * nk;
+    }
+};
+
+struct RowsFF {  // contiguous float-float rows of length K (stride ld)
+    const float2* base;
+    long long ld;
+    __device__ const float2* row(long long i) const { return base + i * ld; }
+};
+
+__global__ void k_slice_rows_f64(RowsF64Batched src, long long M, int K, int Kp, int s,
+                                 __nv_bfloat16* __restrict__ out, int* __restrict__ exps) {
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long i = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < M;
+         i += warps) {
+        const double* p = src.row(i);
+        int S = -2000;
+        for (int k = lane; k < K; k += 32) S = max(S, scale_exp_f64(p[k]));
+        for (int o = 16; o; o >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, o));
+        if (lane == 0) exps[i] = S;
+        for (int k = lane; k < Kp; k += 32) {
+            int d[MAX_SLICES + 1];
+            int64_t X = (k < K && S > -1000) ? fixed_f64(p[k], S, s) : 0;
+            digits7(X, s, d);
+            for (int t = 0; t < s; ++t) out[((long long)t * M + i) * Kp + k] = digit_bf16(d[t], t);
+        }
+    }
+}
+
+__global__ void k_slice_rows_ff(RowsFF src, long long M, int K, int Kp, int s,
+                                __nv_bfloat16* __restrict__ out, int* __restrict__ exps) {
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long i = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < M;
+         i += warps) {
+        const float2* p = src.row(i);
+        int S = -2000;
+        for (int k = lane; k < K; k += 32) S = max(S, scale_exp_f32(p[k].x));
+        for (int o = 16; o; o >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, o));
+        if (lane == 0) exps[i] = S;
+        for (int k = lane; k < Kp; k += 32) {
+            int d[MAX_SLICES + 1];
+            int64_t X = 0;
+            if (k < K && S > -1000) {
+                float2 v = p[k];
+                X = fixed_f32(v.x, S, s) + fixed_f32(v.y, S, s);
+            }
+            digits7(X, s, d);
+            for (int t = 0; t < s; ++t) out[((long long)t * M + i) * Kp + k] = digit_bf16(d[t], t);
+        }
+    }
+}
+
+// column scales of a K x N float-float matrix (row-major, ld)
+__global__ void k_col_exp_ff(const float2* __restrict__ src, long long ld, int K, long long N,
+                             int* __restrict__ exps) {
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N;
+         j += (long long)gridDim.x * blockDim.x) {
+        int S = -2000;
+        for (int k = 0; k < K; ++k) S = max(S, scale_exp_f32(src[(long long)k * ld + j].x));
+        exps[j] = S;
+    }
+}
+
+// B operand slices, transposed to [s][N][Kp] (K-major) through shared memory
+__global__ void __launch_bounds__(256) k_slice_cols_ff(const float2* __restrict__ src, long long ld,
+                                                       int K, long long N, int Kp, int s,
+                                                       const int* __restrict__ exps,
+                                                       __nv_bfloat16* __restrict__ out) {
+    __shared__ __nv_bfloat16 tile[MAX_SLICES][32][34];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+    const long long n0 = (long long)blockIdx.x * 32;
+    const int k0 = blockIdx.y * 32;
+    const long long n = n0 + tx;
+    const int S = n < N ? exps[n] : -2000;
+    for (int kk = ty; kk < 32; kk += 8) {
+        const int k = k0 + kk;
+        int d[MAX_SLICES + 1];
+        int64_t X = 0;
+        if (n < N && k < K && S > -1000) {
+            float2 v = src[(long long)k * ld + n];
+            X = fixed_f32(v.x, S, s) + fixed_f32(v.y, S, s);
+        }
+        digits7(X, s, d);
+        for (int t = 0; t < s; ++t) tile[t][tx][kk] = digit_bf16(d[t], t);
+    }
+    __syncthreads();
+    for (int t = 0; t < s; ++t)
+        for (int nn = ty; nn < 32; nn += 8) {
+            const long long col = n0 + nn;
+            if (col < N && k0 + tx < Kp) out[((long long)t * N + col) * Kp + k0 + tx] = tile[t][nn][tx];
+        }
+}
+
+// ---------------------------------------------------------------------------
+// host-side slicing of the constant operands (same digit arithmetic)
+// ---------------------------------------------------------------------------
+static inline uint16_t host_bf16(float f) {  // exact for digits (<= 8 significant bits)
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return (uint16_t)(u >> 16);
+}
+
+// A operand: rows of a row-major double matrix (M x K)
+static void host_slice_rows(const std::vector<double>& a, int M, int K, int Kp, int s,
+                            std::vector<uint16_t>& out, std::vector<int>& exps) {
+    out.assign((size_t)s * M * Kp, 0);
+    exps.assign(M, -2000);
+    for (int i = 0; i < M; ++i) {
+        int S = -2000;
+        for (int k = 0; k < K; ++k) S = std::max(S, scale_exp_f64(a[(size_t)i * K + k]));
+        exps[i] = S;
+        if (S < -1000) continue;
+        for (int k = 0; k < K; ++k) {
+            int d[MAX_SLICES + 1];
+            digits7(fixed_f64(a[(size_t)i * K + k], S, s), s, d);
+            for (int t = 0; t < s; ++t)
+                out[((size_t)t * M + i) * Kp + k] = host_bf16(std::ldexp((float)d[t], -7 * (t - 1)));
+        }
+    }
+}
+
+// B operand: columns of a row-major double matrix (K x N), output [s][N][Kp]
+static void host_slice_cols(const double* b, int K, int N, long long ld, int Kp, int s,
+                            std::vector<uint16_t>& out, std::vector<int>& exps) {
+    out.assign((size_t)s * N * Kp, 0);
+    exps.assign(N, -2000);
+    for (int j = 0; j < N; ++j) {
+        int S = -2000;
+        for (int k = 0; k < K; ++k) S = std::max(S, scale_exp_f64(b[(size_t)k * ld + j]));
+        exps[j] = S;
+        if (S < -1000) continue;
+        for (int k = 0; k < K; ++k) {
+            int d[MAX_SLICES + 1];
+            digits7(fixed_f64(b[(size_t)k * ld + j], S, s), s, d);
+            for (int t = 0; t < s; ++t)
+                out[((size_t)t * N + j) * Kp + k] = host_bf16(std::ldexp((float)d[t], -7 * (t - 1)));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the tcgen05 GEMM
+// ---------------------------------------------------------------------------
+struct SplitArgs {
+    long long M, N;
+    int Kp, s;
+    int tiles_m, tiles_n;
+    const int* row_exp;
+    const int* col_exp;
+    int* error;
+};
+
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+
+template <class Epi>
+__global__ void __launch_bounds__(192, 1)
+    k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                 SplitArgs g, Epi epi) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[NSTAGE], empty[NSTAGE], tfull, tempty;
+    __shared__ uint32_t tbase;
+    __shared__ volatile int abort_flag;
+    __shared__ int issued[NSTAGE];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int s = g.s;
+    const uint32_t slice_a = SBM * SBK * 2, slice_b = SBN * SBK * 2;
+    const uint32_t stage_bytes = (uint32_t)s * (slice_a + slice_b);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nkb = g.Kp / SBK;
+    const long long ntiles = (long long)g.tiles_m * g.tiles_n;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NSTAGE; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+            issued[i] = 0;
+        }
+        mbar_init(&tfull, 1);
+        mbar_init(&tempty, 4);
+        abort_flag = 0;
+        mbar_fence_init();
+    }
+    if (warp == 0) tmem_alloc(&tbase, TMEM_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tbase;
+
+    if (warp == 0) {
+        if (lane == 0) {  // ---- TMA producer ----
+            long long gk = 0;
+            for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x) {
+                const long long tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
+                for (int kb = 0; kb < nkb; ++kb, ++gk) {
+                    const int st = (int)(gk % NSTAGE);
+                    const uint32_t ph = (uint32_t)((gk / NSTAGE) & 1);
+                    if (!mbar_wait_bounded(&empty[st], ph ^ 1u, &abort_flag, WAIT_NS)) {
+                        if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_EMPTY);
+                        abort_flag = 1;
+                        break;
+                    }
+                    unsigned char* base = smem + (size_t)st * stage_bytes;
+                    mbar_expect_tx(&full[st], stage_bytes);
+                    for (int t = 0; t < s; ++t) {
+                        tma_load_2d(base + t * slice_a, &mapA, &full[st], kb * SBK,
+                                    (int)(t * g.M + tm * SBM));
+                        tma_load_2d(base + (size_t)s * slice_a + t * slice_b, &mapB, &full[st],
+                                    kb * SBK, (int)(t * g.N + tn * SBN));
+                    }
+                    issued[st] = 1 + (int)ph;  // phase parity of the outstanding load
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // ---- MMA issuer ----
+            const uint32_t idesc = umma_idesc_bf16(SBM, SBN);
+            long long gk = 0;
+            int it = 0;
+            for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x, ++it) {
+                if (it > 0 && !mbar_wait_bounded(&tempty, (uint32_t)((it - 1) & 1), &abort_flag, WAIT_NS)) {
+                    if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_TMEM);
+                    abort_flag = 1;
+                    break;
+                }
+                tc_fence_after();
+                bool started[4] = {false, false, false, false};
+                for (int kb = 0; kb < nkb; ++kb, ++gk) {
+                    const int st = (int)(gk % NSTAGE);
+                    const uint32_t ph = (uint32_t)((gk / NSTAGE) & 1);
+                    if (!mbar_wait_bounded(&full[st], ph, &abort_flag, WAIT_NS)) {
+                        if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_FULL);
+                        abort_flag = 1;
+                        break;
+                    }
+                    issued[st] = 0;
+                    tc_fence_after();
+                    unsigned char* base = smem + (size_t)st * stage_bytes;
+                    for (int t = 0; t < s; ++t)
+                        for (int u = 0; u + t < s; ++u) {
+                            const int acc = t + u < 3 ? t + u : 3;
+                            const uint32_t dt = tmem + (uint32_t)(acc * SBN);
+                            const uint64_t da = umma_sdesc(base + t * slice_a, 512, UMMA_SWIZZLE_64B);
+                            const uint64_t db = umma_sdesc(base + (size_t)s * slice_a + u * slice_b, 512,
+                                                           UMMA_SWIZZLE_64B);
+#pragma unroll
+                            for (int kk = 0; kk < SBK / 16; ++kk) {
+                                umma_bf16(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc,
+                                          started[acc] ? 1u : 0u);
+                                started[acc] = true;
+                            }
+                        }
+                    umma_commit(&empty[st]);
+                }
+                if (abort_flag) break;
+                umma_commit(&tfull);
+            }
+        }
+    } else {  // ---- epilogue: warps 2..5, one TMEM lane per thread ----
+        const int lg = warp & 3;
+        const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
+        int it = 0;
+        for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x, ++it) {
+            if (!mbar_wait_bounded(&tfull, (uint32_t)(it & 1), &abort_flag, WAIT_NS)) {
+                if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_TMEM);
+                abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const long long tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
+            const long long row = tm * SBM + lg * 32 + lane;
+            const int erow = row < g.M ? g.row_exp[row] : -2000;
+            for (int c0 = 0; c0 < SBN; c0 += 32) {
+                uint32_t r0[32], r1[32], r2[32], r3[32];
+                tmem_ld32(tmem + lane_base + (uint32_t)c0, r0);
+                if (s >= 2) tmem_ld32(tmem + lane_base + (uint32_t)(SBN + c0), r1);
+                if (s >= 3) tmem_ld32(tmem + lane_base + (uint32_t)(2 * SBN + c0), r2);
+                if (s >= 4) tmem_ld32(tmem + lane_base + (uint32_t)(3 * SBN + c0), r3);
+                tmem_ld_wait();
+                if (c0 + 32 == SBN) {  // accumulators drained: release TMEM
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&tempty);
+                }
+                if (row >= g.M) continue;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const long long col = tn * SBN + c0 + j;
+                    if (col >= g.N) continue;
+                    const int ecol = g.col_exp[col];
+                    const float a0 = __uint_as_float(r0[j]);
+                    const float a1 = s >= 2 ? __uint_as_float(r1[j]) : 0.f;
+                    const float a2 = s >= 3 ? __uint_as_float(r2[j]) : 0.f;
+                    const float a3 = s >= 4 ? __uint_as_float(r3[j]) : 0.f;
+                    // exact sum of the exact diagonals, then the rounded tail
+                    float s1, e1, s2, e2, s3, e3, hi, lo;
+                    two_sum(a0, a1, s1, e1);
+                    two_sum(s1, a2, s2, e2);
+                    two_sum(s2, a3, s3, e3);
+                    fast_two_sum(s3, (e1 + e2) + e3, hi, lo);
+                    if (ecol < -1000 || erow < -1000) { hi = 0.f; lo = 0.f; }  // zero row / column
+                    else {
+                        const int k = erow + ecol - 28;  // pre-scaled digits carry 2^14 per operand
+                        const int k1 = k / 2, k2 = k - k1;
+                        const float f1 = pow2f(max(-126, min(127, k1))),
+                                    f2 = pow2f(max(-126, min(127, k2)));
+                        hi = hi * f1 * f2;
+                        lo = lo * f1 * f2;
+                    }
+                    epi(row, col, hi, lo);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && abort_flag) {
+        // let the outstanding tensor copies of this CTA land before exit
+        volatile int never = 0;
+        for (int st = 0; st < NSTAGE; ++st)
+            if (issued[st]) mbar_wait_bounded(&full[st], (uint32_t)(issued[st] - 1), &never, WAIT_NS);
+    }
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
+}
+
+// ---------------------------------------------------------------------------
+// epilogue functors (float-float outputs)
+// ---------------------------------------------------------------------------
+struct EpiFF_HA {  // GEMM1: row = r*npc + pql, col = plane*m + b
+    float2* ha;
+    int r0, m, npc;
+    long long plane;
+    __device__ __forceinline__ void operator()(long long row, long long col, float hi, float lo) const {
+        long long r = row / npc, q = row - r * npc;
+        int pl = col >= m;
+        long long b = col - pl * m;
+        ha[pl * plane + ((r0 + r) * m + b) * npc + q] = make_float2(hi, lo);
+    }
+};
+
+struct EpiFF_RowMajor {
+    float2* c;
+    long long ldc;
+    __device__ __forceinline__ void operator()(long long row, long long col, float hi, float lo) const {
+        c[row * ldc + col] = make_float2(hi, lo);
+    }
+};
+
+struct EpiFF_RK {
+    float2* rk;
+    int m;
+    long long rowoff, plane;
+    __device__ __forceinline__ void operator()(long long row, long long col, float hi, float lo) const {
+        int pl = col >= m;
+        long long k = col - pl * m;
+        rk[pl * plane + (rowoff + row) * m + k] = make_float2(hi, lo);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// state and host orchestration
+// ---------------------------------------------------------------------------
+struct ConstSlices {
+    __nv_bfloat16* d = nullptr;
+    int* exps = nullptr;
+    int rows = 0, K = 0, Kp = 0;
+};
+
+struct SplitState {
+    int s = 6;
+    PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    int num_sms = 152;
+    // constant operands
+    ConstSlices qah;                 // A of GEMM2/4: rows 2m, K = 2n
+    std::vector<ConstSlices> qap;    // B of GEMM1 per AO block: N = 2m, K = block size
+    ConstSlices qar[2];              // B of GEMM3 per component: N = 2m, K = 2nc
+    // work buffers
+    __nv_bfloat16* a_sl = nullptr;
+    int* a_exp = nullptr;
+    size_t a_cap = 0, a_exp_cap = 0;
+    __nv_bfloat16* b_sl = nullptr;
+    int* b_exp = nullptr;
+    size_t b_cap = 0, b_exp_cap = 0;
+    int* d_err = nullptr;
+    std::vector<void*> allocs;
+};
+
+static int kpad(int K) { return (K + SBK - 1) / SBK * SBK; }
+
+static void* salloc(SplitState* S, size_t bytes) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(RT_ERR_DIM, std::string("split-path allocation failed: ") + cudaGetErrorString(e));
+    }
+    S->allocs.push_back(p);
+    return p;
+}
+
+static void sfree(SplitState* S, void* p) {
+    if (!p) return;
+    auto it = std::find(S->allocs.begin(), S->allocs.end(), p);
+    if (it != S->allocs.end()) S->allocs.erase(it);
+    cudaFree(p);
+}
+
+static SplitState* state(rt_ctx* c) {
+    if (!c->split) {
+        SplitState* S = new SplitState();
+        S->s = c->cfg.slices;
+        if (S->s > MAX_SLICES) throw Error(RT_ERR_DIM, "at most 7 slices are supported");
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        RT_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                 cudaEnableDefault, &q));
+        if (!fn || q != cudaDriverEntryPointSuccess)
+            throw Error(RT_ERR_PROGRAM, "cuTensorMapEncodeTiled unavailable");
+        S->encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        cudaDeviceProp prop;
+        RT_CUDA(cudaGetDeviceProperties(&prop, c->device));
+        S->num_sms = prop.multiProcessorCount;
+        S->d_err = (int*)salloc(S, sizeof(int));
+        RT_CUDA(cudaMemset(S->d_err, 0, sizeof(int)));
+        RT_CUDA(cudaFuncSetAttribute(k_split_gemm<EpiFF_HA>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448 - 1024));
+        RT_CUDA(cudaFuncSetAttribute(k_split_gemm<EpiFF_RowMajor>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448 - 1024));
+        RT_CUDA(cudaFuncSetAttribute(k_split_gemm<EpiFF_RK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448 - 1024));
+        c->split = S;
+    }
+    return c->split;
+}
+
+static void upload_const(SplitState* S, ConstSlices& cs, const std::vector<uint16_t>& sl,
+                         const std::vector<int>& ex, int rows, int K) {
+    sfree(S, cs.d);
+    sfree(S, cs.exps);
+    cs.d = (__nv_bfloat16*)salloc(S, sl.size() * 2);
+    cs.exps = (int*)salloc(S, ex.size() * sizeof(int));
+    RT_CUDA(cudaMemcpy(cs.d, sl.data(), sl.size() * 2, cudaMemcpyHostToDevice));
+    RT_CUDA(cudaMemcpy(cs.exps, ex.data(), ex.size() * sizeof(int), cudaMemcpyHostToDevice));
+    cs.rows = rows;
+    cs.K = K;
+    cs.Kp = kpad(K);
+}
+
+void split_prepare_constants(rt_ctx* c) {
+    SplitState* S = state(c);
+    const Plan& P = c->plan;
+    const int n = P.n, m = P.m, s = S->s;
+    if (2 * n > 1024)
+        throw Error(RT_ERR_DIM, "split path: 2*NSC > 1024 exceeds the exact FP32 accumulation range");
+    // planar QA in sorted AO order
+    std::vector<double> qr((size_t)n * m), qi((size_t)n * m);
+    for (int p = 0; p < n; ++p)
+        for (int i = 0; i < m; ++i) {
+            qr[(size_t)P.ao_sorted[p] * m + i] = c->qa[2 * ((size_t)p + (size_t)i * n)];
+            qi[(size_t)P.ao_sorted[p] * m + i] = c->qa[2 * ((size_t)p + (size_t)i * n) + 1];
+        }
+    std::vector<uint16_t> sl;
+    std::vector<int> ex;
+    // qah: [(plane',a)][(plane,r)] rows 2m, K 2n
+    {
+        std::vector<double> a((size_t)2 * m * 2 * n);
+        for (int i = 0; i < m; ++i)
+            for (int r = 0; r < n; ++r) {
+                double re = qr[(size_t)r * m + i], im = qi[(size_t)r * m + i];
+                a[(size_t)i * 2 * n + r] = re;
+                a[(size_t)i * 2 * n + n + r] = im;
+                a[(size_t)(m + i) * 2 * n + r] = -im;
+                a[(size_t)(m + i) * 2 * n + n + r] = re;
+            }
+        host_slice_rows(a, 2 * m, 2 * n, kpad(2 * n), s, sl, ex);
+        upload_const(S, S->qah, sl, ex, 2 * m, 2 * n);
+    }
+    // qap per AO block: B = rows s in block, cols (plane, b)
+    S->qap.resize(P.nblk);
+    for (int b = 0; b < P.nblk; ++b) {
+        const int nk = P.blk_size[b], st = P.blk_start[b];
+        std::vector<double> bm((size_t)nk * 2 * m);
+        for (int k = 0; k < nk; ++k)
+            for (int j = 0; j < m; ++j) {
+                bm[(size_t)k * 2 * m + j] = qr[(size_t)(st + k) * m + j];
+                bm[(size_t)k * 2 * m + m + j] = qi[(size_t)(st + k) * m + j];
+            }
+        host_slice_cols(bm.data(), nk, 2 * m, 2 * m, kpad(nk), s, sl, ex);
+        upload_const(S, S->qap[b], sl, ex, 2 * m, nk);
+    }
+    // qar per component: [(plane,q)][(plane',k)] = [[QAr, QAi], [-QAi, QAr]]
+    for (int comp = 0; comp < 2; ++comp) {
+        const int nc = P.ncomp[comp], off = P.comp_off[comp];
+        if (nc == 0) continue;
+        std::vector<double> bm((size_t)2 * nc * 2 * m);
+        for (int q = 0; q < nc; ++q)
+            for (int k = 0; k < m; ++k) {
+                double re = qr[(size_t)(off + q) * m + k], im = qi[(size_t)(off + q) * m + k];
+                bm[(size_t)q * 2 * m + k] = re;
+                bm[(size_t)q * 2 * m + m + k] = im;
+                bm[(size_t)(nc + q) * 2 * m + k] = -im;
+                bm[(size_t)(nc + q) * 2 * m + m + k] = re;
+            }
+        host_slice_cols(bm.data(), 2 * nc, 2 * m, 2 * m, kpad(2 * nc), s, sl, ex);
+        upload_const(S, S->qar[comp], sl, ex, 2 * m, 2 * nc);
+    }
+}
+
+double split_stageA_bytes_per_pair(rt_ctx* c) {
+    const Plan& P = c->plan;
+    const int s = c->cfg.slices;
+    int maxnr = 1, maxk = 1;
+    for (auto& g : P.g1) {
+        maxnr = std::max(maxnr, P.blk_size[g.rblk]);
+        maxk = std::max(maxk, kpad(P.blk_size[g.kblk]));
+    }
+    double a = 2.0 * s * maxnr * maxk + 4.0 * maxnr;          // GEMM1 A slices + exps
+    double b = 2.0 * s * P.m * kpad(2 * P.n) + 4.0 * P.m;     // GEMM2 B slices + exps
+    return std::max(a, b);
+}
+
+double split_stageB_bytes_per_item(rt_ctx* c) {
+    const Plan& P = c->plan;
+    const int s = c->cfg.slices;
+    int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+    double a = 2.0 * s * ncmax * kpad(2 * ncmax) + 4.0 * ncmax;  // GEMM3 A slices
+    double b = 2.0 * s * P.m * kpad(2 * P.n) + 4.0 * P.m;        // GEMM4 B slices
+    return std::max(a, b);
+}
+
+void split_alloc_work(rt_ctx* c, int pair_chunk, int item_chunk) {
+    SplitState* S = state(c);
+    size_t bytes = (size_t)std::max(split_stageA_bytes_per_pair(c) * pair_chunk,
+                                    split_stageB_bytes_per_item(c) * item_chunk);
+    const Plan& P = c->plan;
+    int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+    int maxnr = 1;
+    for (auto& g : P.g1) maxnr = std::max(maxnr, P.blk_size[g.rblk]);
+    size_t rows = std::max({(size_t)maxnr * pair_chunk, (size_t)P.m * pair_chunk,
+                            (size_t)ncmax * item_chunk, (size_t)P.m * item_chunk});
+    sfree(S, S->a_sl);
+    sfree(S, S->a_exp);
+    S->a_sl = (__nv_bfloat16*)salloc(S, bytes);  // A and B slices share the arena in turn
+    S->a_cap = bytes;
+    S->a_exp = (int*)salloc(S, rows * sizeof(int));
+    S->a_exp_cap = rows;
+    sfree(S, S->b_exp);
+    S->b_exp = (int*)salloc(S, rows * sizeof(int));
+    S->b_exp_cap = rows;
+}
+
+void split_prepare_g3(rt_ctx* c, int*) { state(c); }
+
+double split_flop_factor(rt_ctx* c) {
+    const int s = c->cfg.slices;
+    return s * (s + 1) / 2.0;
+}
+
+static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int Kp) {
+    CUtensorMap m;
+    cuuint64_t gd[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+    cuuint64_t gs[1] = {(cuuint64_t)Kp * 2};
+    cuuint32_t box[2] = {(cuuint32_t)SBK, (cuuint32_t)SBM};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = S->encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), gd, gs,
+                           box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(RT_ERR_PROGRAM, "cuTensorMapEncodeTiled failed");
+    return m;
+}
+
+template <class Epi>
+static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M, const void* b_sl,
+                     const int* b_exp, long long N, int Kp, Epi epi, int* launches) {
+    SplitState* S = state(c);
+    if (M <= 0 || N <= 0) return;
+    const int s = S->s;
+    CUtensorMap ma = make_map(S, a_sl, (long long)s * M, Kp);
+    CUtensorMap mb = make_map(S, b_sl, (long long)s * N, Kp);
+    SplitArgs g;
+    g.M = M;
+    g.N = N;
+    g.Kp = Kp;
+    g.s = s;
+    g.tiles_m = (int)((M + SBM - 1) / SBM);
+    g.tiles_n = (int)((N + SBN - 1) / SBN);
+    g.row_exp = a_exp;
+    g.col_exp = b_exp;
+    g.error = S->d_err;
+    const long long ntiles = (long long)g.tiles_m * g.tiles_n;
+    const int grid = (int)std::min<long long>(ntiles, S->num_sms);
+    const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
+    k_split_gemm<Epi><<<grid, 192, smem, c->stream>>>(ma, mb, g, epi);
+    ++*launches;
+    RT_CUDA(cudaGetLastError());
+}
+
+static void check_error(rt_ctx* c) {
+    SplitState* S = state(c);
+    int e = 0;
+    RT_CUDA(cudaMemcpyAsync(&e, S->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    RT_CUDA(cudaStreamSynchronize(c->stream));
+    if (e) {
+        RT_CUDA(cudaMemset(S->d_err, 0, sizeof(int)));
+        throw Error(RT_ERR_PROGRAM, "split GEMM gave up waiting (status " + std::to_string(e) + ")");
+    }
+}
+
+void split_check(rt_ctx* c) { check_error(c); }
+
+void split_gemm1(rt_ctx* c, const G1Group& gg, int c0, int npc, const EpiHA& e, int* launches) {
+    SplitState* S = state(c);
+    const Plan& P = c->plan;
+    const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk], Kp = kpad(nk);
+    const long long M = (long long)nr * npc;
+    RowsF64Batched src{c->d_g3 + gg.base, (long long)P.pgroups[gg.pg].size, c0, npc, nk};
+    k_slice_rows_f64<<<(unsigned)std::min<long long>((M + 7) / 8, 152LL * 32), 256, 0, c->stream>>>(
+        src, M, nk, Kp, S->s, S->a_sl, S->a_exp);
+    ++*launches;
+    const ConstSlices& B = S->qap[gg.kblk];
+    EpiFF_HA epi{(float2*)e.ha, e.r0, e.m, e.npc, e.plane};
+    run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * P.m, Kp, epi, launches);
+}
+
+void split_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRowMajor& e,
+                  int* launches) {
+    SplitState* S = state(c);
+    const int Kp = kpad(K);
+    const float2* src = (const float2*)Bsrc;
+    k_col_exp_ff<<<(unsigned)std::min<long long>((N + 255) / 256, 152LL * 16), 256, 0, c->stream>>>(
+        src, N, K, N, S->b_exp);
+    dim3 grid((unsigned)((N + 31) / 32), (unsigned)(Kp / 32));
+    k_slice_cols_ff<<<grid, 256, 0, c->stream>>>(src, N, K, N, Kp, S->s, S->b_exp, S->a_sl);
+    *launches += 2;
+    EpiFF_RowMajor epi{(float2*)e.c, e.ldc};
+    run_gemm(c, S->qah.d, S->qah.exps, S->qah.rows, S->a_sl, S->b_exp, N, Kp, epi, launches);
+}
+
+void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& e,
+                 int* launches) {
+    SplitState* S = state(c);
+    const int K = 2 * nc, Kp = kpad(K);
+    const long long M = (long long)nc * nij;
+    RowsFF src{(const float2*)m3, (long long)K};
+    k_slice_rows_ff<<<(unsigned)std::min<long long>((M + 7) / 8, 152LL * 32), 256, 0, c->stream>>>(
+        src, M, K, Kp, S->s, S->a_sl, S->a_exp);
+    ++*launches;
+    const ConstSlices& B = S->qar[comp];
+    EpiFF_RK epi{(float2*)e.rk, e.m, e.rowoff, e.plane};
+    run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * c->plan.m, Kp, epi, launches);
+}
+
+void split_release(rt_ctx* c) {
+    if (!c->split) return;
+    for (void* p : c->split->allocs) cudaFree(p);
+    delete c->split;
+    c->split = nullptr;
+}
 
 }  // namespace rt
+
+extern "C" int rt_split_dgemm(int M, int N, int K, const double* A, const double* B, double* C,
+                              int slices, int mode) {
+    using namespace rt;
+    if (M < 1 || N < 1 || K < 1 || K > 1024 || !A || !B || !C || slices < 2 ||
+        slices > MAX_SLICES || mode < 0 || mode > 2)
+        return RT_ERR_USER;
+    rt_ctx ctx;
+    int rc = RT_OK;
+    std::vector<void*> tmp;
+    auto dal = [&](size_t bytes) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) throw Error(RT_ERR_DIM, "allocation failed");
+        tmp.push_back(p);
+        return p;
+    };
+    try {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(RT_ERR_PROGRAM, "no CUDA device");
+        RT_CUDA(cudaGetDevice(&ctx.device));
+        RT_CUDA(cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking));
+        ctx.cfg.slices = slices;
+        SplitState* S = state(&ctx);
+        const int Kp = kpad(K);
+        int launches = 0;
+        __nv_bfloat16 *da, *db;
+        int *ea, *eb;
+        if (mode == 0) {
+            std::vector<uint16_t> sl;
+            std::vector<int> ex;
+            std::vector<double> av(A, A + (size_t)M * K);
+            host_slice_rows(av, M, K, Kp, slices, sl, ex);
+            da = (__nv_bfloat16*)dal(sl.size() * 2);
+            ea = (int*)dal(ex.size() * 4);
+            RT_CUDA(cudaMemcpy(da, sl.data(), sl.size() * 2, cudaMemcpyHostToDevice));
+            RT_CUDA(cudaMemcpy(ea, ex.data(), ex.size() * 4, cudaMemcpyHostToDevice));
+            host_slice_cols(B, K, N, N, Kp, slices, sl, ex);
+            db = (__nv_bfloat16*)dal(sl.size() * 2);
+            eb = (int*)dal(ex.size() * 4);
+            RT_CUDA(cudaMemcpy(db, sl.data(), sl.size() * 2, cudaMemcpyHostToDevice));
+            RT_CUDA(cudaMemcpy(eb, ex.data(), ex.size() * 4, cudaMemcpyHostToDevice));
+        } else {
+            da = (__nv_bfloat16*)dal((size_t)2 * slices * M * Kp);
+            ea = (int*)dal((size_t)4 * M);
+            db = (__nv_bfloat16*)dal((size_t)2 * slices * N * Kp);
+            eb = (int*)dal((size_t)4 * N);
+            std::vector<float2> bf((size_t)K * N);
+            for (size_t i = 0; i < bf.size(); ++i) {
+                float h = (float)B[i];
+                bf[i] = make_float2(h, (float)(B[i] - (double)h));
+            }
+            float2* dbf = (float2*)dal(bf.size() * 8);
+            RT_CUDA(cudaMemcpy(dbf, bf.data(), bf.size() * 8, cudaMemcpyHostToDevice));
+            k_col_exp_ff<<<(N + 255) / 256, 256, 0, ctx.stream>>>(dbf, N, K, N, eb);
+            k_slice_cols_ff<<<dim3((N + 31) / 32, Kp / 32), 256, 0, ctx.stream>>>(dbf, N, K, N, Kp, slices, eb, db);
+            if (mode == 1) {
+                std::vector<float2> af((size_t)M * K);
+                for (size_t i = 0; i < af.size(); ++i) {
+                    float h = (float)A[i];
+                    af[i] = make_float2(h, (float)(A[i] - (double)h));
+                }
+                float2* daf = (float2*)dal(af.size() * 8);
+                RT_CUDA(cudaMemcpy(daf, af.data(), af.size() * 8, cudaMemcpyHostToDevice));
+                k_slice_rows_ff<<<(M + 7) / 8, 256, 0, ctx.stream>>>(RowsFF{daf, K}, M, K, Kp, slices, da, ea);
+            } else {
+                double* dad = (double*)dal((size_t)M * K * 8);
+                RT_CUDA(cudaMemcpy(dad, A, (size_t)M * K * 8, cudaMemcpyHostToDevice));
+                RowsF64Batched src{dad, (long long)M, 0, M, K};
+                k_slice_rows_f64<<<(M + 7) / 8, 256, 0, ctx.stream>>>(src, M, K, Kp, slices, da, ea);
+            }
+            RT_CUDA(cudaGetLastError());
+        }
+        float2* dc = (float2*)dal((size_t)M * N * 8);
+        RT_CUDA(cudaMemsetAsync(dc, 0, (size_t)M * N * 8, ctx.stream));
+        run_gemm(&ctx, da, ea, M, db, eb, N, Kp, EpiFF_RowMajor{dc, N}, &launches);
+        check_error(&ctx);
+        std::vector<float2> hc((size_t)M * N);
+        RT_CUDA(cudaMemcpy(hc.data(), dc, hc.size() * 8, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < hc.size(); ++i) C[i] = (double)hc[i].x + (double)hc[i].y;
+    } catch (const Error& e) {
+        rc = e.code;
+    }
+    for (void* p : tmp) cudaFree(p);
+    split_release(&ctx);
+    if (ctx.stream) cudaStreamDestroy(ctx.stream);
+    return rc;
+}

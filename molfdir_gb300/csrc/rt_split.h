@@ -20,5 +20,7 @@ void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const E
 void split_release(rt_ctx* c);
 // executed FLOPs per algorithmic FLOP of a split GEMM (slice products)
 double split_flop_factor(rt_ctx* c);
+// raise if a split GEMM gave up waiting (bounded-wait timeout)
+void split_check(rt_ctx* c);
 
 }  // namespace rt

@@ -71,7 +71,7 @@ class RtPlanInfo(C.Structure):
 EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_add_ao_records_bulk", "rt_read_srt_files", "rt_clear_ao_records",
            "rt_transform", "rt_result_sizes", "rt_copy_result", "rt_write_mdcint",
-           "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check"]
+           "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm"]
 
 _lib = None
 
@@ -108,6 +108,8 @@ def load(build: bool = True):
     lib.rt_destroy.restype = None
     lib.rt_kramers_check.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_double), C.c_int,
                                      P(C.c_int), P(C.c_double)]
+    lib.rt_split_dgemm.argtypes = [C.c_int, C.c_int, C.c_int, P(C.c_double), P(C.c_double),
+                                   P(C.c_double), C.c_int, C.c_int]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy"):
@@ -290,3 +292,19 @@ class Rotran:
         s = RtStats()
         self._check(self.lib.rt_get_stats(self.h, C.byref(s)))
         return s
+
+
+def split_dgemm(a: np.ndarray, b: np.ndarray, slices: int = 7, mode: int = 0) -> np.ndarray:
+    """C = A B through the split-precision tensor-core engine (``rt_split_dgemm``)."""
+    lib = load()
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    m, k = a.shape
+    k2, n = b.shape
+    assert k == k2
+    c = np.empty((m, n), np.float64)
+    rc = lib.rt_split_dgemm(m, n, k, _p(a, C.c_double), _p(b, C.c_double), _p(c, C.c_double),
+                            slices, mode)
+    if rc:
+        raise RotranError(rc, "rt_split_dgemm failed")
+    return c

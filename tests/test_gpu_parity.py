@@ -73,6 +73,9 @@ def test_fp64_thresholds(thrgen, throut):
     # screens the complete half-transformed integrals), so only the
     # default-threshold runs are compared element for element
     tol = TOL_FP64 if thrgen <= 1e-16 else 1e-4
+    # with a large THROUT the reference drops canonical or pp-interchanged
+    # halves below THROUT before summing them (outpp1.F:76, outpp2.F:156)
+    tol = max(tol, throut)
     assert compare_streams(got, ref, tol, presence_tol=max(tol, 2 * throut)) <= tol
 
 
