@@ -34,6 +34,9 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(name="precision_study_n400_k120", n_l=160, n_s=240, nkr=120, seed=0)
 SMALL = dict(name="c1_n64_k32", n_l=24, n_s=40, nkr=32, seed=0)
+# a profiling case: the same kernels at a size whose device footprint stays
+# near 1 GB (inputs still larger than L2)
+PROFILE = dict(name="profile_n128_k32", n_l=48, n_s=80, nkr=32, seed=0)
 
 
 def peaks():
@@ -139,12 +142,14 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="auto", choices=["auto", "split", "fp64"])
-    ap.add_argument("--workload", default="precision", choices=["precision", "c1"])
+    ap.add_argument("--precision", default="split", choices=["split", "fp64"])
+    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--workload", default="precision", choices=["precision", "c1", "profile"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
-    work = WORKLOAD if args.workload == "precision" else SMALL
+    work = {"precision": WORKLOAD, "c1": SMALL, "profile": PROFILE}[args.workload]
     rank, world, local = dist_env()
     hbm_peak, bf16_peak, peak_kind = peaks()
 
@@ -173,71 +178,77 @@ def main():
         dist.init_process_group("nccl")
     from molfdir_gb300 import rotran, synth
 
-    prec_name = args.precision
-    if prec_name == "auto":
-        prec_name = "split" if rotran_split_available() else "fp64"
+    prec_name = "fp64" if args.precision == "fp64" else "split"
     prec = rotran.RT_PREC_SPLIT_BF16 if prec_name == "split" else rotran.RT_PREC_FP64
+    barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
 
     prob = synth.make_spinor_problem(work["n_l"], work["n_s"], work["nkr"], seed=work["seed"])
     cls, its, nts, dv, dl2, dl1 = synth.device_records(prob, 3, device="cuda")
     torch.cuda.synchronize()
     nint = int(nts.sum())
 
-    def make_ctx():
-        rt = rotran.Rotran.for_problem(prob, precision=prec)
+    def make_ctx(p, slices):
+        rt = rotran.Rotran.for_problem(prob, precision=p, slices=slices)
         rt.set_problem_coefficients(prob)
         return rt
 
-    # ---- value: records resident in HBM ----
-    rt = make_ctx()
-    rt.add_records_bulk_device(cls, nts, its, dv, dl2, dl1)
-    for _ in range(args.warmup):
-        rt.transform()
-    barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
-    barrier()
-    torch.cuda.synchronize()
-    gemm_ms, step_ms = [], []
-    with ClockSampler(local) as clk:
+    def run_leg(p, slices, warmup, steps, clocks=False):
+        rt = make_ctx(p, slices)
+        rt.add_records_bulk_device(cls, nts, its, dv, dl2, dl1)
+        for _ in range(warmup):
+            rt.transform()
+        barrier()
+        torch.cuda.synchronize()
+        gemm_ms, dev_ms = [], []
+        sampler = ClockSampler(local) if clocks else None
+        if sampler:
+            sampler.__enter__()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             rt.transform()
             st = rt.stats()
             gemm_ms.append(st.ms_gemm)
-            step_ms.append(st.ms_total)
+            dev_ms.append(st.ms_total)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-    barrier()
-    wall = (t1 - t0) / args.steps
-    dev_ms = statistics.mean(step_ms)
-    sec = barrier_max(max(wall, dev_ms / 1e3), world)
+        if sampler:
+            sampler.__exit__(None, None, None)
+        barrier()
+        sec = barrier_max(max((t1 - t0) / steps, statistics.mean(dev_ms) / 1e3), world)
+        res = rt.result()
+        out = dict(sec=sec, stats=st, gemm_ms=statistics.mean(gemm_ms),
+                   clocks=sampler.summary() if sampler else None, result=res)
+        rt.close()
+        return out
+
+    # ---- value: records resident in HBM ----
+    main = run_leg(prec, args.slices, args.warmup, args.steps, clocks=True)
+    st = main["stats"]
     flops = st.flops_algorithmic
-    value = flops * world / sec / 1e12
-    nrec, nz = rt.result_sizes()
-    launches = st.gpu_launches * args.steps
-    roof_achieved = st.flops_gemm_executed / (statistics.mean(gemm_ms) / 1e3) / 1e12
-    rt_stats = st.as_dict()
-    rt.close()
+    value = flops * world / main["sec"] / 1e12
+    hdr, idx, val = main["result"]
+    nrec, nz = hdr.shape[0], idx.shape[0]
 
     # ---- e2e through the public API with host buffers ----
     e2e = None
     if not args.no_e2e:
         hv, h2, h1 = (x.cpu().pin_memory() for x in (dv, dl2, dl1))
-        rt = make_ctx()
-        hdr = np.empty((nrec, 3), np.int32)
-        idx = torch.empty((nz, 2), dtype=torch.int32).pin_memory()
-        val = torch.empty((nz, 2), dtype=torch.float64).pin_memory()
-        idx_np, val_np = idx.numpy(), val.numpy().view(np.complex128).reshape(-1)
+        rt = make_ctx(prec, args.slices)
+        ehdr = np.empty((nrec, 3), np.int32)
+        eidx = torch.empty((nz, 2), dtype=torch.int32).pin_memory()
+        evalt = torch.empty((nz, 2), dtype=torch.float64).pin_memory()
+        eidx_np, eval_np = eidx.numpy(), evalt.numpy().view(np.complex128).reshape(-1)
 
         def e2e_step():
             rt.clear_records()
             rt.add_records_bulk_ptr(cls, nts, its, hv.data_ptr(), h2.data_ptr(), h1.data_ptr())
             rt.transform()
-            rt.result(hdr, idx_np, val_np)
+            rt.result(ehdr, eidx_np, eval_np)
 
         e2e_step()
         barrier()
+        ne = max(1, min(args.steps, 3))
         t0 = time.perf_counter()
-        ne = max(1, min(args.steps, 2))
         for _ in range(ne):
             e2e_step()
         t1 = time.perf_counter()
@@ -246,7 +257,23 @@ def main():
                "h2d_bytes_per_step": nint * 16, "d2h_bytes_per_step": nz * 24 + nrec * 12,
                "ms_per_step": esec * 1e3}
         rt.close()
-        del hv, h2, h1
+        del hv, h2, h1, eidx, evalt
+
+    # ---- plain FP64 GPU transform: the comparison leg and accuracy reference ----
+    fp64 = None
+    if prec_name == "split" and not args.no_fp64:
+        ref = run_leg(rotran.RT_PREC_FP64, 0, 0, 1)
+        rh, ri, rv = ref["result"]
+        acc = {}
+        if np.array_equal(rh, hdr) and np.array_equal(ri, idx):
+            d = np.abs(val - rv)
+            acc = {"max_abs_err": float(d.max()), "rms_err": float(np.sqrt(np.mean(d * d))),
+                   "max_abs_value": float(np.abs(rv).max()), "same_elements": True}
+        else:
+            acc = {"same_elements": False}
+        fp64 = {"value": flops * world / ref["sec"] / 1e12, "unit": "TFLOP/s",
+                "ms_per_step": ref["sec"] * 1e3, "steps": 1, "warmup": 0,
+                "split_speedup": ref["sec"] / main["sec"], "split_vs_fp64": acc}
 
     # ---- CPU baseline (rank 0, N = 1) ----
     cpu = None
@@ -256,35 +283,34 @@ def main():
                "sample": res["sample"]}
 
     if rank == 0:
+        achieved = st.flops_gemm_executed / (main["gemm_ms"] / 1e3) / 1e12
         if prec_name == "split":
-            bound, peak, unit = "tensor", bf16_peak, "TFLOP/s"
+            roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                    "frac": achieved / bf16_peak, "traffic": None,
+                    "kernel": "k_split_gemm (tcgen05 BF16 digit products, executed FLOPs)",
+                    "peak_source": f"bf16_tflops of {peak_kind}"}
         else:
-            bound, peak, unit = "fp64", None, "TFLOP/s"
+            roof = {"bound": "fp64", "achieved": achieved, "peak": None, "unit": "TFLOP/s",
+                    "frac": None, "traffic": None, "kernel": "k_gemm_f64"}
         line = {
             "metric": "4-index transform TFLOP/s", "value": value, "unit": "TFLOP/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16x-split/f64" if prec_name == "split" else "f64",
+            "ms_per_step": main["sec"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16-slices/f32-acc (split)" if prec_name == "split" else "f64",
             "data": "synthetic",
             "config": {"workload": work["name"], "n": prob.n, "n_large": work["n_l"],
                        "n_small": work["n_s"], "nkr": work["nkr"], "seed": work["seed"],
-                       "precision": prec_name, "integrals": nint,
-                       "l2": "inputs larger than L2 (records 16 B x integrals)",
+                       "precision": prec_name, "slices": args.slices if prec_name == "split" else None,
+                       "integrals": nint, "flops_algorithmic": flops,
+                       "l2": "inputs larger than L2 (integral records 16 B each)",
                        "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": bound, "achieved": roof_achieved, "peak": peak, "unit": unit,
-                         "frac": (roof_achieved / peak) if peak else None, "traffic": None,
-                         "kernel": "half-transformation GEMMs", "peak_kind": peak_kind},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk.summary(), "stats": rt_stats,
-            "mdcint": {"records": nrec, "elements": nz},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64,
+            "gpu_launches": st.gpu_launches * args.steps, "clocks": main["clocks"],
+            "stats": st.as_dict(), "mdcint": {"records": nrec, "elements": nz},
         }
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
-
-
-def rotran_split_available():
-    return os.environ.get("ROTRAN_BENCH_SPLIT", "0") == "1"
 
 
 if __name__ == "__main__":

@@ -621,38 +621,6 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
     up(g1b.data(), g1b.size(), T.g1_base);
 }
 
-// events around the GEMM launches: their summed device time is the live
-// duration of the dominant kernel class
-namespace {
-struct GemmTimer {
-    rt_ctx* c;
-    std::vector<cudaEvent_t> ev;
-    int used = 0;
-    double flops_exec = 0.0;
-    explicit GemmTimer(rt_ctx* ctx) : c(ctx) {}
-    ~GemmTimer() {
-        for (auto e : ev) cudaEventDestroy(e);
-    }
-    void mark() {
-        if (used == (int)ev.size()) {
-            cudaEvent_t e;
-            RT_CUDA(cudaEventCreate(&e));
-            ev.push_back(e);
-        }
-        RT_CUDA(cudaEventRecord(ev[used++], c->stream));
-    }
-    double total_ms() {
-        double t = 0.0;
-        for (int i = 0; i + 1 < used; i += 2) {
-            float ms = 0.f;
-            RT_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
-            t += ms;
-        }
-        return t;
-    }
-};
-}  // namespace
-
 extern "C" int rt_transform(rt_ctx* ctx) {
     if (!ctx) return RT_ERR_USER;
     std::vector<void*> tmp;
@@ -664,11 +632,13 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     const int n = P.n, m = P.m, K = P.K;
     const int KK1 = (int)P.items.size();
     const bool split = ctx->cfg.precision == RT_PREC_SPLIT_BF16;
-    int launches = 0, gemms = 0;
-    GemmTimer gt(ctx);
-    auto gemm_begin = [&]() { gt.mark(); };
-    auto gemm_end = [&](double fl) { gt.mark(); ++gemms; gt.flops_exec += fl; };
-    const double sfac = split ? split_flop_factor(ctx) : 1.0;
+    int launches = 0;
+    KTimer& kt = ctx->ktimer;
+    kt.reset(st);
+    // the FP64 GEMMs are timed here; the split path times its tensor-core
+    // kernels itself (rt_split.cu), without the slicing kernels around them
+    auto gemm_begin = [&]() { if (!split) kt.begin(); };
+    auto gemm_end = [&](double fl) { if (!split) kt.end(fl); };
     RT_CUDA(cudaEventRecord(ctx->ev[0], st));
     flush_staged(ctx);
     RT_CUDA(cudaEventRecord(ctx->ev[1], st));
@@ -765,7 +735,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
                 else
                     gemm_f64(st, A, nk, (long long)pg.size * nk, ctx->d_qap + (long long)P.blk_start[gg.kblk] * 2 * m,
                              2 * m, 0, npc, 2 * m, nk, nr, epi), ++launches;
-                gemm_end(2.0 * npc * 2.0 * m * nk * nr * sfac);
+                gemm_end(2.0 * npc * 2.0 * m * nk * nr);
             }
             EpiRowMajor e2{ri, (long long)m * npc, 0};
             gemm_begin();
@@ -773,7 +743,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
                 split_gemm24(ctx, ha, 2 * n, (long long)m * npc, e2, &launches);
             else
                 gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2), ++launches;
-            gemm_end(2.0 * 2 * m * (double)m * npc * 2 * n * sfac);
+            gemm_end(2.0 * 2 * m * (double)m * npc * 2 * n);
             launch_tr_select(st, split, ri, m, npc, pg.start + c0, P.P, d_items, d_isign, KK1, d_pvmx,
                              ctx->cfg.thrgen, ctx->d_hp, d_stat + 1);
             launches += (KK1 + 65534) / 65535;
@@ -811,7 +781,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
                 split_gemm3(ctx, cc, m3, nc, nij, e3, &launches);
             else
                 gemm_f64(st, m3, 2 * nc, 0, ctx->d_qar[cc], 2 * m, 0, nc * nij, 2 * m, 2 * nc, 1, e3), ++launches;
-            gemm_end(2.0 * nc * (double)nij * 2 * m * 2 * nc * sfac);
+            gemm_end(2.0 * nc * (double)nij * 2 * m * 2 * nc);
         }
         EpiRowMajor e4{rlr, (long long)nij * m, 0};
         gemm_begin();
@@ -819,7 +789,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             split_gemm24(ctx, rk, 2 * n, (long long)nij * m, e4, &launches);
         else
             gemm_f64(st, ctx->d_qah, 2 * n, 0, rk, (long long)nij * m, 0, 2 * m, nij * m, 2 * n, 1, e4), ++launches;
-        gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n * sfac);
+        gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
         // MDCINT selection for the records of this chunk
         chunk_recs.assign(w.recs.begin() + w.item_rec0[i0], w.recs.begin() + w.item_rec0[i0 + nij]);
         for (int t = i0; t < i0 + nij; ++t)
@@ -871,9 +841,9 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     S.flops_algorithmic = f1 + f2;
     S.device_bytes = (long long)ctx->dev_peak;
     S.gpu_launches = launches;
-    S.gemm_launches = gemms;
-    S.ms_gemm = gt.total_ms();
-    S.flops_gemm_executed = gt.flops_exec;
+    S.gemm_launches = kt.launches;
+    S.ms_gemm = kt.total_ms();
+    S.flops_gemm_executed = kt.flops;
     ctx->transformed = true;
     for (void* p : tmp) dfree(ctx, p);
     tmp.clear();

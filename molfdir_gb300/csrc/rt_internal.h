@@ -119,6 +119,38 @@ struct Work {
 
 struct SplitState;  // rt_split.cu
 
+// CUDA events around the GEMM kernel launches of one transform: their summed
+// device time is the live duration of the dominant kernel class.
+struct KTimer {
+    cudaStream_t st = nullptr;
+    std::vector<cudaEvent_t> ev;
+    int used = 0;
+    int launches = 0;
+    double flops = 0.0;  // FLOPs the timed kernels executed
+    void reset(cudaStream_t s) { st = s; used = 0; launches = 0; flops = 0.0; }
+    void begin() { mark(); }
+    void end(double fl) { mark(); ++launches; flops += fl; }
+    void mark() {
+        if (used == (int)ev.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            ev.push_back(e);
+        }
+        cudaEventRecord(ev[used++], st);
+    }
+    double total_ms() const {
+        double t = 0.0;
+        for (int i = 0; i + 1 < used; i += 2) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ev[i], ev[i + 1]) == cudaSuccess) t += ms;
+        }
+        return t;
+    }
+    ~KTimer() {
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+};
+
 }  // namespace rt
 
 struct rt_ctx {
@@ -136,6 +168,7 @@ struct rt_ctx {
     rt::Stage stage;
     rt::Work work;
     rt::SplitState* split = nullptr;
+    rt::KTimer ktimer;
     // records
     std::vector<int> rec_file, rec_it;
     std::vector<long long> rec_off, rec_nt;

@@ -647,7 +647,10 @@ static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M,
     const long long ntiles = (long long)g.tiles_m * g.tiles_n;
     const int grid = (int)std::min<long long>(ntiles, S->num_sms);
     const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
+    c->ktimer.begin();
     k_split_gemm<Epi><<<grid, 192, smem, c->stream>>>(ma, mb, g, epi);
+    // executed tensor FLOPs: s(s+1)/2 digit products over the padded K
+    c->ktimer.end(2.0 * M * (double)N * Kp * (s * (s + 1) / 2));
     ++*launches;
     RT_CUDA(cudaGetLastError());
 }
@@ -736,6 +739,7 @@ extern "C" int rt_split_dgemm(int M, int N, int K, const double* A, const double
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(RT_ERR_PROGRAM, "no CUDA device");
         RT_CUDA(cudaGetDevice(&ctx.device));
         RT_CUDA(cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking));
+        ctx.ktimer.reset(ctx.stream);
         ctx.cfg.slices = slices;
         SplitState* S = state(&ctx);
         const int Kp = kpad(K);
