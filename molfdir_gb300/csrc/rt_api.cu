@@ -72,8 +72,8 @@ void check_config(const rt_config* cfg) {
     if (cfg->breit) throw Error(RT_ERR_USER, "Breit (Gaunt) integrals are not implemented");
     if (cfg->precision != RT_PREC_FP64 && cfg->precision != RT_PREC_SPLIT_BF16)
         throw Error(RT_ERR_USER, "unknown precision");
-    if (cfg->slices != 0 && (cfg->slices < 2 || cfg->slices > 8))
-        throw Error(RT_ERR_USER, "slices must be 0 or 2..8");
+    if (cfg->slices != 0 && (cfg->slices < 2 || cfg->slices > 6))
+        throw Error(RT_ERR_USER, "slices must be 0 or 2..6");
     if (cfg->n_irrep != 1 && cfg->n_irrep != 4) throw Error(RT_ERR_USER, "n_irrep must be 1 or 4");
     if (cfg->n_irrep == 4) {
         if (!cfg->ao_irrep) throw Error(RT_ERR_USER, "ao_irrep required when n_irrep == 4");
@@ -345,7 +345,7 @@ extern "C" int rt_create(rt_ctx** out, const rt_config* cfg) {
     ctx->cfg = *cfg;
     if (cfg->n_irrep == 4) ctx->ao_irrep.assign(cfg->ao_irrep, cfg->ao_irrep + cfg->nsc);
     ctx->cfg.ao_irrep = nullptr;
-    if (ctx->cfg.slices == 0) ctx->cfg.slices = 7;
+    if (ctx->cfg.slices == 0) ctx->cfg.slices = 6;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();

@@ -107,4 +107,50 @@ __device__ __forceinline__ __nv_bfloat16 digit_bf16(int d, int t) {
     return __float2bfloat16_rn(ldexpf((float)d, -7 * (t - 1)));
 }
 
+// 2^k as a float for -126 <= k <= 127 (0 below)
+__host__ __device__ __forceinline__ float pow2f_safe(int k) {
+    if (k < -126) return 0.0f;
+    if (k > 127) k = 127;
+    union { uint32_t u; float f; } v;
+    v.u = (uint32_t)(k + 127) << 23;
+    return v.f;
+}
+
+// Float-float split of a double by bit operations (no FP64 arithmetic):
+// hi = the leading 24 mantissa bits (truncated), lo = the remaining 29 bits
+// rounded to 24.  hi + lo = x to 2^-48 relative.  |x| must lie in the
+// normal float range (values beyond it give hi = lo = 0 or saturate).
+__device__ __forceinline__ float2 ff_from_double(double x) {
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    const int e = (int)((u >> 52) & 0x7FF);
+    const int fe = e - 1023 + 127;
+    if (e == 0 || fe <= 0) return make_float2(0.f, 0.f);
+    const uint32_t sign = (uint32_t)(u >> 63) << 31;
+    const uint64_t m = u & 0xFFFFFFFFFFFFFull;
+    const float hi = __uint_as_float(sign | ((uint32_t)min(fe, 254) << 23) | (uint32_t)(m >> 29));
+    const float rest = (float)(uint32_t)(m & 0x1FFFFFFFu);  // units of 2^(e-1075)
+    float lo = rest * pow2f_safe(e - 1075 + 0) ;
+    if (e - 1075 < -126) lo = rest * pow2f_safe(e - 1075 + 64) * 5.421010862427522e-20f;  // 2^-64
+    return make_float2(hi, sign ? -lo : lo);
+}
+
+// Digits of a float-float value y = yh + yl with |y| < 1 (already scaled by
+// 2^-S): d_1 = rint(128 yh) in [-128,128], then d_t in [-64,64]; each step
+// is exact (products by 128, rint, Sterbenz subtraction, TwoSum).
+// Writes the pre-scaled BF16 digits d_t * 2^(-7(t-2)) to out[t].
+template <int S>
+__device__ __forceinline__ void ff_digits(float yh, float yl, __nv_bfloat16* out) {
+#pragma unroll
+    for (int t = 0; t < S; ++t) {
+        const float a = yh * 128.0f, b = yl * 128.0f;
+        const float d = rintf(a);
+        const float r = a - d;
+        float h, l;
+        two_sum(r, b, h, l);
+        yh = h;
+        yl = l;
+        out[t] = __float2bfloat16_rn(d * pow2f_safe(7 - 7 * t));
+    }
+}
+
 }  // namespace rt

@@ -40,7 +40,7 @@
 
 namespace rt {
 
-constexpr int SBM = 128, SBN = 128, SBK = 32, NSTAGE = 2, MAX_SLICES = 7;
+constexpr int SBM = 128, SBN = 128, SBK = 32, NSTAGE = 2, MAX_SLICES = 6;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
@@ -67,89 +67,125 @@ struct RowsFF {  // contiguous float-float rows of length K (stride ld)
     __device__ const float2* row(long long i) const { return base + i * ld; }
 };
 
-__global__ void k_slice_rows_f64(RowsF64Batched src, long long M, int K, int Kp, int s,
-                                 __nv_bfloat16* __restrict__ out, int* __restrict__ exps) {
-    const int lane = threadIdx.x & 31;
-    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long i = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < M;
-         i += warps) {
-        const double* p = src.row(i);
-        int S = -2000;
-        for (int k = lane; k < K; k += 32) S = max(S, scale_exp_f64(p[k]));
-        for (int o = 16; o; o >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, o));
-        if (lane == 0) exps[i] = S;
-        for (int k = lane; k < Kp; k += 32) {
-            int d[MAX_SLICES + 1];
-            int64_t X = (k < K && S > -1000) ? fixed_f64(p[k], S, s) : 0;
-            digits7(X, s, d);
-            for (int t = 0; t < s; ++t) out[((long long)t * M + i) * Kp + k] = digit_bf16(d[t], t);
-        }
-    }
+// Element access of the slicing kernels: float-float value and the
+// exponent S with |value| < 2^S.
+__device__ __forceinline__ float2 ff_load(const double* p) { return ff_from_double(*p); }
+__device__ __forceinline__ float2 ff_load(const float2* p) { return *p; }
+__device__ __forceinline__ int exp_load(const double* p) { return scale_exp_f64(*p); }
+__device__ __forceinline__ int exp_load(const float2* p) { return scale_exp_f32(p->x); }
+
+__device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
+    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
-__global__ void k_slice_rows_ff(RowsFF src, long long M, int K, int Kp, int s,
-                                __nv_bfloat16* __restrict__ out, int* __restrict__ exps) {
+// A operand: one warp per row, four consecutive k per lane; output
+// [s][M][Kp] BF16 (K-major) plus the row exponents.
+template <int NS, class Src>
+__global__ void __launch_bounds__(256) k_slice_rows(Src src, long long M, int K, int Kp,
+                                                    __nv_bfloat16* __restrict__ out,
+                                                    int* __restrict__ exps) {
     const int lane = threadIdx.x & 31;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long i = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < M;
          i += warps) {
-        const float2* p = src.row(i);
+        const auto* p = src.row(i);
         int S = -2000;
-        for (int k = lane; k < K; k += 32) S = max(S, scale_exp_f32(p[k].x));
+        for (int k = lane; k < K; k += 32) S = max(S, exp_load(p + k));
         for (int o = 16; o; o >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, o));
         if (lane == 0) exps[i] = S;
-        for (int k = lane; k < Kp; k += 32) {
-            int d[MAX_SLICES + 1];
-            int64_t X = 0;
-            if (k < K && S > -1000) {
-                float2 v = p[k];
-                X = fixed_f32(v.x, S, s) + fixed_f32(v.y, S, s);
+        const float sc = pow2f_safe(-S);
+        for (int k0 = lane * 4; k0 < Kp; k0 += 128) {
+            __nv_bfloat16 d[4][NS];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float2 v = make_float2(0.f, 0.f);
+                if (k0 + j < K && S > -1000) v = ff_load(p + k0 + j);
+                ff_digits<NS>(v.x * sc, v.y * sc, d[j]);
             }
-            digits7(X, s, d);
-            for (int t = 0; t < s; ++t) out[((long long)t * M + i) * Kp + k] = digit_bf16(d[t], t);
+#pragma unroll
+            for (int t = 0; t < NS; ++t) {
+                uint2 w = make_uint2(pack_bf16x2(d[0][t], d[1][t]), pack_bf16x2(d[2][t], d[3][t]));
+                *reinterpret_cast<uint2*>(out + ((long long)t * M + i) * Kp + k0) = w;
+            }
         }
     }
 }
 
-// column scales of a K x N float-float matrix (row-major, ld)
-__global__ void k_col_exp_ff(const float2* __restrict__ src, long long ld, int K, long long N,
-                             int* __restrict__ exps) {
-    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N;
-         j += (long long)gridDim.x * blockDim.x) {
-        int S = -2000;
-        for (int k = 0; k < K; ++k) S = max(S, scale_exp_f32(src[(long long)k * ld + j].x));
-        exps[j] = S;
-    }
-}
-
-// B operand slices, transposed to [s][N][Kp] (K-major) through shared memory
-__global__ void __launch_bounds__(256) k_slice_cols_ff(const float2* __restrict__ src, long long ld,
-                                                       int K, long long N, int Kp, int s,
-                                                       const int* __restrict__ exps,
-                                                       __nv_bfloat16* __restrict__ out) {
-    __shared__ __nv_bfloat16 tile[MAX_SLICES][32][34];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+// B operand: a block handles 32 columns of a K x N float-float matrix:
+// column exponents, then digits transposed through shared memory to
+// [s][N][Kp] (K-major), 64 k per tile.
+template <int NS>
+__global__ void __launch_bounds__(256) k_slice_cols(const float2* __restrict__ src, long long ld,
+                                                    int K, long long N, int Kp,
+                                                    int* __restrict__ exps,
+                                                    __nv_bfloat16* __restrict__ out) {
+    __shared__ __nv_bfloat16 tile[NS][32][66];
+    __shared__ int part[8][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const long long n0 = (long long)blockIdx.x * 32;
-    const int k0 = blockIdx.y * 32;
     const long long n = n0 + tx;
-    const int S = n < N ? exps[n] : -2000;
-    for (int kk = ty; kk < 32; kk += 8) {
-        const int k = k0 + kk;
-        int d[MAX_SLICES + 1];
-        int64_t X = 0;
-        if (n < N && k < K && S > -1000) {
-            float2 v = src[(long long)k * ld + n];
-            X = fixed_f32(v.x, S, s) + fixed_f32(v.y, S, s);
-        }
-        digits7(X, s, d);
-        for (int t = 0; t < s; ++t) tile[t][tx][kk] = digit_bf16(d[t], t);
-    }
+    int S = -2000;
+    if (n < N)
+        for (int k = ty; k < K; k += 8) S = max(S, scale_exp_f32(src[(long long)k * ld + n].x));
+    part[ty][tx] = S;
     __syncthreads();
-    for (int t = 0; t < s; ++t)
-        for (int nn = ty; nn < 32; nn += 8) {
-            const long long col = n0 + nn;
-            if (col < N && k0 + tx < Kp) out[((long long)t * N + col) * Kp + k0 + tx] = tile[t][nn][tx];
+    S = part[0][tx];
+#pragma unroll
+    for (int w = 1; w < 8; ++w) S = max(S, part[w][tx]);
+    if (ty == 0 && n < N) exps[n] = S;
+    const float sc = pow2f_safe(-S);
+    for (int k0 = 0; k0 < Kp; k0 += 64) {
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int kk = ty * 8 + j, k = k0 + kk;
+            float2 v = make_float2(0.f, 0.f);
+            if (n < N && k < K && S > -1000) v = src[(long long)k * ld + n];
+            __nv_bfloat16 d[NS];
+            ff_digits<NS>(v.x * sc, v.y * sc, d);
+#pragma unroll
+            for (int t = 0; t < NS; ++t) tile[t][tx][kk] = d[t];
         }
+        __syncthreads();
+        // warp ty writes rows 4ty..4ty+3 of the strip, 64 k = 128 bytes per row
+        const int kw = k0 + 2 * tx;
+#pragma unroll
+        for (int t = 0; t < NS; ++t)
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const int nn = ty * 4 + rr;
+                const long long col = n0 + nn;
+                if (col < N && kw < Kp) {
+                    uint32_t w = pack_bf16x2(tile[t][nn][2 * tx], tile[t][nn][2 * tx + 1]);
+                    *reinterpret_cast<uint32_t*>(out + ((long long)t * N + col) * Kp + kw) = w;
+                }
+            }
+    }
+}
+
+template <class Src>
+static void launch_slice_rows(int s, Src src, long long M, int K, int Kp, __nv_bfloat16* out,
+                              int* exps, cudaStream_t st) {
+    const unsigned g = (unsigned)std::min<long long>((M + 7) / 8, 152LL * 64);
+    switch (s) {
+        case 2: k_slice_rows<2><<<g, 256, 0, st>>>(src, M, K, Kp, out, exps); break;
+        case 3: k_slice_rows<3><<<g, 256, 0, st>>>(src, M, K, Kp, out, exps); break;
+        case 4: k_slice_rows<4><<<g, 256, 0, st>>>(src, M, K, Kp, out, exps); break;
+        case 5: k_slice_rows<5><<<g, 256, 0, st>>>(src, M, K, Kp, out, exps); break;
+        default: k_slice_rows<6><<<g, 256, 0, st>>>(src, M, K, Kp, out, exps); break;
+    }
+}
+
+static void launch_slice_cols(int s, const float2* src, long long ld, int K, long long N, int Kp,
+                              int* exps, __nv_bfloat16* out, cudaStream_t st) {
+    const unsigned g = (unsigned)((N + 31) / 32);
+    switch (s) {
+        case 2: k_slice_cols<2><<<g, 256, 0, st>>>(src, ld, K, N, Kp, exps, out); break;
+        case 3: k_slice_cols<3><<<g, 256, 0, st>>>(src, ld, K, N, Kp, exps, out); break;
+        case 4: k_slice_cols<4><<<g, 256, 0, st>>>(src, ld, K, N, Kp, exps, out); break;
+        case 5: k_slice_cols<5><<<g, 256, 0, st>>>(src, ld, K, N, Kp, exps, out); break;
+        default: k_slice_cols<6><<<g, 256, 0, st>>>(src, ld, K, N, Kp, exps, out); break;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -211,10 +247,12 @@ struct SplitArgs {
     int* error;
 };
 
-__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+constexpr int EPI_WARPS = 8;                 // two per TMEM lane group
+constexpr int EC = 16;                       // epilogue columns per TMEM load
+constexpr int GEMM_THREADS = 64 + 32 * EPI_WARPS;
 
 template <class Epi>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                  SplitArgs g, Epi epi) {
     extern __shared__ unsigned char smem_raw[];
@@ -222,6 +260,7 @@ __global__ void __launch_bounds__(192, 1)
     __shared__ uint32_t tbase;
     __shared__ volatile int abort_flag;
     __shared__ int issued[NSTAGE];
+    __shared__ float fcol_w[EPI_WARPS][SBN / 2];  // per epilogue warp: 2^ecol of its columns
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int s = g.s;
     const uint32_t slice_a = SBM * SBK * 2, slice_b = SBN * SBK * 2;
@@ -236,7 +275,7 @@ __global__ void __launch_bounds__(192, 1)
             issued[i] = 0;
         }
         mbar_init(&tfull, 1);
-        mbar_init(&tempty, 4);
+        mbar_init(&tempty, EPI_WARPS);
         abort_flag = 0;
         mbar_fence_init();
     }
@@ -315,38 +354,49 @@ __global__ void __launch_bounds__(192, 1)
                 umma_commit(&tfull);
             }
         }
-    } else {  // ---- epilogue: warps 2..5, one TMEM lane per thread ----
+    } else {  // ---- epilogue: warps 2..9; lane group warp%4, column half (warp-2)/4 ----
+        const int ew = warp - 2;
         const int lg = warp & 3;
+        const int chalf = ew >> 2;
         const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
         int it = 0;
         for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x, ++it) {
+            const long long tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
+            // column scale factors of this warp's half tile (warp-local: no
+            // barrier another role could leave waiting)
+            float* fcol = fcol_w[ew];
+            __syncwarp();
+            for (int j = lane; j < SBN / 2; j += 32) {
+                const long long col = tn * SBN + chalf * (SBN / 2) + j;
+                const int e = col < g.N ? g.col_exp[col] : -2000;
+                fcol[j] = e < -1000 ? 0.0f : pow2f_safe(e);
+            }
+            __syncwarp();
             if (!mbar_wait_bounded(&tfull, (uint32_t)(it & 1), &abort_flag, WAIT_NS)) {
                 if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_TMEM);
                 abort_flag = 1;
                 break;
             }
             tc_fence_after();
-            const long long tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
             const long long row = tm * SBM + lg * 32 + lane;
             const int erow = row < g.M ? g.row_exp[row] : -2000;
-            for (int c0 = 0; c0 < SBN; c0 += 32) {
-                uint32_t r0[32], r1[32], r2[32], r3[32];
-                tmem_ld32(tmem + lane_base + (uint32_t)c0, r0);
-                if (s >= 2) tmem_ld32(tmem + lane_base + (uint32_t)(SBN + c0), r1);
-                if (s >= 3) tmem_ld32(tmem + lane_base + (uint32_t)(2 * SBN + c0), r2);
-                if (s >= 4) tmem_ld32(tmem + lane_base + (uint32_t)(3 * SBN + c0), r3);
+            const float frow = erow < -1000 ? 0.0f : pow2f_safe(erow - 28);
+            const typename Epi::Row er = epi.row(row < g.M ? row : 0);
+            for (int c0 = chalf * (SBN / 2); c0 < (chalf + 1) * (SBN / 2); c0 += EC) {
+                uint32_t r0[EC], r1[EC], r2[EC], r3[EC];
+                tmem_ld16(tmem + lane_base + (uint32_t)c0, r0);
+                if (s >= 2) tmem_ld16(tmem + lane_base + (uint32_t)(SBN + c0), r1);
+                if (s >= 3) tmem_ld16(tmem + lane_base + (uint32_t)(2 * SBN + c0), r2);
+                if (s >= 4) tmem_ld16(tmem + lane_base + (uint32_t)(3 * SBN + c0), r3);
                 tmem_ld_wait();
-                if (c0 + 32 == SBN) {  // accumulators drained: release TMEM
+                if (c0 + EC == (chalf + 1) * (SBN / 2)) {  // this warp's accumulators drained
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty);
                 }
                 if (row >= g.M) continue;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const long long col = tn * SBN + c0 + j;
-                    if (col >= g.N) continue;
-                    const int ecol = g.col_exp[col];
+                for (int j = 0; j < EC; ++j) {
                     const float a0 = __uint_as_float(r0[j]);
                     const float a1 = s >= 2 ? __uint_as_float(r1[j]) : 0.f;
                     const float a2 = s >= 3 ? __uint_as_float(r2[j]) : 0.f;
@@ -357,17 +407,11 @@ __global__ void __launch_bounds__(192, 1)
                     two_sum(s1, a2, s2, e2);
                     two_sum(s2, a3, s3, e3);
                     fast_two_sum(s3, (e1 + e2) + e3, hi, lo);
-                    if (ecol < -1000 || erow < -1000) { hi = 0.f; lo = 0.f; }  // zero row / column
-                    else {
-                        const int k = erow + ecol - 28;  // pre-scaled digits carry 2^14 per operand
-                        const int k1 = k / 2, k2 = k - k1;
-                        const float f1 = pow2f(max(-126, min(127, k1))),
-                                    f2 = pow2f(max(-126, min(127, k2)));
-                        hi = hi * f1 * f2;
-                        lo = lo * f1 * f2;
-                    }
-                    epi(row, col, hi, lo);
+                    const float f = fcol[c0 - chalf * (SBN / 2) + j] * frow;  // 2^(erow+ecol-28)
+                    r0[j] = __float_as_uint(hi * f);   // the accumulator registers now hold
+                    r1[j] = __float_as_uint(lo * f);   // the float-float result
                 }
+                epi.store(er, tn * SBN + c0, g.N, r0, r1);
             }
         }
     }
@@ -386,34 +430,63 @@ __global__ void __launch_bounds__(192, 1)
 // ---------------------------------------------------------------------------
 // epilogue functors (float-float outputs)
 // ---------------------------------------------------------------------------
-struct EpiFF_HA {  // GEMM1: row = r*npc + pql, col = plane*m + b
+// Each functor maps an output row once (row()) and then stores EC
+// consecutive columns col0.. of it (store(), columns >= N skipped).
+struct EpiFF_HA {  // GEMM1: row = r*npc + pql, col = plane*m + b -> HA[plane][r0+r][b][pql]
     float2* ha;
     int r0, m, npc;
     long long plane;
-    __device__ __forceinline__ void operator()(long long row, long long col, float hi, float lo) const {
-        long long r = row / npc, q = row - r * npc;
-        int pl = col >= m;
-        long long b = col - pl * m;
-        ha[pl * plane + ((r0 + r) * m + b) * npc + q] = make_float2(hi, lo);
+    typedef float2* Row;
+    __device__ __forceinline__ Row row(long long i) const {
+        const long long r = i / npc, q = i - r * npc;
+        return ha + (r0 + r) * (long long)m * npc + q;
+    }
+    __device__ __forceinline__ void store(Row p, long long col0, long long N, const uint32_t (&h)[EC],
+                                         const uint32_t (&l)[EC]) const {
+#pragma unroll
+        for (int j = 0; j < EC; ++j) {
+            const long long col = col0 + j;
+            if (col >= N) break;
+            const int pl = col >= m;
+            p[pl * plane + (col - pl * m) * npc] = make_float2(__uint_as_float(h[j]), __uint_as_float(l[j]));
+        }
     }
 };
 
-struct EpiFF_RowMajor {
+struct EpiFF_RowMajor {  // C[row][col], leading dimension ldc
     float2* c;
     long long ldc;
-    __device__ __forceinline__ void operator()(long long row, long long col, float hi, float lo) const {
-        c[row * ldc + col] = make_float2(hi, lo);
+    typedef float2* Row;
+    __device__ __forceinline__ Row row(long long i) const { return c + i * ldc; }
+    __device__ __forceinline__ void store(Row p, long long col0, long long N, const uint32_t (&h)[EC],
+                                         const uint32_t (&l)[EC]) const {
+        if (col0 + EC <= N && (((uintptr_t)(p + col0)) & 15) == 0) {
+#pragma unroll
+            for (int j = 0; j < EC; j += 2)
+                *reinterpret_cast<uint4*>(p + col0 + j) = make_uint4(h[j], l[j], h[j + 1], l[j + 1]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < EC; ++j)
+                if (col0 + j < N) p[col0 + j] = make_float2(__uint_as_float(h[j]), __uint_as_float(l[j]));
+        }
     }
 };
 
-struct EpiFF_RK {
+struct EpiFF_RK {  // GEMM3: row = (p, ijl), col = plane*m + k -> RK[plane][c0+p][ijl][k]
     float2* rk;
     int m;
     long long rowoff, plane;
-    __device__ __forceinline__ void operator()(long long row, long long col, float hi, float lo) const {
-        int pl = col >= m;
-        long long k = col - pl * m;
-        rk[pl * plane + (rowoff + row) * m + k] = make_float2(hi, lo);
+    typedef float2* Row;
+    __device__ __forceinline__ Row row(long long i) const { return rk + (rowoff + i) * m; }
+    __device__ __forceinline__ void store(Row p, long long col0, long long N, const uint32_t (&h)[EC],
+                                         const uint32_t (&l)[EC]) const {
+#pragma unroll
+        for (int j = 0; j < EC; ++j) {
+            const long long col = col0 + j;
+            if (col >= N) break;
+            const int pl = col >= m;
+            p[pl * plane + (col - pl * m)] = make_float2(__uint_as_float(h[j]), __uint_as_float(l[j]));
+        }
     }
 };
 
@@ -465,11 +538,20 @@ static void sfree(SplitState* S, void* p) {
     cudaFree(p);
 }
 
+template <class K>
+static void set_smem_limit(K kernel, size_t need, const cudaDeviceProp& prop) {
+    cudaFuncAttributes fa;
+    RT_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    if (need + fa.sharedSizeBytes > prop.sharedMemPerBlockOptin)
+        throw Error(RT_ERR_DIM, "split GEMM stages exceed the shared memory of one SM");
+    RT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+}
+
 static SplitState* state(rt_ctx* c) {
     if (!c->split) {
         SplitState* S = new SplitState();
         S->s = c->cfg.slices;
-        if (S->s > MAX_SLICES) throw Error(RT_ERR_DIM, "at most 7 slices are supported");
+        if (S->s > MAX_SLICES) throw Error(RT_ERR_DIM, "at most 6 slices are supported");
         cudaDriverEntryPointQueryResult q;
         void* fn = nullptr;
         RT_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
@@ -482,9 +564,10 @@ static SplitState* state(rt_ctx* c) {
         S->num_sms = prop.multiProcessorCount;
         S->d_err = (int*)salloc(S, sizeof(int));
         RT_CUDA(cudaMemset(S->d_err, 0, sizeof(int)));
-        RT_CUDA(cudaFuncSetAttribute(k_split_gemm<EpiFF_HA>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448 - 1024));
-        RT_CUDA(cudaFuncSetAttribute(k_split_gemm<EpiFF_RowMajor>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448 - 1024));
-        RT_CUDA(cudaFuncSetAttribute(k_split_gemm<EpiFF_RK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448 - 1024));
+        const size_t need = (size_t)NSTAGE * S->s * (SBM + SBN) * SBK * 2 + 1024;
+        set_smem_limit(k_split_gemm<EpiFF_HA>, need, prop);
+        set_smem_limit(k_split_gemm<EpiFF_RowMajor>, need, prop);
+        set_smem_limit(k_split_gemm<EpiFF_RK>, need, prop);
         c->split = S;
     }
     return c->split;
@@ -648,7 +731,7 @@ static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M,
     const int grid = (int)std::min<long long>(ntiles, S->num_sms);
     const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
     c->ktimer.begin();
-    k_split_gemm<Epi><<<grid, 192, smem, c->stream>>>(ma, mb, g, epi);
+    k_split_gemm<Epi><<<grid, GEMM_THREADS, smem, c->stream>>>(ma, mb, g, epi);
     // executed tensor FLOPs: s(s+1)/2 digit products over the padded K
     c->ktimer.end(2.0 * M * (double)N * Kp * (s * (s + 1) / 2));
     ++*launches;
@@ -674,8 +757,7 @@ void split_gemm1(rt_ctx* c, const G1Group& gg, int c0, int npc, const EpiHA& e, 
     const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk], Kp = kpad(nk);
     const long long M = (long long)nr * npc;
     RowsF64Batched src{c->d_g3 + gg.base, (long long)P.pgroups[gg.pg].size, c0, npc, nk};
-    k_slice_rows_f64<<<(unsigned)std::min<long long>((M + 7) / 8, 152LL * 32), 256, 0, c->stream>>>(
-        src, M, nk, Kp, S->s, S->a_sl, S->a_exp);
+    launch_slice_rows(S->s, src, M, nk, Kp, S->a_sl, S->a_exp, c->stream);
     ++*launches;
     const ConstSlices& B = S->qap[gg.kblk];
     EpiFF_HA epi{(float2*)e.ha, e.r0, e.m, e.npc, e.plane};
@@ -687,11 +769,8 @@ void split_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRo
     SplitState* S = state(c);
     const int Kp = kpad(K);
     const float2* src = (const float2*)Bsrc;
-    k_col_exp_ff<<<(unsigned)std::min<long long>((N + 255) / 256, 152LL * 16), 256, 0, c->stream>>>(
-        src, N, K, N, S->b_exp);
-    dim3 grid((unsigned)((N + 31) / 32), (unsigned)(Kp / 32));
-    k_slice_cols_ff<<<grid, 256, 0, c->stream>>>(src, N, K, N, Kp, S->s, S->b_exp, S->a_sl);
-    *launches += 2;
+    launch_slice_cols(S->s, src, N, K, N, Kp, S->b_exp, S->a_sl, c->stream);
+    *launches += 1;
     EpiFF_RowMajor epi{(float2*)e.c, e.ldc};
     run_gemm(c, S->qah.d, S->qah.exps, S->qah.rows, S->a_sl, S->b_exp, N, Kp, epi, launches);
 }
@@ -702,8 +781,7 @@ void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const E
     const int K = 2 * nc, Kp = kpad(K);
     const long long M = (long long)nc * nij;
     RowsFF src{(const float2*)m3, (long long)K};
-    k_slice_rows_ff<<<(unsigned)std::min<long long>((M + 7) / 8, 152LL * 32), 256, 0, c->stream>>>(
-        src, M, K, Kp, S->s, S->a_sl, S->a_exp);
+    launch_slice_rows(S->s, src, M, K, Kp, S->a_sl, S->a_exp, c->stream);
     ++*launches;
     const ConstSlices& B = S->qar[comp];
     EpiFF_RK epi{(float2*)e.rk, e.m, e.rowoff, e.plane};
@@ -772,8 +850,7 @@ extern "C" int rt_split_dgemm(int M, int N, int K, const double* A, const double
             }
             float2* dbf = (float2*)dal(bf.size() * 8);
             RT_CUDA(cudaMemcpy(dbf, bf.data(), bf.size() * 8, cudaMemcpyHostToDevice));
-            k_col_exp_ff<<<(N + 255) / 256, 256, 0, ctx.stream>>>(dbf, N, K, N, eb);
-            k_slice_cols_ff<<<dim3((N + 31) / 32, Kp / 32), 256, 0, ctx.stream>>>(dbf, N, K, N, Kp, slices, eb, db);
+            launch_slice_cols(slices, dbf, N, K, N, Kp, eb, db, ctx.stream);
             if (mode == 1) {
                 std::vector<float2> af((size_t)M * K);
                 for (size_t i = 0; i < af.size(); ++i) {
@@ -782,12 +859,12 @@ extern "C" int rt_split_dgemm(int M, int N, int K, const double* A, const double
                 }
                 float2* daf = (float2*)dal(af.size() * 8);
                 RT_CUDA(cudaMemcpy(daf, af.data(), af.size() * 8, cudaMemcpyHostToDevice));
-                k_slice_rows_ff<<<(M + 7) / 8, 256, 0, ctx.stream>>>(RowsFF{daf, K}, M, K, Kp, slices, da, ea);
+                launch_slice_rows(slices, RowsFF{daf, K}, M, K, Kp, da, ea, ctx.stream);
             } else {
                 double* dad = (double*)dal((size_t)M * K * 8);
                 RT_CUDA(cudaMemcpy(dad, A, (size_t)M * K * 8, cudaMemcpyHostToDevice));
                 RowsF64Batched src{dad, (long long)M, 0, M, K};
-                k_slice_rows_f64<<<(M + 7) / 8, 256, 0, ctx.stream>>>(src, M, K, Kp, slices, da, ea);
+                launch_slice_rows(slices, src, M, K, Kp, da, ea, ctx.stream);
             }
             RT_CUDA(cudaGetLastError());
         }
