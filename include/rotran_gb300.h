@@ -81,7 +81,7 @@ typedef struct rt_stats {
 typedef struct rt_plan_info {
     long long npairs;          /* pq blocks transformed */
     long long nitems;          /* Kramers-unique spinor pairs, NKR*(NKR+1) */
-    long long g3_bytes;        /* AO integrals expanded to G_pq(r,s) */
+    long long expand_bytes_per_pair; /* FP64 G_pq(r,s) operand of one pq block */
     long long hp_bytes;        /* half-transformed integrals */
     long long nrec[4];         /* MDCINT records per class */
     long long elem_cap[4];     /* upper bound of MDCINT elements per class */

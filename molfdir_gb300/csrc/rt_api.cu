@@ -75,6 +75,9 @@ void check_config(const rt_config* cfg) {
     if (cfg->slices != 0 && (cfg->slices < 2 || cfg->slices > 6))
         throw Error(RT_ERR_USER, "slices must be 0 or 2..6");
     if (cfg->n_irrep != 1 && cfg->n_irrep != 4) throw Error(RT_ERR_USER, "n_irrep must be 1 or 4");
+    // bucket entries pack (block, position) in 3 + 10 bits per index
+    if (cfg->nsc1 > 1023 || cfg->nsc - cfg->nsc1 > 1023)
+        throw Error(RT_ERR_DIM, "more than 1023 functions of one component");
     if (cfg->n_irrep == 4) {
         if (!cfg->ao_irrep) throw Error(RT_ERR_USER, "ao_irrep required when n_irrep == 4");
         for (int p = 0; p < cfg->nsc; ++p)
@@ -165,11 +168,10 @@ void plan_ao(rt_ctx* c) {
             for (int b = 0; b < P.nblk; ++b)
                 if (P.blk_comp[b] == comp && P.blk_irr[b] == (P.blk_irr[rb] ^ pg.gamma)) kb = b;
             if (kb < 0) continue;
-            P.g1.push_back({g, rb, kb, base});
-            base += (long long)P.blk_size[rb] * pg.size * P.blk_size[kb];
+            P.g1.push_back({g, rb, kb, 0, 0});
         }
     }
-    P.g3_doubles = base;
+    (void)base;
     // expansion tables per component
     for (int comp = 0; comp < 2; ++comp) {
         int nc = P.ncomp[comp], off = P.comp_off[comp];
@@ -187,6 +189,38 @@ void plan_ao(rt_ctx* c) {
     (void)ao_pos;
 }
 
+// Expansion bands of every pair group and the per-pair layout of the GEMM1
+// operand buffer (FP64 rows, or BF16 slices when nslices > 0).
+void plan_expand(rt_ctx* c, int nslices) {
+    Plan& P = c->plan;
+    if (P.expand_kp_slices == nslices) return;
+    P.pg_jobs.assign(P.pgroups.size(), {});
+    P.pg_a_pp.assign(P.pgroups.size(), 0);
+    P.pg_e_pp.assign(P.pgroups.size(), 0);
+    for (auto& gg : P.g1) {
+        const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk];
+        const int kp = (nk + 31) / 32 * 32;
+        gg.a_pp = P.pg_a_pp[gg.pg];
+        gg.e_pp = P.pg_e_pp[gg.pg];
+        const int band = std::max(1, std::min(nr, (int)(204800 / (8 * nk))));
+        for (int r0 = 0; r0 < nr; r0 += band) {
+            ExpandJob j;
+            j.rblk = gg.rblk;
+            j.r_lo = r0;
+            j.r_hi = std::min(nr, r0 + band);
+            j.nr = nr;
+            j.nk = nk;
+            j.kp = kp;
+            j.out_pp = gg.a_pp;
+            j.exp_pp = gg.e_pp;
+            P.pg_jobs[gg.pg].push_back(j);
+        }
+        P.pg_a_pp[gg.pg] += nslices ? (long long)nslices * nr * kp : (long long)nr * nk;
+        P.pg_e_pp[gg.pg] += nr;
+    }
+    P.expand_kp_slices = nslices;
+}
+
 // Size of the canonical element set of a record (see in_set in rt_kernels.cu).
 long long set_size(int cls, int i, int j, int K, bool all) {
     if (all || cls == 3) return (long long)K * K;
@@ -199,7 +233,6 @@ struct DeviceTabs {
     unsigned char* pq_read;
     int *pair_of_orig, *pair_group, *pg_start, *pg_size, *ao_block, *ao_pos, *blk_size, *g1_of,
         *g1_kblk;
-    long long* g1_base;
 };
 
 }  // namespace
@@ -530,7 +563,19 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk) {
     Work& w = W(c);
     const int n = P.n, m = P.m;
     const long long KK1 = (long long)P.items.size();
-    if (!c->d_g3) c->d_g3 = dalloc<double>(c, (size_t)P.g3_doubles);
+    const int S0 = c->cfg.precision == RT_PREC_SPLIT_BF16 ? c->cfg.slices : 0;
+    plan_expand(c, S0);
+    if (!c->d_bcount) {
+        c->d_bcount = dalloc<int>(c, (size_t)P.P + 1);
+        c->d_boff = dalloc<long long>(c, (size_t)P.P + 1);
+    }
+    if (c->bucket_cap < 2 * c->n_int) {
+        dfree(c, c->d_bval);
+        dfree(c, c->d_brs);
+        c->bucket_cap = std::max(1LL, 2 * c->n_int);
+        c->d_bval = dalloc<double>(c, (size_t)c->bucket_cap);
+        c->d_brs = dalloc<int>(c, (size_t)c->bucket_cap);
+    }
     if (!c->d_hp) c->d_hp = dalloc<double>(c, (size_t)2 * KK1 * P.P);
     for (int cc = 0; cc < 4; ++cc) {
         if (!c->d_oidx[cc]) {
@@ -547,7 +592,9 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk) {
                                             : (long long)(0.85 * (double)freeb);
     const int S = c->cfg.precision == RT_PREC_SPLIT_BF16 ? c->cfg.slices : 0;
     // bytes per pair of stage A and per item of stage B
-    double per_pair = 16.0 * n * m + 16.0 * m * m;
+    long long a_pp = 0;
+    for (long long v : P.pg_a_pp) a_pp = std::max(a_pp, v);
+    double per_pair = 16.0 * n * m + 16.0 * m * m + (S ? 0.0 : 8.0 * a_pp);
     int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
     double per_item = 16.0 * ncmax * ncmax + 16.0 * n * m + 16.0 * m * m;
     if (S) {
@@ -596,7 +643,6 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
             pqr[(long long)p * (p + 1) / 2 + q] = inc ? 1 : 0;
         }
     std::vector<int> pgroup(P.P), pgs, pgz, aopos(P.n), g1of(P.pgroups.size() * P.nblk, -1), g1k;
-    std::vector<long long> g1b;
     for (size_t g = 0; g < P.pgroups.size(); ++g) {
         pgs.push_back(P.pgroups[g].start);
         pgz.push_back(P.pgroups[g].size);
@@ -606,7 +652,6 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
     for (size_t g = 0; g < P.g1.size(); ++g) {
         g1of[P.g1[g].pg * P.nblk + P.g1[g].rblk] = (int)g;
         g1k.push_back(P.g1[g].kblk);
-        g1b.push_back(P.g1[g].base);
     }
     up(pqr.data(), pqr.size(), T.pq_read);
     up(P.pair_of_orig.data(), P.pair_of_orig.size(), T.pair_of_orig);
@@ -618,7 +663,6 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
     up(P.blk_size.data(), P.blk_size.size(), T.blk_size);
     up(g1of.data(), g1of.size(), T.g1_of);
     up(g1k.data(), g1k.size(), T.g1_kblk);
-    up(g1b.data(), g1b.size(), T.g1_base);
 }
 
 extern "C" int rt_transform(rt_ctx* ctx) {
@@ -693,13 +737,13 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         d_off[cc] = dalloc<long long>(ctx, std::max(1LL, w.nrec[cc]));
         tmp.push_back(d_off[cc]);
     }
-    // ---- scatter the records into G3 (SORT1) ----
-    RT_CUDA(cudaMemsetAsync(ctx->d_g3, 0, P.g3_doubles * sizeof(double), st));
+    // ---- sort the records into pq buckets (SORT1) ----
     ScatterTabs tb{n, ctx->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
-                   T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk, T.g1_base};
-    launch_scatter(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, ctx->n_int, d_roff, d_rmeta,
-                   (int)ctx->rec_off.size(), tb, ctx->d_g3, (unsigned int*)d_stat);
-    launches += ctx->n_int > 0;
+                   T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk};
+    launch_bucket(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, ctx->n_int, d_roff, d_rmeta,
+                  (int)ctx->rec_off.size(), tb, P.P, ctx->d_bcount, ctx->d_boff, ctx->d_bval,
+                  ctx->d_brs, (unsigned int*)d_stat);
+    launches += ctx->n_int > 0 ? 3 : 1;
     RT_CUDA(cudaGetLastError());
     unsigned long long hstat[8];
     RT_CUDA(cudaMemcpyAsync(hstat, d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
@@ -710,31 +754,51 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         throw Error(RT_ERR_USER, "integral outside the (LL|LL)/(SS|LL)/(SS|SS) or irrep block structure");
     RT_CUDA(cudaMemsetAsync(d_stat, 0, 8 * sizeof(unsigned long long), st));
     RT_CUDA(cudaEventRecord(ctx->ev[2], st));
-    if (split) split_prepare_g3(ctx, &launches);
+    // expansion jobs of every pair group
+    std::vector<ExpandJob*> d_jobs(P.pgroups.size(), nullptr);
+    for (size_t g = 0; g < P.pgroups.size(); ++g) {
+        const auto& jv = P.pg_jobs[g];
+        d_jobs[g] = dalloc<ExpandJob>(ctx, std::max<size_t>(1, jv.size()));
+        tmp.push_back(d_jobs[g]);
+        if (!jv.empty())
+            RT_CUDA(cudaMemcpyAsync(d_jobs[g], jv.data(), jv.size() * sizeof(ExpandJob), cudaMemcpyHostToDevice, st));
+    }
+    const int nsl = split ? ctx->cfg.slices : 0;
     // ---- stage A: first half-transformation (TRANS1) per pair chunk ----
     double* ha = ctx->d_ha;
     double* ri = ha + (size_t)2 * n * m * pair_chunk;
+    double* a1 = ri + (size_t)2 * m * m * pair_chunk;  // FP64 GEMM1 operand (plain path)
     for (size_t g = 0; g < P.pgroups.size(); ++g) {
         const PairGroup& pg = P.pgroups[g];
         // does every r block meet this pair group?
         int covered = 0;
+        size_t smem = 0;
         for (auto& gg : P.g1)
             if (gg.pg == (int)g) covered += P.blk_size[gg.rblk];
+        for (auto& j : P.pg_jobs[g]) smem = std::max(smem, (size_t)(j.r_hi - j.r_lo) * j.nk * 8);
         for (int c0 = 0; c0 < pg.size; c0 += pair_chunk) {
             const int npc = std::min(pair_chunk, pg.size - c0);
             const long long plane = (long long)n * m * npc;
             if (covered < n) RT_CUDA(cudaMemsetAsync(ha, 0, 2 * plane * sizeof(double), st));
+            // G_pq(r,s) of the chunk from the buckets
+            if (!P.pg_jobs[g].empty()) {
+                launch_expand_rows(st, nsl, ctx->d_bval, ctx->d_brs, ctx->d_boff, d_jobs[g],
+                                   (int)P.pg_jobs[g].size(), pg.start + c0, npc, T.ao_block, T.ao_pos,
+                                   smem, a1, split ? split_a1_slices(ctx) : nullptr,
+                                   split ? split_a1_exps(ctx) : nullptr);
+                ++launches;
+            }
             for (auto& gg : P.g1) {
                 if (gg.pg != (int)g) continue;
                 const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk];
-                const double* A = ctx->d_g3 + gg.base + (long long)c0 * nk;
                 EpiHA epi{ha, P.blk_start[gg.rblk], m, npc, plane};
                 gemm_begin();
                 if (split)
-                    split_gemm1(ctx, gg, c0, npc, epi, &launches);
+                    split_gemm1(ctx, gg, npc, epi, &launches);
                 else
-                    gemm_f64(st, A, nk, (long long)pg.size * nk, ctx->d_qap + (long long)P.blk_start[gg.kblk] * 2 * m,
-                             2 * m, 0, npc, 2 * m, nk, nr, epi), ++launches;
+                    gemm_f64(st, a1 + gg.a_pp * npc, nk, (long long)npc * nk,
+                             ctx->d_qap + (long long)P.blk_start[gg.kblk] * 2 * m, 2 * m, 0, npc, 2 * m, nk,
+                             nr, epi), ++launches;
                 gemm_end(2.0 * npc * 2.0 * m * nk * nr);
             }
             EpiRowMajor e2{ri, (long long)m * npc, 0};
@@ -935,7 +999,10 @@ extern "C" int rt_plan(const rt_config* cfg, rt_plan_info* out) {
     const long long KK1 = (long long)K * (K + 1);
     out->npairs = P.P;
     out->nitems = KK1;
-    out->g3_bytes = P.g3_doubles * 8;
+    plan_expand(&tmp, 0);
+    long long a_pp = 0;
+    for (long long v : tmp.plan.pg_a_pp) a_pp = std::max(a_pp, v);
+    out->expand_bytes_per_pair = a_pp * 8;
     out->hp_bytes = 2 * KK1 * P.P * 8;
     const bool all = cfg->throut < 0.0;
     for (int i = 1; i <= K; ++i)

@@ -10,10 +10,12 @@
 //                 when S functions exist; makind.F:235-255) grouped by
 //                 (class, pair irrep), inside a group in increasing
 //                 p(p-1)/2+q.  P = number of pairs.
-//   G3            AO integrals expanded per pair-group x r-block:
-//                 G3_g[pq][r][s], r in the r-block, s in the partner block,
-//                 G(pq|rs) with both r<->s orders (the full symmetric
-//                 matrix G_pq(r,s) of the integrals of pair pq).
+//   buckets       the integral records sorted by pq bucket (value + (r,s)),
+//                 one entry per (pq, rs) direction of every stored integral
+//   A1            (stage A, per pair chunk) the GEMM1 operand G_pq(r,s),
+//                 r in an AO block, s in its partner block (both r<->s
+//                 orders: the full symmetric matrix of pair pq), expanded
+//                 from the buckets: [r][pq][s] FP64, or BF16 digit slices
 //   HA            (stage A, per pair chunk) [plane][r][b][pq]: sum_s G_pq(r,s) QA(s,b)
 //   RI            (stage A) [plane][a][b][pq]: sum_r conj(QA(r,a)) HA(r,b)
 //   Hp            [plane][ij][pq]: (pq| I J) = RI(I,J) + s_IJ RI(Jbar,Ibar)
@@ -56,7 +58,8 @@ struct G1Group {
     int pg;          // pair group index
     int rblk;        // AO block of r
     int kblk;        // AO block of s (partner block)
-    long long base;  // offset of G3_g in the G3 arena (doubles)
+    long long a_pp;  // offset of its operand in the expanded chunk buffer, per pair (elements)
+    long long e_pp;  // offset of its row exponents, per pair
 };
 
 struct PairGroup {
@@ -90,7 +93,10 @@ struct Plan {
     std::vector<int> pair_of_orig; // p(p-1)/2+q-1 -> pair order index or -1
     std::vector<int> pair_p, pair_q; // sorted AO positions of each pair (p >= q in reference order)
     std::vector<G1Group> g1;
-    long long g3_doubles = 0;
+    std::vector<std::vector<ExpandJob>> pg_jobs;   // expansion bands per pair group
+    std::vector<long long> pg_a_pp;                // operand elements per pair (all groups)
+    std::vector<long long> pg_e_pp;                // row exponents per pair
+    int expand_kp_slices = -1;                     // slice count the jobs were laid out for
     std::vector<Item> items;      // K(K+1) items in TRANS2 order
     std::vector<int> cls1_rank;   // record position of each item within its class stream(s)
     int n_cls1 = 0, n_cls234 = 0;
@@ -185,7 +191,11 @@ struct rt_ctx {
     int* h_pin_l1 = nullptr;
     size_t pin_cap = 0;
     // device arrays
-    double* d_g3 = nullptr;
+    int* d_bcount = nullptr;      // bucket fill counters [P+1]
+    long long* d_boff = nullptr;  // bucket offsets [P+1]
+    double* d_bval = nullptr;     // bucket entries: value
+    int* d_brs = nullptr;         // bucket entries: r<<16|s
+    long long bucket_cap = 0;
     double* d_qap = nullptr;     // [s_sorted][plane*m + b]     (n x 2m)
     double* d_qah = nullptr;     // [(plane',a)][(plane,r)]     (2m x 2n)
     double* d_qar[2] = {nullptr, nullptr};  // per component: [(plane,q)][(plane',k)] (2nc x 2m)

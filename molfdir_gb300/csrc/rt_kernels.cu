@@ -10,11 +10,6 @@
 
 namespace rt {
 
-// ---------------------------------------------------------------------------
-// record scatter (replaces GETTW + SORT1 + GETSTI: gettw.F:15-56,
-// sort1.F:128-200, getsti.F:250-269)
-// ---------------------------------------------------------------------------
-
 // GETTW's factor for integral type it (gettw.F:33-45).
 __device__ __forceinline__ double gettw_factor(int it) {
     if (it == 1) return 0.125;
@@ -22,67 +17,6 @@ __device__ __forceinline__ double gettw_factor(int it) {
     if (it == 3) return 0.25;
     if (it <= 8) return 0.5;
     return 1.0;
-}
-
-// Each stored integral (ab|cd) (label2 = a<<16|b, label1 = c<<16|d) is
-// scaled by GETTW's type factor and by 2^(number of index coincidences);
-// for a consistent type the product is 1 and the element of the symmetric
-// supermatrix is recovered, which the reference's three symmetrisation
-// steps (MTIMHER, MATMUL3, PPSYM) rebuild implicitly.
-__global__ void k_scatter(const double* __restrict__ rint, const int* __restrict__ l2,
-                          const int* __restrict__ l1, long long nint,
-                          const long long* __restrict__ rec_off, const int2* __restrict__ rec_meta,
-                          int nrec, ScatterTabs tb, double* __restrict__ g3,
-                          unsigned int* __restrict__ status) {
-    long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < nint; x += stride) {
-        // record containing x (records sorted by offset)
-        int lo = 0, hi = nrec - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (rec_off[mid] <= x) lo = mid; else hi = mid - 1;
-        }
-        const int2 meta = rec_meta[lo];
-        const int file = meta.x, it = meta.y;
-        if (file < 1 || file > tb.mfil) continue;  // SORT1 reads files 1..MFIL only
-        int L2 = l2[x], L1 = l1[x];
-        int a = (L2 >> 16) & 0xFFFF, b = L2 & 0xFFFF;
-        int c = (L1 >> 16) & 0xFFFF, d = L1 & 0xFFFF;
-        if (a < 1 || b < 1 || c < 1 || d < 1 || a > tb.n || b > tb.n || c > tb.n || d > tb.n ||
-            d > c) {
-            atomicOr(status, ST_BAD_LABEL);
-            continue;
-        }
-        --a; --b; --c; --d;
-        int pa = a > b ? a : b, pb = a > b ? b : a;
-        // the pq bucket of the reference is label1's pair (sort1.F:139-152)
-        int cdo = c * (c + 1) / 2 + d;
-        if (!tb.pq_read[cdo]) continue;   // INDPQ(pq) == 0: never transformed
-        int coinc = (pa == pb) + (c == d) + (pa == c && pb == d);
-        double v = rint[x] * gettw_factor(it) * (double)(1 << coinc);
-        // direction 1: pair cd against the r,s = a,b indices
-        int abo = pa * (pa + 1) / 2 + pb;
-        for (int dir = 0; dir < 2; ++dir) {
-            int pqo = dir == 0 ? cdo : abo;
-            int r = dir == 0 ? pa : c, s = dir == 0 ? pb : d;
-            if (dir == 1 && abo == cdo) break;
-            int pq = tb.pair_of_orig[pqo];
-            if (pq < 0) { atomicOr(status, ST_BAD_BLOCK); break; }
-            int pg = tb.pair_group[pq];
-            for (int sw = 0; sw < 2; ++sw) {
-                int rr = sw ? s : r, ss = sw ? r : s;
-                if (sw && r == s) break;
-                int rb = tb.ao_block[rr];
-                int g = tb.g1_of[pg * tb.nblk + rb];
-                if (g < 0 || tb.g1_kblk[g] != tb.ao_block[ss]) { atomicOr(status, ST_BAD_BLOCK); break; }
-                long long pql = pq - tb.pg_start[pg];
-                long long off = tb.g1_base[g] +
-                                ((long long)tb.ao_pos[rr] * tb.pg_size[pg] + pql) * tb.blk_size[tb.g1_kblk[g]] +
-                                tb.ao_pos[ss];
-                atomicAdd(&g3[off], v);
-            }
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -363,16 +297,6 @@ __global__ void __launch_bounds__(1024) k_scan_records(const EmitRec* __restrict
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
-void launch_scatter(cudaStream_t st, const double* rint, const int* l2, const int* l1,
-                    long long nint, const long long* rec_off, const int2* rec_meta, int nrec,
-                    const ScatterTabs& tb, double* g3, unsigned int* status) {
-    if (nint <= 0) return;
-    long long blocks = (nint + 255) / 256;
-    if (blocks > 152LL * 64) blocks = 152LL * 64;
-    k_scatter<<<(unsigned)blocks, 256, 0, st>>>(rint, l2, l1, nint, rec_off, rec_meta, nrec, tb,
-                                                 g3, status);
-}
-
 void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc, int pq0, int P,
                       const int4* items, const float* item_sign, int nitems,
                       const double* pair_vmx, double thrgen, double* hp,
@@ -409,6 +333,261 @@ void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, in
             k_emit<F64El><<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, mode,
                                                os);
     }
+}
+
+}  // namespace rt
+
+// ===========================================================================
+// pq buckets of the integral records (the role of SORT1 + INTSRT + GETSTI:
+// sort1.F:128-221, getsti.F:230-278) and their expansion into the GEMM1
+// operand, one pair chunk at a time
+// ===========================================================================
+namespace rt {
+
+// rank of this lane among the active lanes with the same key, after one
+// atomic per distinct key and warp
+__device__ __forceinline__ long long warp_agg_add(int* counter, int key, bool active) {
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    if (mask == 0u) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    const int lkey = __shfl_sync(0xffffffffu, key, leader);
+    // common case of integrals sharing their first pair: one atomic per warp
+    if (__all_sync(0xffffffffu, !active || key == lkey)) {
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&counter[key], __popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        return active ? (long long)base + __popc(mask & ((1u << lane) - 1u)) : -1;
+    }
+    return active ? (long long)atomicAdd(&counter[key], 1) : -1;
+}
+
+// Decode integral x; returns the number of bucket entries (0..2) with their
+// pq buckets and (r,s) labels and the value.
+__device__ __forceinline__ int decode_integral(long long x, const double* __restrict__ rint,
+                                               const int* __restrict__ l2, const int* __restrict__ l1,
+                                               const long long* __restrict__ rec_off,
+                                               const int2* __restrict__ rec_meta, int nrec,
+                                               const ScatterTabs& tb, unsigned int* status,
+                                               int* pqs, int* rss, double& v) {
+    int lo = 0, hi = nrec - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rec_off[mid] <= x) lo = mid; else hi = mid - 1;
+    }
+    const int2 meta = rec_meta[lo];
+    if (meta.x < 1 || meta.x > tb.mfil) return 0;  // SORT1 reads files 1..MFIL only
+    const int L2 = l2[x], L1 = l1[x];
+    int a = (L2 >> 16) & 0xFFFF, b = L2 & 0xFFFF;
+    int c = (L1 >> 16) & 0xFFFF, d = L1 & 0xFFFF;
+    if (a < 1 || b < 1 || c < 1 || d < 1 || a > tb.n || b > tb.n || c > tb.n || d > tb.n || d > c) {
+        atomicOr(status, ST_BAD_LABEL);
+        return 0;
+    }
+    --a; --b; --c; --d;
+    const int pa = a > b ? a : b, pb = a > b ? b : a;
+    const int cdo = c * (c + 1) / 2 + d;
+    if (!tb.pq_read[cdo]) return 0;  // INDPQ(pq) == 0: never transformed
+    const int coinc = (pa == pb) + (c == d) + (pa == c && pb == d);
+    v = rint[x] * gettw_factor(meta.y) * (double)(1 << coinc);
+    const int abo = pa * (pa + 1) / 2 + pb;
+    int ne = 0;
+    for (int dir = 0; dir < 2; ++dir) {
+        if (dir == 1 && abo == cdo) break;
+        const int pq = tb.pair_of_orig[dir == 0 ? cdo : abo];
+        const int r = dir == 0 ? pa : c, s = dir == 0 ? pb : d;
+        if (pq < 0) { atomicOr(status, ST_BAD_BLOCK); return 0; }
+        const int pg = tb.pair_group[pq];
+        const int g = tb.g1_of[pg * tb.nblk + tb.ao_block[r]];
+        if (g < 0 || tb.g1_kblk[g] != tb.ao_block[s]) { atomicOr(status, ST_BAD_BLOCK); return 0; }
+        pqs[ne] = pq;
+        // (block, position) of r and s: the expansion needs no table lookups
+        rss[ne] = (tb.ao_block[r] << 29) | (tb.ao_pos[r] << 19) | (tb.ao_block[s] << 16) |
+                  (tb.ao_pos[s] << 6) | (r == s ? 1 : 0);
+        ++ne;
+    }
+    return ne;
+}
+
+__global__ void __launch_bounds__(256) k_bucket_count(const double* __restrict__ rint, const int* __restrict__ l2,
+                                                      const int* __restrict__ l1, long long nint,
+                                                      const long long* __restrict__ rec_off,
+                                                      const int2* __restrict__ rec_meta, int nrec,
+                                                      ScatterTabs tb, int* __restrict__ count,
+                                                      unsigned int* __restrict__ status) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long base0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    for (long long xb = base0; xb < nint; xb += stride) {
+        const long long x = xb + (threadIdx.x & 31);
+        int pqs[2], rss[2], ne = 0;
+        double v;
+        if (x < nint) ne = decode_integral(x, rint, l2, l1, rec_off, rec_meta, nrec, tb, status, pqs, rss, v);
+        warp_agg_add(count, ne > 0 ? pqs[0] : 0, ne > 0);
+        warp_agg_add(count, ne > 1 ? pqs[1] : 0, ne > 1);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bucket_place(const double* __restrict__ rint, const int* __restrict__ l2,
+                                                      const int* __restrict__ l1, long long nint,
+                                                      const long long* __restrict__ rec_off,
+                                                      const int2* __restrict__ rec_meta, int nrec,
+                                                      ScatterTabs tb, const long long* __restrict__ off,
+                                                      int* __restrict__ fill, double* __restrict__ bval,
+                                                      int* __restrict__ brs, unsigned int* __restrict__ status) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long base0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    for (long long xb = base0; xb < nint; xb += stride) {
+        const long long x = xb + (threadIdx.x & 31);
+        int pqs[2], rss[2], ne = 0;
+        double v = 0.0;
+        if (x < nint) ne = decode_integral(x, rint, l2, l1, rec_off, rec_meta, nrec, tb, status, pqs, rss, v);
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const long long p = warp_agg_add(fill, ne > e ? pqs[e] : 0, ne > e);
+            if (ne > e) {
+                const long long o = off[pqs[e]] + p;
+                bval[o] = v;
+                brs[o] = rss[e];
+            }
+        }
+    }
+}
+
+// exclusive scan of n ints into long long offsets (single block)
+__global__ void __launch_bounds__(1024) k_scan_counts(const int* __restrict__ cnt, int n,
+                                                      long long* __restrict__ off) {
+    __shared__ long long part[1024];
+    const int t = threadIdx.x, per = (n + 1023) / 1024;
+    const int a = t * per, b = min(n, a + per);
+    long long s = 0;
+    for (int i = a; i < b; ++i) s += cnt[i];
+    part[t] = s;
+    __syncthreads();
+    if (t == 0) {
+        long long run = 0;
+        for (int q = 0; q < 1024; ++q) { long long v = part[q]; part[q] = run; run += v; }
+    }
+    __syncthreads();
+    long long o = part[t];
+    for (int i = a; i < b; ++i) { off[i] = o; o += cnt[i]; }
+    if (t == 1023) off[n] = o;
+}
+
+// One CTA per (job, pq of the chunk): job = (GEMM1 group, band of r rows).
+// The band of G_pq(r,s) is accumulated in shared memory from the pq bucket,
+// then written as GEMM1 operand rows: FP64 [r][pql][nk] (nslices == 0) or
+// BF16 digit slices [t][r*npc + pql][Kp] with row exponents (split path).
+template <int NS>
+__global__ void __launch_bounds__(512) k_expand_rows(const double* __restrict__ bval,
+                                                     const int* __restrict__ brs,
+                                                     const long long* __restrict__ off,
+                                                     const ExpandJob* __restrict__ jobs, int pq0,
+                                                     int npc, const int* __restrict__ ao_block,
+                                                     const int* __restrict__ ao_pos,
+                                                     double* __restrict__ out_f64,
+                                                     __nv_bfloat16* __restrict__ out_sl,
+                                                     int* __restrict__ out_exp) {
+    extern __shared__ double tile[];
+    const ExpandJob J = jobs[blockIdx.x];
+    const int pql = blockIdx.y, pq = pq0 + pql;
+    const int rows = J.r_hi - J.r_lo, nk = J.nk;
+    for (int i = threadIdx.x; i < rows * nk; i += blockDim.x) tile[i] = 0.0;
+    __syncthreads();
+    const long long e0 = off[pq], e1 = off[pq + 1];
+    for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const unsigned rs = (unsigned)brs[e];
+        const int br = (int)(rs >> 29), pr0 = (int)((rs >> 19) & 0x3FF);
+        const int bs = (int)((rs >> 16) & 0x7), ps0 = (int)((rs >> 6) & 0x3FF);
+        if (br == J.rblk) {
+            const int pr = pr0 - J.r_lo;
+            if (pr >= 0 && pr < rows) atomicAdd(&tile[pr * nk + ps0], bval[e]);
+        }
+        if (!(rs & 1u) && bs == J.rblk) {
+            const int ps = ps0 - J.r_lo;
+            if (ps >= 0 && ps < rows) atomicAdd(&tile[ps * nk + pr0], bval[e]);
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (NS == 0) {
+        double* o = out_f64 + J.out_pp * npc;
+        for (int i = warp; i < rows; i += nw) {
+            const long long rowo = ((long long)(J.r_lo + i) * npc + pql) * nk;
+            for (int k = lane; k < nk; k += 32) o[rowo + k] = tile[i * nk + k];
+        }
+    } else {
+        __nv_bfloat16* o = out_sl + J.out_pp * npc;
+        const long long M = (long long)J.nr * npc;
+        for (int i = warp; i < rows; i += nw) {
+            const double* p = tile + i * nk;
+            int S = -2000;
+            for (int k = lane; k < nk; k += 32) S = max(S, scale_exp_f64(p[k]));
+            for (int q = 16; q; q >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, q));
+            const long long row = (long long)(J.r_lo + i) * npc + pql;
+            if (lane == 0) out_exp[J.exp_pp * npc + row] = S;
+            const float sc = pow2f_safe(-S);
+            for (int k0 = lane * 2; k0 < J.kp; k0 += 64) {
+                __nv_bfloat16 d0[NS > 0 ? NS : 1], d1[NS > 0 ? NS : 1];
+                float2 v0 = make_float2(0.f, 0.f), v1 = v0;
+                if (S > -1000) {
+                    if (k0 < nk) v0 = ff_from_double(p[k0]);
+                    if (k0 + 1 < nk) v1 = ff_from_double(p[k0 + 1]);
+                }
+                ff_digits<NS>(v0.x * sc, v0.y * sc, d0);
+                ff_digits<NS>(v1.x * sc, v1.y * sc, d1);
+#pragma unroll
+                for (int t = 0; t < NS; ++t) {
+                    const uint32_t w = (uint32_t)__bfloat16_as_ushort(d0[t]) |
+                                       ((uint32_t)__bfloat16_as_ushort(d1[t]) << 16);
+                    *reinterpret_cast<uint32_t*>(o + ((long long)t * M + row) * J.kp + k0) = w;
+                }
+            }
+        }
+    }
+}
+
+void launch_bucket(cudaStream_t st, const double* rint, const int* l2, const int* l1, long long nint,
+                   const long long* rec_off, const int2* rec_meta, int nrec, const ScatterTabs& tb,
+                   int P, int* count, long long* off, double* bval, int* brs,
+                   unsigned int* status) {
+    cudaMemsetAsync(count, 0, sizeof(int) * (P + 1), st);
+    if (nint > 0) {
+        long long blocks = (nint + 255) / 256;
+        if (blocks > 152LL * 32) blocks = 152LL * 32;
+        k_bucket_count<<<(unsigned)blocks, 256, 0, st>>>(rint, l2, l1, nint, rec_off, rec_meta,
+                                                         nrec, tb, count, status);
+    }
+    k_scan_counts<<<1, 1024, 0, st>>>(count, P, off);
+    cudaMemsetAsync(count, 0, sizeof(int) * (P + 1), st);
+    if (nint > 0) {
+        long long blocks = (nint + 255) / 256;
+        if (blocks > 152LL * 32) blocks = 152LL * 32;
+        k_bucket_place<<<(unsigned)blocks, 256, 0, st>>>(rint, l2, l1, nint, rec_off, rec_meta,
+                                                         nrec, tb, off, count, bval, brs, status);
+    }
+}
+
+void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const int* brs,
+                        const long long* off, const ExpandJob* jobs, int njobs, int pq0, int npc,
+                        const int* ao_block, const int* ao_pos, size_t smem, double* out_f64,
+                        __nv_bfloat16* out_sl, int* out_exp) {
+    dim3 grid(njobs, npc);
+#define RT_EXPAND(NSV)                                                                          \
+    do {                                                                                        \
+        cudaFuncSetAttribute(k_expand_rows<NSV>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                             (int)smem);                                                        \
+        k_expand_rows<NSV><<<grid, 512, smem, st>>>(bval, brs, off, jobs, pq0, npc, ao_block,   \
+                                                    ao_pos, out_f64, out_sl, out_exp);          \
+    } while (0)
+    switch (nslices) {
+        case 0: RT_EXPAND(0); break;
+        case 2: RT_EXPAND(2); break;
+        case 3: RT_EXPAND(3); break;
+        case 4: RT_EXPAND(4); break;
+        case 5: RT_EXPAND(5); break;
+        default: RT_EXPAND(6); break;
+    }
+#undef RT_EXPAND
 }
 
 }  // namespace rt

@@ -2,6 +2,7 @@
 // paths.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace rt {
@@ -11,7 +12,7 @@ enum : unsigned int {
     ST_BAD_BLOCK = 2u,   // an integral outside the (LL|LL),(SS|LL),(SS|SS) / irrep block structure
 };
 
-// Index tables used by the record scatter (device pointers).
+// Index tables of the record bucketing (device pointers).
 struct ScatterTabs {
     int n, mfil, nblk;
     const unsigned char* pq_read;  // [n(n+1)/2] rotran transforms this pq bucket (makind.F:235-255)
@@ -24,7 +25,6 @@ struct ScatterTabs {
     const int* blk_size;           // [nblk]
     const int* g1_of;              // [npg*nblk] GEMM1 group of (pair group, r block) or -1
     const int* g1_kblk;            // [ng1] partner block of the group
-    const long long* g1_base;      // [ng1] offset of the group in G3
 };
 
 // One MDCINT record of the current item chunk.
@@ -42,6 +42,17 @@ struct OutStreams {
     int* idx[4];        // (INDK, INDL) pairs
     double* val[4];     // (re, im) pairs
     long long* total;   // [4] running element totals
+};
+
+// One band of rows of one GEMM1 group, expanded from the pq buckets.
+struct ExpandJob {
+    int rblk;         // AO block of r
+    int r_lo, r_hi;   // band of r positions inside the block
+    int nr;           // rows of the block (the group's r extent)
+    int nk;           // columns (size of the partner block)
+    int kp;           // padded K of the slices
+    long long out_pp;   // offset of the group's operand in the output buffer, per pair
+    long long exp_pp;   // offset of the group's row exponents, per pair
 };
 
 // GEMM1 (batched over r): row = pq_local, col = plane*m + b
@@ -87,9 +98,13 @@ template <class Epi>
 void gemm_f64(cudaStream_t st, const double* A, long long lda, long long sA, const double* B,
               long long ldb, long long sB, int M, int N, int K, int batch, Epi epi);
 
-void launch_scatter(cudaStream_t st, const double* rint, const int* l2, const int* l1,
-                    long long nint, const long long* rec_off, const int2* rec_meta, int nrec,
-                    const ScatterTabs& tb, double* g3, unsigned int* status);
+void launch_bucket(cudaStream_t st, const double* rint, const int* l2, const int* l1, long long nint,
+                   const long long* rec_off, const int2* rec_meta, int nrec, const ScatterTabs& tb,
+                   int P, int* count, long long* off, double* bval, int* brs, unsigned int* status);
+void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const int* brs,
+                        const long long* off, const ExpandJob* jobs, int njobs, int pq0, int npc,
+                        const int* ao_block, const int* ao_pos, size_t smem, double* out_f64,
+                        __nv_bfloat16* out_sl, int* out_exp);
 void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc, int pq0, int P,
                       const int4* items, const float* item_sign, int nitems,
                       const double* pair_vmx, double thrgen, double* hp,

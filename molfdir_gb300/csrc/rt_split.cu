@@ -649,14 +649,11 @@ void split_prepare_constants(rt_ctx* c) {
 double split_stageA_bytes_per_pair(rt_ctx* c) {
     const Plan& P = c->plan;
     const int s = c->cfg.slices;
-    int maxnr = 1, maxk = 1;
-    for (auto& g : P.g1) {
-        maxnr = std::max(maxnr, P.blk_size[g.rblk]);
-        maxk = std::max(maxk, kpad(P.blk_size[g.kblk]));
-    }
-    double a = 2.0 * s * maxnr * maxk + 4.0 * maxnr;          // GEMM1 A slices + exps
-    double b = 2.0 * s * P.m * kpad(2 * P.n) + 4.0 * P.m;     // GEMM2 B slices + exps
-    return std::max(a, b);
+    long long a_pp = 0;  // GEMM1 operand slices of all groups of a pair group (BF16 elements)
+    for (long long v : P.pg_a_pp) a_pp = std::max(a_pp, v);
+    double a = 2.0 * a_pp;
+    double b = 2.0 * s * P.m * kpad(2 * P.n);                 // GEMM2 B slices
+    return std::max(a, b) + 8.0 * P.m + 8.0 * P.n;            // + exponents
 }
 
 double split_stageB_bytes_per_item(rt_ctx* c) {
@@ -674,9 +671,9 @@ void split_alloc_work(rt_ctx* c, int pair_chunk, int item_chunk) {
                                     split_stageB_bytes_per_item(c) * item_chunk);
     const Plan& P = c->plan;
     int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
-    int maxnr = 1;
-    for (auto& g : P.g1) maxnr = std::max(maxnr, P.blk_size[g.rblk]);
-    size_t rows = std::max({(size_t)maxnr * pair_chunk, (size_t)P.m * pair_chunk,
+    long long e_pp = 1;
+    for (long long v : P.pg_e_pp) e_pp = std::max(e_pp, v);
+    size_t rows = std::max({(size_t)e_pp * pair_chunk, (size_t)P.m * pair_chunk,
                             (size_t)ncmax * item_chunk, (size_t)P.m * item_chunk});
     sfree(S, S->a_sl);
     sfree(S, S->a_exp);
@@ -689,7 +686,6 @@ void split_alloc_work(rt_ctx* c, int pair_chunk, int item_chunk) {
     S->b_exp_cap = rows;
 }
 
-void split_prepare_g3(rt_ctx* c, int*) { state(c); }
 
 double split_flop_factor(rt_ctx* c) {
     const int s = c->cfg.slices;
@@ -751,17 +747,19 @@ static void check_error(rt_ctx* c) {
 
 void split_check(rt_ctx* c) { check_error(c); }
 
-void split_gemm1(rt_ctx* c, const G1Group& gg, int c0, int npc, const EpiHA& e, int* launches) {
+__nv_bfloat16* split_a1_slices(rt_ctx* c) { return state(c)->a_sl; }
+int* split_a1_exps(rt_ctx* c) { return state(c)->a_exp; }
+
+// GEMM1 of one group on the slices the bucket expansion wrote
+void split_gemm1(rt_ctx* c, const G1Group& gg, int npc, const EpiHA& e, int* launches) {
     SplitState* S = state(c);
     const Plan& P = c->plan;
     const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk], Kp = kpad(nk);
     const long long M = (long long)nr * npc;
-    RowsF64Batched src{c->d_g3 + gg.base, (long long)P.pgroups[gg.pg].size, c0, npc, nk};
-    launch_slice_rows(S->s, src, M, nk, Kp, S->a_sl, S->a_exp, c->stream);
-    ++*launches;
     const ConstSlices& B = S->qap[gg.kblk];
     EpiFF_HA epi{(float2*)e.ha, e.r0, e.m, e.npc, e.plane};
-    run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * P.m, Kp, epi, launches);
+    run_gemm(c, S->a_sl + gg.a_pp * npc, S->a_exp + gg.e_pp * npc, M, B.d, B.exps, 2LL * P.m, Kp,
+             epi, launches);
 }
 
 void split_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRowMajor& e,

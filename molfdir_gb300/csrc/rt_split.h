@@ -11,8 +11,10 @@ void split_prepare_constants(rt_ctx* c);
 double split_stageA_bytes_per_pair(rt_ctx* c);
 double split_stageB_bytes_per_item(rt_ctx* c);
 void split_alloc_work(rt_ctx* c, int pair_chunk, int item_chunk);
-void split_prepare_g3(rt_ctx* c, int* launches);
-void split_gemm1(rt_ctx* c, const G1Group& g, int c0, int npc, const EpiHA& epi, int* launches);
+// GEMM1 operand buffers the bucket expansion fills (slices, row exponents)
+__nv_bfloat16* split_a1_slices(rt_ctx* c);
+int* split_a1_exps(rt_ctx* c);
+void split_gemm1(rt_ctx* c, const G1Group& g, int npc, const EpiHA& epi, int* launches);
 void split_gemm24(rt_ctx* c, const double* B, int K, long long N, const EpiRowMajor& epi,
                   int* launches);
 void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& epi,

@@ -63,7 +63,7 @@ class RtStats(C.Structure):
 
 class RtPlanInfo(C.Structure):
     _fields_ = [("npairs", C.c_longlong), ("nitems", C.c_longlong),
-                ("g3_bytes", C.c_longlong), ("hp_bytes", C.c_longlong),
+                ("expand_bytes_per_pair", C.c_longlong), ("hp_bytes", C.c_longlong),
                 ("nrec", C.c_longlong * 4), ("elem_cap", C.c_longlong * 4),
                 ("flops_algorithmic", C.c_double)]
 

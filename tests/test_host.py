@@ -33,6 +33,7 @@ def test_plan_sizes():
     assert pi.npairs == 24 * 25 // 2 + 40 * 41 // 2
     assert pi.nitems == 32 * 33
     assert list(pi.nrec) == [528] * 4
+    assert pi.expand_bytes_per_pair == 8 * (24 * 24 + 40 * 40)
     # dense-block FLOPs of both half-transformations
     n, m, k, P = 64, 64, 32, pi.npairs
     f1 = 2 * 2 * m * (P * (24 ** 2 + 40 ** 2)) + P * 8 * n * m * m
