@@ -159,6 +159,24 @@ void rt_destroy(rt_ctx* ctx);
 int rt_split_dgemm(int M, int N, int K, const double* A, const double* B, double* C, int slices,
                    int mode);
 
+/* No counterpart in the reference.  C = A B like rt_split_dgemm mode 2, on
+ * DEVICE-resident row-major FP64 matrices (A M x K, B K x N, C M x N),
+ * without allocating: all scratch (slices, scales, error flag, a
+ * float-float copy of B) lives in one fixed 48 MiB device array per device,
+ * so it suits callers that must not call cudaMalloc/cudaFree.  Needs
+ *   256 + r(4M) + r(4N) + r(2 s M Kp) + r(2 s N Kp) + r(8 K N) <= 50331648
+ * bytes, r() rounding up to 256 and Kp = K rounded up to 32 (M = N = K = 1024
+ * fits at 6 slices); larger sizes and K > 1024 return RT_ERR_DIM with the
+ * reason in rt_last_error(NULL).  `stream` is a cudaStream_t (NULL: the
+ * legacy default stream); the call returns after the product is complete.
+ * The first call on each device, with that device current, does a one-time
+ * set-up (device address of the array, kernel attributes); make that first
+ * call before any stream capture.  Every call shares the array and it keeps
+ * the last call's contents: calls that overlap on the GPU (other host
+ * threads, other streams) race and must be serialised by the caller. */
+int rt_split_dgemm_noalloc(int M, int N, int K, const double* A, const double* B, double* C,
+                           int slices, void* stream);
+
 /* KRAMERS pairing check (kramers.F:26-131) on host data: finds the
  * time-reversal partner of every spinor (tolerance 1e-10), writes ITRMO and
  * the largest deviation; returns RT_ERR_PROGRAM, like the reference's

@@ -368,6 +368,8 @@ static void plan_items(rt_ctx* c) {
 
 static thread_local std::string g_create_err;
 
+void rt::set_thread_error(const std::string& msg) { g_create_err = msg; }
+
 extern "C" int rt_create(rt_ctx** out, const rt_config* cfg) {
     if (!out) return RT_ERR_USER;
     *out = nullptr;

@@ -53,6 +53,9 @@ struct Error {
     Error(int c, std::string m) : code(c), msg(std::move(m)) {}
 };
 
+// message returned by rt_last_error(NULL) on the calling thread
+void set_thread_error(const std::string& msg);
+
 // A GEMM1 group: pairs of one pair-group against one r-block.
 struct G1Group {
     int pg;          // pair group index

@@ -32,6 +32,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "rt_ff.cuh"
@@ -490,6 +492,20 @@ struct EpiFF_RK {  // GEMM3: row = (p, ijl), col = plane*m + k -> RK[plane][c0+p
     }
 };
 
+struct EpiF64_RowMajor {  // C[row][col] = hi + lo rounded to FP64, leading dimension ldc
+    double* c;
+    long long ldc;
+    typedef double* Row;
+    __device__ __forceinline__ Row row(long long i) const { return c + i * ldc; }
+    __device__ __forceinline__ void store(Row p, long long col0, long long N, const uint32_t (&h)[EC],
+                                         const uint32_t (&l)[EC]) const {
+#pragma unroll
+        for (int j = 0; j < EC; ++j)
+            if (col0 + j < N)
+                p[col0 + j] = (double)__uint_as_float(h[j]) + (double)__uint_as_float(l[j]);
+    }
+};
+
 // ---------------------------------------------------------------------------
 // state and host orchestration
 // ---------------------------------------------------------------------------
@@ -880,4 +896,148 @@ extern "C" int rt_split_dgemm(int M, int N, int K, const double* A, const double
     split_release(&ctx);
     if (ctx.stream) cudaStreamDestroy(ctx.stream);
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// rt_split_dgemm_noalloc: the same product on device-resident FP64 matrices
+// with every scratch buffer carved from one fixed device array.
+// ---------------------------------------------------------------------------
+namespace rt {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)48 << 20;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+// error flag, row/column exponents, A and B slices, float-float copy of B
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+struct NoallocDevice {
+    unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
+    int num_sms = 0;
+};
+static NoallocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+static PFN_cuTensorMapEncodeTiled_v12000 g_noalloc_encode = nullptr;
+static std::mutex g_noalloc_mutex;
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static size_t noalloc_bytes(long long M, long long N, int K, int s) {
+    const long long Kp = kpad(K);
+    return 256 + align256(4 * (size_t)M) + align256(4 * (size_t)N) +
+           align256((size_t)2 * s * M * Kp) + align256((size_t)2 * s * N * Kp) +
+           align256((size_t)8 * K * N);
+}
+
+// FP64 -> float-float with the leading part rounded to nearest (the same
+// split the host applies before device slicing)
+__global__ void k_ff_round(const double* __restrict__ x, long long n, float2* __restrict__ out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        const float h = __double2float_rn(v);
+        out[i] = make_float2(h, __double2float_rn(v - (double)h));
+    }
+}
+
+// Per-device set-up, with that device current: the device address of the
+// scratch array, the SM count and the GEMM's shared-memory limit.
+static const NoallocDevice& noalloc_setup(int dev) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoallocDevice& d = g_noalloc_dev[dev];
+    if (d.scratch) return d;
+    if (!g_noalloc_encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        RT_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                 cudaEnableDefault, &q));
+        if (!fn || q != cudaDriverEntryPointSuccess)
+            throw Error(RT_ERR_PROGRAM, "cuTensorMapEncodeTiled unavailable");
+        g_noalloc_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    cudaDeviceProp prop;
+    RT_CUDA(cudaGetDeviceProperties(&prop, dev));
+    if (prop.major * 10 + prop.minor != 103)
+        throw Error(RT_ERR_PROGRAM, "rt_split_dgemm_noalloc needs an sm_103 device");
+    set_smem_limit(k_split_gemm<EpiF64_RowMajor>,
+                   (size_t)NSTAGE * MAX_SLICES * (SBM + SBN) * SBK * 2 + 1024, prop);
+    void* p = nullptr;
+    RT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    d.num_sms = prop.multiProcessorCount;
+    d.scratch = (unsigned char*)p;
+    return d;
+}
+
+}  // namespace rt
+
+extern "C" int rt_split_dgemm_noalloc(int M, int N, int K, const double* A, const double* B,
+                                      double* C, int slices, void* stream) {
+    using namespace rt;
+    if (M < 1 || N < 1 || K < 1 || !A || !B || !C || slices < 2 || slices > MAX_SLICES) {
+        set_thread_error("rt_split_dgemm_noalloc: M, N, K >= 1, non-null A, B, C and 2 <= slices <= 6 required");
+        return RT_ERR_USER;
+    }
+    if (K > 1024) {
+        set_thread_error("rt_split_dgemm_noalloc: K > 1024 (the exact FP32 accumulation needs K <= 1024)");
+        return RT_ERR_DIM;
+    }
+    const size_t need = noalloc_bytes(M, N, K, slices);
+    if (need > NOALLOC_SCRATCH_BYTES) {
+        set_thread_error("rt_split_dgemm_noalloc: needs " + std::to_string(need) +
+                         " bytes of scratch, more than the fixed " +
+                         std::to_string(NOALLOC_SCRATCH_BYTES) + " bytes");
+        return RT_ERR_DIM;
+    }
+    try {
+        int dev = 0;
+        RT_CUDA(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) throw Error(RT_ERR_DIM, "device ordinal above 63");
+        const NoallocDevice& D = noalloc_setup(dev);
+        cudaStream_t st = (cudaStream_t)stream;
+        const int s = slices, Kp = kpad(K);
+        unsigned char* w = D.scratch;
+        int* err = (int*)w;
+        w += 256;
+        int* ea = (int*)w;
+        w += align256(4 * (size_t)M);
+        int* eb = (int*)w;
+        w += align256(4 * (size_t)N);
+        __nv_bfloat16* da = (__nv_bfloat16*)w;
+        w += align256((size_t)2 * s * M * Kp);
+        __nv_bfloat16* db = (__nv_bfloat16*)w;
+        w += align256((size_t)2 * s * N * Kp);
+        float2* bff = (float2*)w;
+        // the slicing kernels write every element they are asked for; only
+        // the error flag has to start at zero
+        RT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        const long long nb = (long long)K * N;
+        k_ff_round<<<(unsigned)std::min<long long>((nb + 255) / 256, 152LL * 16), 256, 0, st>>>(B, nb, bff);
+        launch_slice_cols(s, bff, N, K, N, Kp, eb, db, st);
+        launch_slice_rows(s, RowsF64Batched{A, (long long)M, 0, M, K}, M, K, Kp, da, ea, st);
+        RT_CUDA(cudaGetLastError());
+        SplitState S;
+        S.encode = g_noalloc_encode;
+        CUtensorMap ma = make_map(&S, da, (long long)s * M, Kp);
+        CUtensorMap mb = make_map(&S, db, (long long)s * N, Kp);
+        SplitArgs g;
+        g.M = M;
+        g.N = N;
+        g.Kp = Kp;
+        g.s = s;
+        g.tiles_m = (M + SBM - 1) / SBM;
+        g.tiles_n = (N + SBN - 1) / SBN;
+        g.row_exp = ea;
+        g.col_exp = eb;
+        g.error = err;
+        const int grid = std::min(g.tiles_m * g.tiles_n, D.num_sms);
+        const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
+        k_split_gemm<EpiF64_RowMajor><<<grid, GEMM_THREADS, smem, st>>>(ma, mb, g, EpiF64_RowMajor{C, N});
+        RT_CUDA(cudaGetLastError());
+        int e = 0;
+        RT_CUDA(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        RT_CUDA(cudaStreamSynchronize(st));
+        if (e) throw Error(RT_ERR_PROGRAM, "split GEMM gave up waiting (status " + std::to_string(e) + ")");
+    } catch (const Error& e) {
+        set_thread_error("rt_split_dgemm_noalloc: " + e.msg);
+        return e.code;
+    }
+    return RT_OK;
 }

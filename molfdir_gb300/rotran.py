@@ -71,7 +71,8 @@ class RtPlanInfo(C.Structure):
 EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_add_ao_records_bulk", "rt_read_srt_files", "rt_clear_ao_records",
            "rt_transform", "rt_result_sizes", "rt_copy_result", "rt_write_mdcint",
-           "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm"]
+           "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm",
+           "rt_split_dgemm_noalloc"]
 
 _lib = None
 
@@ -110,6 +111,7 @@ def load(build: bool = True):
                                      P(C.c_int), P(C.c_double)]
     lib.rt_split_dgemm.argtypes = [C.c_int, C.c_int, C.c_int, P(C.c_double), P(C.c_double),
                                    P(C.c_double), C.c_int, C.c_int]
+    lib.rt_split_dgemm_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy"):
@@ -308,3 +310,16 @@ def split_dgemm(a: np.ndarray, b: np.ndarray, slices: int = 7, mode: int = 0) ->
     if rc:
         raise RotranError(rc, "rt_split_dgemm failed")
     return c
+
+
+def split_dgemm_noalloc(m: int, n: int, k: int, a_ptr: int, b_ptr: int, c_ptr: int,
+                        slices: int = 6, stream: int = 0) -> None:
+    """C = A B on device-resident row-major FP64 matrices through
+    ``rt_split_dgemm_noalloc`` (no device allocation; fixed scratch array).
+    Pointers and the stream are raw addresses (e.g. ``tensor.data_ptr()``,
+    ``torch.cuda.current_stream().cuda_stream``)."""
+    lib = load()
+    rc = lib.rt_split_dgemm_noalloc(m, n, k, C.c_void_p(a_ptr), C.c_void_p(b_ptr),
+                                    C.c_void_p(c_ptr), slices, C.c_void_p(stream or None))
+    if rc:
+        raise RotranError(rc, lib.rt_last_error(None).decode())
