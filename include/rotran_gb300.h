@@ -59,7 +59,7 @@ typedef struct rt_config {
     int n_irrep;      /* 1, or 4: AO functions carry the labels in ao_irrep and
                          (pq|rs) vanishes unless irr(p)^irr(q) == irr(r)^irr(s) */
     const int* ao_irrep; /* NSC labels 0..n_irrep-1 (NULL when n_irrep == 1) */
-    long long mem_budget; /* device bytes the context may use (0: 90% of free) */
+    long long mem_budget; /* device bytes the context may use (0: 85% of free) */
 } rt_config;
 
 typedef struct rt_stats {
@@ -73,6 +73,7 @@ typedef struct rt_stats {
     int gemm_launches;        /* of which GEMM (half-transformation) kernels */
     double ms_gemm;           /* summed device time of the GEMM kernels */
     double flops_gemm_executed; /* FLOPs the GEMM kernels executed (slice products included) */
+    double flops_gemm_algorithmic; /* the same GEMMs counted once (2 M N K each) */
 } rt_stats;
 
 /* Sizes of a transformation, computed on the host without a device: the

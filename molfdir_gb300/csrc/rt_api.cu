@@ -684,7 +684,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     // the FP64 GEMMs are timed here; the split path times its tensor-core
     // kernels itself (rt_split.cu), without the slicing kernels around them
     auto gemm_begin = [&]() { if (!split) kt.begin(); };
-    auto gemm_end = [&](double fl) { if (!split) kt.end(fl); };
+    auto gemm_end = [&](double fl) { if (!split) kt.end(fl, fl); };
     RT_CUDA(cudaEventRecord(ctx->ev[0], st));
     flush_staged(ctx);
     RT_CUDA(cudaEventRecord(ctx->ev[1], st));
@@ -910,6 +910,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     S.gemm_launches = kt.launches;
     S.ms_gemm = kt.total_ms();
     S.flops_gemm_executed = kt.flops;
+    S.flops_gemm_algorithmic = kt.alg;
     ctx->transformed = true;
     for (void* p : tmp) dfree(ctx, p);
     tmp.clear();

@@ -136,9 +136,10 @@ struct KTimer {
     int used = 0;
     int launches = 0;
     double flops = 0.0;  // FLOPs the timed kernels executed
-    void reset(cudaStream_t s) { st = s; used = 0; launches = 0; flops = 0.0; }
+    double alg = 0.0;    // their algorithmic (one-product) FLOPs
+    void reset(cudaStream_t s) { st = s; used = 0; launches = 0; flops = 0.0; alg = 0.0; }
     void begin() { mark(); }
-    void end(double fl) { mark(); ++launches; flops += fl; }
+    void end(double fl, double al) { mark(); ++launches; flops += fl; alg += al; }
     void mark() {
         if (used == (int)ev.size()) {
             cudaEvent_t e;

@@ -402,8 +402,9 @@ __device__ __forceinline__ int decode_integral(long long x, const double* __rest
         if (g < 0 || tb.g1_kblk[g] != tb.ao_block[s]) { atomicOr(status, ST_BAD_BLOCK); return 0; }
         pqs[ne] = pq;
         // (block, position) of r and s: the expansion needs no table lookups
-        rss[ne] = (tb.ao_block[r] << 29) | (tb.ao_pos[r] << 19) | (tb.ao_block[s] << 16) |
-                  (tb.ao_pos[s] << 6) | (r == s ? 1 : 0);
+        rss[ne] = (int)(((unsigned)tb.ao_block[r] << 29) | ((unsigned)tb.ao_pos[r] << 19) |
+                        ((unsigned)tb.ao_block[s] << 16) | ((unsigned)tb.ao_pos[s] << 6) |
+                        (r == s ? 1u : 0u));
         ++ne;
     }
     return ne;

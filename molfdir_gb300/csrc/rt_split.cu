@@ -723,7 +723,7 @@ static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int
 
 template <class Epi>
 static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M, const void* b_sl,
-                     const int* b_exp, long long N, int Kp, Epi epi, int* launches) {
+                     const int* b_exp, long long N, int K, int Kp, Epi epi, int* launches) {
     SplitState* S = state(c);
     if (M <= 0 || N <= 0) return;
     const int s = S->s;
@@ -745,7 +745,7 @@ static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M,
     c->ktimer.begin();
     k_split_gemm<Epi><<<grid, GEMM_THREADS, smem, c->stream>>>(ma, mb, g, epi);
     // executed tensor FLOPs: s(s+1)/2 digit products over the padded K
-    c->ktimer.end(2.0 * M * (double)N * Kp * (s * (s + 1) / 2));
+    c->ktimer.end(2.0 * M * (double)N * Kp * (s * (s + 1) / 2), 2.0 * M * (double)N * K);
     ++*launches;
     RT_CUDA(cudaGetLastError());
 }
@@ -774,8 +774,8 @@ void split_gemm1(rt_ctx* c, const G1Group& gg, int npc, const EpiHA& e, int* lau
     const long long M = (long long)nr * npc;
     const ConstSlices& B = S->qap[gg.kblk];
     EpiFF_HA epi{(float2*)e.ha, e.r0, e.m, e.npc, e.plane};
-    run_gemm(c, S->a_sl + gg.a_pp * npc, S->a_exp + gg.e_pp * npc, M, B.d, B.exps, 2LL * P.m, Kp,
-             epi, launches);
+    run_gemm(c, S->a_sl + gg.a_pp * npc, S->a_exp + gg.e_pp * npc, M, B.d, B.exps, 2LL * P.m, nk,
+             Kp, epi, launches);
 }
 
 void split_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRowMajor& e,
@@ -786,7 +786,7 @@ void split_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRo
     launch_slice_cols(S->s, src, N, K, N, Kp, S->b_exp, S->a_sl, c->stream);
     *launches += 1;
     EpiFF_RowMajor epi{(float2*)e.c, e.ldc};
-    run_gemm(c, S->qah.d, S->qah.exps, S->qah.rows, S->a_sl, S->b_exp, N, Kp, epi, launches);
+    run_gemm(c, S->qah.d, S->qah.exps, S->qah.rows, S->a_sl, S->b_exp, N, K, Kp, epi, launches);
 }
 
 void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& e,
@@ -799,7 +799,7 @@ void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const E
     ++*launches;
     const ConstSlices& B = S->qar[comp];
     EpiFF_RK epi{(float2*)e.rk, e.m, e.rowoff, e.plane};
-    run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * c->plan.m, Kp, epi, launches);
+    run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * c->plan.m, K, Kp, epi, launches);
 }
 
 void split_release(rt_ctx* c) {
@@ -884,7 +884,7 @@ extern "C" int rt_split_dgemm(int M, int N, int K, const double* A, const double
         }
         float2* dc = (float2*)dal((size_t)M * N * 8);
         RT_CUDA(cudaMemsetAsync(dc, 0, (size_t)M * N * 8, ctx.stream));
-        run_gemm(&ctx, da, ea, M, db, eb, N, Kp, EpiFF_RowMajor{dc, N}, &launches);
+        run_gemm(&ctx, da, ea, M, db, eb, N, K, Kp, EpiFF_RowMajor{dc, N}, &launches);
         check_error(&ctx);
         std::vector<float2> hc((size_t)M * N);
         RT_CUDA(cudaMemcpy(hc.data(), dc, hc.size() * 8, cudaMemcpyDeviceToHost));

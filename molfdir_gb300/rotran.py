@@ -52,7 +52,7 @@ class RtStats(C.Structure):
                 ("ms_total", C.c_double), ("flops_algorithmic", C.c_double),
                 ("device_bytes", C.c_longlong), ("gpu_launches", C.c_int),
                 ("gemm_launches", C.c_int), ("ms_gemm", C.c_double),
-                ("flops_gemm_executed", C.c_double)]
+                ("flops_gemm_executed", C.c_double), ("flops_gemm_algorithmic", C.c_double)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
