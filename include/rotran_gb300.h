@@ -132,6 +132,20 @@ int rt_clear_ao_records(rt_ctx* ctx);
  * in device memory until copied or written. */
 int rt_transform(rt_ctx* ctx);
 
+/* Adjoint of the transformation (no counterpart in the reference, which
+ * has no derivatives).  With the integrals (ij|kl) of all NSP^4 spinor
+ * quadruples defined from QA as rt_transform defines them, and
+ *   E = sum_{ijkl} gamma(i,j,k,l) (ij|kl),
+ * writes dedc(p,x) = dE/dRe QA(p,x) + i dE/dIm QA(p,x) (NSC x NSP COMPLEX*16,
+ * column-major, leading dimension NSC) and *energy = E.  gamma is NSP^4
+ * COMPLEX*16 in Fortran order, host or device memory; only its part
+ * symmetric under pair exchange (ij)<->(kl) contributes.  The
+ * half-transformed integrals are recomputed (without the THRGEN screen),
+ * not taken from an earlier rt_transform.  Needs the context's records and
+ * coefficients and precision RT_PREC_FP64; device memory: the density
+ * (16 NSP^4 bytes) plus the arrays of rt_transform. */
+int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double* energy);
+
 /* Sizes of the MDCINT record stream of the last transform (records without
  * header and terminator; nz = total elements). */
 int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz);

@@ -619,6 +619,7 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk) {
     if (!c->d_ha || c->stage.pair_chunk != pair_chunk || c->stage.item_chunk != item_chunk) {
         dfree(c, c->d_ha);
         c->d_ha = dalloc<double>(c, need);
+        c->ha_len = need;
         c->stage.pair_chunk = pair_chunk;
         c->stage.item_chunk = item_chunk;
         if (S) split_alloc_work(c, pair_chunk, item_chunk);
@@ -667,106 +668,115 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
     up(g1k.data(), g1k.size(), T.g1_kblk);
 }
 
-extern "C" int rt_transform(rt_ctx* ctx) {
-    if (!ctx) return RT_ERR_USER;
+namespace {
+
+// Device tables and temporaries of one pass over the integral records
+// (rt_transform and rt_adjoint), freed when the pass ends.
+struct Pass {
+    rt_ctx* c = nullptr;
     std::vector<void*> tmp;
-    API_TRY
-    if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
+    DeviceTabs T{};
+    long long* d_roff = nullptr;
+    int2* d_rmeta = nullptr;
+    int4* d_items = nullptr;
+    float* d_isign = nullptr;
+    double* d_pvmx = nullptr;
+    int *d_kra = nullptr, *d_krb = nullptr, *d_itrmo = nullptr;
+    int* d_pidx[2] = {nullptr, nullptr};
+    unsigned long long* d_stat = nullptr;
+    int pair_chunk = 0, item_chunk = 0;
+    int launches = 0;
+    bool split = false;
+    explicit Pass(rt_ctx* ctx) : c(ctx) {}
+    ~Pass() {
+        for (void* p : tmp) dfree(c, p);
+    }
+    template <class T>
+    T* alloc(size_t count) {
+        T* p = dalloc<T>(c, count);
+        tmp.push_back(p);
+        return p;
+    }
+    template <class T>
+    T* upload(const T* host, size_t count) {
+        T* p = alloc<T>(count);
+        if (count) RT_CUDA(cudaMemcpyAsync(p, host, count * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+        return p;
+    }
+};
+
+// Work arena, tables, item and Kramers tables on the device.
+void pass_setup(Pass& ps) {
+    rt_ctx* ctx = ps.c;
     Plan& P = ctx->plan;
     Work& w = W(ctx);
-    cudaStream_t st = ctx->stream;
-    const int n = P.n, m = P.m, K = P.K;
+    const int m = P.m, K = P.K;
     const int KK1 = (int)P.items.size();
-    const bool split = ctx->cfg.precision == RT_PREC_SPLIT_BF16;
-    int launches = 0;
-    KTimer& kt = ctx->ktimer;
-    kt.reset(st);
-    // the FP64 GEMMs are timed here; the split path times its tensor-core
-    // kernels itself (rt_split.cu), without the slicing kernels around them
-    auto gemm_begin = [&]() { if (!split) kt.begin(); };
-    auto gemm_end = [&](double fl) { if (!split) kt.end(fl, fl); };
-    RT_CUDA(cudaEventRecord(ctx->ev[0], st));
-    flush_staged(ctx);
-    RT_CUDA(cudaEventRecord(ctx->ev[1], st));
-    int pair_chunk = 0, item_chunk = 0;
-    ensure_fixed(ctx, pair_chunk, item_chunk);
-    // ---- tables (small) ----
-    DeviceTabs T;
-    upload_tables(ctx, T, tmp);
-    long long* d_roff = dalloc<long long>(ctx, ctx->rec_off.size());
-    tmp.push_back(d_roff);
-    int2* d_rmeta = dalloc<int2>(ctx, ctx->rec_off.size());
-    tmp.push_back(d_rmeta);
-    {
-        std::vector<int2> meta(ctx->rec_off.size());
-        for (size_t r = 0; r < meta.size(); ++r) meta[r] = make_int2(ctx->rec_file[r], ctx->rec_it[r]);
-        if (!meta.empty()) {
-            RT_CUDA(cudaMemcpyAsync(d_roff, ctx->rec_off.data(), meta.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
-            RT_CUDA(cudaMemcpyAsync(d_rmeta, meta.data(), meta.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-        }
-    }
-    int4* d_items = dalloc<int4>(ctx, KK1);
-    tmp.push_back(d_items);
-    float* d_isign = dalloc<float>(ctx, KK1);
-    tmp.push_back(d_isign);
-    double* d_pvmx = dalloc<double>(ctx, P.P);
-    tmp.push_back(d_pvmx);
-    int* d_kra = dalloc<int>(ctx, K);
-    int* d_krb = dalloc<int>(ctx, K);
-    int* d_itrmo = dalloc<int>(ctx, m);
-    tmp.push_back(d_kra); tmp.push_back(d_krb); tmp.push_back(d_itrmo);
-    RT_CUDA(cudaMemcpyAsync(d_items, w.items4.data(), KK1 * sizeof(int4), cudaMemcpyHostToDevice, st));
-    RT_CUDA(cudaMemcpyAsync(d_isign, w.isign.data(), KK1 * sizeof(float), cudaMemcpyHostToDevice, st));
-    RT_CUDA(cudaMemcpyAsync(d_pvmx, w.pair_vmx.data(), P.P * sizeof(double), cudaMemcpyHostToDevice, st));
-    RT_CUDA(cudaMemcpyAsync(d_kra, ctx->kra.data(), K * sizeof(int), cudaMemcpyHostToDevice, st));
-    RT_CUDA(cudaMemcpyAsync(d_krb, ctx->krb.data(), K * sizeof(int), cudaMemcpyHostToDevice, st));
-    RT_CUDA(cudaMemcpyAsync(d_itrmo, ctx->itrmo.data(), m * sizeof(int), cudaMemcpyHostToDevice, st));
-    int* d_pidx[2] = {nullptr, nullptr};
-    for (int cc = 0; cc < 2; ++cc) {
-        d_pidx[cc] = dalloc<int>(ctx, P.pidx[cc].size());
-        tmp.push_back(d_pidx[cc]);
-        if (!P.pidx[cc].empty())
-            RT_CUDA(cudaMemcpyAsync(d_pidx[cc], P.pidx[cc].data(), P.pidx[cc].size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    }
-    unsigned long long* d_stat = dalloc<unsigned long long>(ctx, 8);
-    tmp.push_back(d_stat);
-    RT_CUDA(cudaMemsetAsync(d_stat, 0, 8 * sizeof(unsigned long long), st));
-    long long* d_total = dalloc<long long>(ctx, 4);
-    tmp.push_back(d_total);
-    RT_CUDA(cudaMemsetAsync(d_total, 0, 4 * sizeof(long long), st));
-    long long* d_off[4];
-    for (int cc = 0; cc < 4; ++cc) {
-        d_off[cc] = dalloc<long long>(ctx, std::max(1LL, w.nrec[cc]));
-        tmp.push_back(d_off[cc]);
-    }
-    // ---- sort the records into pq buckets (SORT1) ----
-    ScatterTabs tb{n, ctx->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
+    ps.split = ctx->cfg.precision == RT_PREC_SPLIT_BF16;
+    ensure_fixed(ctx, ps.pair_chunk, ps.item_chunk);
+    upload_tables(ctx, ps.T, ps.tmp);
+    std::vector<int2> meta(ctx->rec_off.size());
+    for (size_t r = 0; r < meta.size(); ++r) meta[r] = make_int2(ctx->rec_file[r], ctx->rec_it[r]);
+    ps.d_roff = ps.upload(ctx->rec_off.data(), ctx->rec_off.size());
+    ps.d_rmeta = ps.upload(meta.data(), meta.size());
+    ps.d_items = ps.upload(w.items4.data(), (size_t)KK1);
+    ps.d_isign = ps.upload(w.isign.data(), (size_t)KK1);
+    ps.d_pvmx = ps.upload(w.pair_vmx.data(), (size_t)P.P);
+    ps.d_kra = ps.upload(ctx->kra.data(), (size_t)K);
+    ps.d_krb = ps.upload(ctx->krb.data(), (size_t)K);
+    ps.d_itrmo = ps.upload(ctx->itrmo.data(), (size_t)m);
+    for (int cc = 0; cc < 2; ++cc) ps.d_pidx[cc] = ps.upload(P.pidx[cc].data(), P.pidx[cc].size());
+    ps.d_stat = ps.alloc<unsigned long long>(8);
+    RT_CUDA(cudaMemsetAsync(ps.d_stat, 0, 8 * sizeof(unsigned long long), ctx->stream));
+}
+
+// Sort the records into pq buckets (SORT1) and check their labels.
+void pass_bucketing(Pass& ps) {
+    rt_ctx* ctx = ps.c;
+    Plan& P = ctx->plan;
+    cudaStream_t st = ctx->stream;
+    const DeviceTabs& T = ps.T;
+    ScatterTabs tb{P.n, ctx->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
                    T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk};
-    launch_bucket(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, ctx->n_int, d_roff, d_rmeta,
+    launch_bucket(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, ctx->n_int, ps.d_roff, ps.d_rmeta,
                   (int)ctx->rec_off.size(), tb, P.P, ctx->d_bcount, ctx->d_boff, ctx->d_bval,
-                  ctx->d_brs, (unsigned int*)d_stat);
-    launches += ctx->n_int > 0 ? 3 : 1;
+                  ctx->d_brs, (unsigned int*)ps.d_stat);
+    ps.launches += ctx->n_int > 0 ? 3 : 1;
     RT_CUDA(cudaGetLastError());
     unsigned long long hstat[8];
-    RT_CUDA(cudaMemcpyAsync(hstat, d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
+    RT_CUDA(cudaMemcpyAsync(hstat, ps.d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
     RT_CUDA(cudaStreamSynchronize(st));
     if (hstat[0] & ST_BAD_LABEL)
         throw Error(RT_ERR_USER, "integral label outside 1..NSC or pq label with q > p");
     if (hstat[0] & ST_BAD_BLOCK)
         throw Error(RT_ERR_USER, "integral outside the (LL|LL)/(SS|LL)/(SS|SS) or irrep block structure");
-    RT_CUDA(cudaMemsetAsync(d_stat, 0, 8 * sizeof(unsigned long long), st));
-    RT_CUDA(cudaEventRecord(ctx->ev[2], st));
+    RT_CUDA(cudaMemsetAsync(ps.d_stat, 0, 8 * sizeof(unsigned long long), st));
+}
+
+// First half-transformation (TRANS1 + MTIMHER + TROUT) into the resident
+// half-transformed array ctx->d_hp, one pair chunk at a time.
+void pass_stage_a(Pass& ps, double thrgen) {
+    rt_ctx* ctx = ps.c;
+    Plan& P = ctx->plan;
+    cudaStream_t st = ctx->stream;
+    const int n = P.n, m = P.m;
+    const int KK1 = (int)P.items.size();
+    const bool split = ps.split;
+    const int pair_chunk = ps.pair_chunk;
+    KTimer& kt = ctx->ktimer;
+    // the FP64 GEMMs are timed here; the split path times its tensor-core
+    // kernels itself (rt_split.cu), without the slicing kernels around them
+    auto gemm_begin = [&]() { if (!split) kt.begin(); };
+    auto gemm_end = [&](double fl) { if (!split) kt.end(fl, fl); };
     // expansion jobs of every pair group
     std::vector<ExpandJob*> d_jobs(P.pgroups.size(), nullptr);
     for (size_t g = 0; g < P.pgroups.size(); ++g) {
         const auto& jv = P.pg_jobs[g];
-        d_jobs[g] = dalloc<ExpandJob>(ctx, std::max<size_t>(1, jv.size()));
-        tmp.push_back(d_jobs[g]);
+        d_jobs[g] = ps.alloc<ExpandJob>(std::max<size_t>(1, jv.size()));
         if (!jv.empty())
             RT_CUDA(cudaMemcpyAsync(d_jobs[g], jv.data(), jv.size() * sizeof(ExpandJob), cudaMemcpyHostToDevice, st));
     }
     const int nsl = split ? ctx->cfg.slices : 0;
-    // ---- stage A: first half-transformation (TRANS1) per pair chunk ----
     double* ha = ctx->d_ha;
     double* ri = ha + (size_t)2 * n * m * pair_chunk;
     double* a1 = ri + (size_t)2 * m * m * pair_chunk;  // FP64 GEMM1 operand (plain path)
@@ -785,10 +795,10 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             // G_pq(r,s) of the chunk from the buckets
             if (!P.pg_jobs[g].empty()) {
                 launch_expand_rows(st, nsl, ctx->d_bval, ctx->d_brs, ctx->d_boff, d_jobs[g],
-                                   (int)P.pg_jobs[g].size(), pg.start + c0, npc, T.ao_block, T.ao_pos,
-                                   smem, a1, split ? split_a1_slices(ctx) : nullptr,
+                                   (int)P.pg_jobs[g].size(), pg.start + c0, npc, ps.T.ao_block,
+                                   ps.T.ao_pos, smem, a1, split ? split_a1_slices(ctx) : nullptr,
                                    split ? split_a1_exps(ctx) : nullptr);
-                ++launches;
+                ++ps.launches;
             }
             for (auto& gg : P.g1) {
                 if (gg.pg != (int)g) continue;
@@ -796,34 +806,81 @@ extern "C" int rt_transform(rt_ctx* ctx) {
                 EpiHA epi{ha, P.blk_start[gg.rblk], m, npc, plane};
                 gemm_begin();
                 if (split)
-                    split_gemm1(ctx, gg, npc, epi, &launches);
+                    split_gemm1(ctx, gg, npc, epi, &ps.launches);
                 else
                     gemm_f64(st, a1 + gg.a_pp * npc, nk, (long long)npc * nk,
                              ctx->d_qap + (long long)P.blk_start[gg.kblk] * 2 * m, 2 * m, 0, npc, 2 * m, nk,
-                             nr, epi), ++launches;
+                             nr, epi), ++ps.launches;
                 gemm_end(2.0 * npc * 2.0 * m * nk * nr);
             }
             EpiRowMajor e2{ri, (long long)m * npc, 0};
             gemm_begin();
             if (split)
-                split_gemm24(ctx, ha, 2 * n, (long long)m * npc, e2, &launches);
+                split_gemm24(ctx, ha, 2 * n, (long long)m * npc, e2, &ps.launches);
             else
-                gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2), ++launches;
+                gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2), ++ps.launches;
             gemm_end(2.0 * 2 * m * (double)m * npc * 2 * n);
-            launch_tr_select(st, split, ri, m, npc, pg.start + c0, P.P, d_items, d_isign, KK1, d_pvmx,
-                             ctx->cfg.thrgen, ctx->d_hp, d_stat + 1);
-            launches += (KK1 + 65534) / 65535;
+            launch_tr_select(st, split, ri, m, npc, pg.start + c0, P.P, ps.d_items, ps.d_isign, KK1,
+                             ps.d_pvmx, thrgen, ctx->d_hp, ps.d_stat + 1);
+            ps.launches += (KK1 + 65534) / 65535;
         }
     }
     RT_CUDA(cudaGetLastError());
+}
+
+// Algorithmic FLOPs of the transformation (dense-block count of the
+// reference algorithm).
+double algorithmic_flops(const Plan& P) {
+    const int n = P.n, m = P.m;
+    const double KK1 = (double)P.items.size();
+    double f1 = 0.0;
+    for (auto& gg : P.g1)
+        f1 += 2.0 * P.blk_size[gg.rblk] * (double)P.pgroups[gg.pg].size * P.blk_size[gg.kblk] * 2.0 * m;
+    f1 += (double)P.P * 8.0 * n * (double)m * m;
+    double f2 = 0.0;
+    for (int cc = 0; cc < 2; ++cc) f2 += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
+    f2 = KK1 * (f2 + 8.0 * n * (double)m * m);
+    return f1 + f2;
+}
+
+}  // namespace
+
+extern "C" int rt_transform(rt_ctx* ctx) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
+    Plan& P = ctx->plan;
+    Work& w = W(ctx);
+    cudaStream_t st = ctx->stream;
+    const int n = P.n, m = P.m, K = P.K;
+    const int KK1 = (int)P.items.size();
+    KTimer& kt = ctx->ktimer;
+    kt.reset(st);
+    RT_CUDA(cudaEventRecord(ctx->ev[0], st));
+    flush_staged(ctx);
+    RT_CUDA(cudaEventRecord(ctx->ev[1], st));
+    Pass ps(ctx);
+    pass_setup(ps);
+    const bool split = ps.split;
+    auto gemm_begin = [&]() { if (!split) kt.begin(); };
+    auto gemm_end = [&](double fl) { if (!split) kt.end(fl, fl); };
+    const int item_chunk = ps.item_chunk;
+    long long* d_total = ps.alloc<long long>(4);
+    RT_CUDA(cudaMemsetAsync(d_total, 0, 4 * sizeof(long long), st));
+    long long* d_off[4];
+    for (int cc = 0; cc < 4; ++cc) d_off[cc] = ps.alloc<long long>(std::max(1LL, w.nrec[cc]));
+    // ---- sort the records into pq buckets (SORT1) ----
+    pass_bucketing(ps);
+    RT_CUDA(cudaEventRecord(ctx->ev[2], st));
+    // ---- stage A: first half-transformation (TRANS1) per pair chunk ----
+    pass_stage_a(ps, ctx->cfg.thrgen);
     RT_CUDA(cudaEventRecord(ctx->ev[3], st));
     // ---- stage B: second half-transformation (TRANS2) + PPSYM per item chunk ----
     double* m3 = ctx->d_ha;
     int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
     double* rk = m3 + (size_t)2 * ncmax * ncmax * item_chunk;
     double* rlr = rk + (size_t)2 * n * m * item_chunk;
-    EmitRec* d_recs = dalloc<EmitRec>(ctx, (size_t)3 * item_chunk);
-    tmp.push_back(d_recs);
+    EmitRec* d_recs = ps.alloc<EmitRec>((size_t)3 * item_chunk);
     OutStreams os;
     for (int cc = 0; cc < 4; ++cc) {
         os.cnt[cc] = ctx->d_hdr[cc];
@@ -839,22 +896,22 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         for (int cc = 0; cc < 2; ++cc) {
             const int nc = P.ncomp[cc];
             if (nc == 0) continue;
-            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, d_pidx[cc], nc, m3);
-            ++launches;
+            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, m3);
+            ++ps.launches;
             EpiRK e3{rk, m, (long long)P.comp_off[cc] * nij, rkplane};
             gemm_begin();
             if (split)
-                split_gemm3(ctx, cc, m3, nc, nij, e3, &launches);
+                split_gemm3(ctx, cc, m3, nc, nij, e3, &ps.launches);
             else
-                gemm_f64(st, m3, 2 * nc, 0, ctx->d_qar[cc], 2 * m, 0, nc * nij, 2 * m, 2 * nc, 1, e3), ++launches;
+                gemm_f64(st, m3, 2 * nc, 0, ctx->d_qar[cc], 2 * m, 0, nc * nij, 2 * m, 2 * nc, 1, e3), ++ps.launches;
             gemm_end(2.0 * nc * (double)nij * 2 * m * 2 * nc);
         }
         EpiRowMajor e4{rlr, (long long)nij * m, 0};
         gemm_begin();
         if (split)
-            split_gemm24(ctx, rk, 2 * n, (long long)nij * m, e4, &launches);
+            split_gemm24(ctx, rk, 2 * n, (long long)nij * m, e4, &ps.launches);
         else
-            gemm_f64(st, ctx->d_qah, 2 * n, 0, rk, (long long)nij * m, 0, 2 * m, nij * m, 2 * n, 1, e4), ++launches;
+            gemm_f64(st, ctx->d_qah, 2 * n, 0, rk, (long long)nij * m, 0, 2 * m, nij * m, 2 * n, 1, e4), ++ps.launches;
         gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
         // MDCINT selection for the records of this chunk
         chunk_recs.assign(w.recs.begin() + w.item_rec0[i0], w.recs.begin() + w.item_rec0[i0 + nij]);
@@ -862,17 +919,18 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             for (int r = w.item_rec0[t]; r < w.item_rec0[t + 1]; ++r)
                 chunk_recs[r - w.item_rec0[i0]].ijl = t - i0;
         RT_CUDA(cudaMemcpyAsync(d_recs, chunk_recs.data(), chunk_recs.size() * sizeof(EmitRec), cudaMemcpyHostToDevice, st));
-        launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), d_kra, d_krb, d_itrmo,
-                    ctx->cfg.throut, os);
-        launches += 3;
+        launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), ps.d_kra, ps.d_krb,
+                    ps.d_itrmo, ctx->cfg.throut, os);
+        ps.launches += 3;
         // the host copy of chunk_recs must outlive the async copy
         RT_CUDA(cudaStreamSynchronize(st));
     }
     RT_CUDA(cudaGetLastError());
     RT_CUDA(cudaEventRecord(ctx->ev[4], st));
     long long tot[4];
+    unsigned long long hstat[8];
     RT_CUDA(cudaMemcpyAsync(tot, d_total, sizeof(tot), cudaMemcpyDeviceToHost, st));
-    RT_CUDA(cudaMemcpyAsync(hstat, d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
+    RT_CUDA(cudaMemcpyAsync(hstat, ps.d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
     RT_CUDA(cudaEventRecord(ctx->ev[5], st));
     RT_CUDA(cudaStreamSynchronize(st));
     if (split) split_check(ctx);
@@ -896,24 +954,178 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         S.nfinal[cc] = tot[cc];
         S.nrec[cc] = w.nrec[cc];
     }
-    // algorithmic FLOPs (dense-block count of the reference algorithm)
-    double f1 = 0.0;
-    for (auto& gg : P.g1)
-        f1 += 2.0 * P.blk_size[gg.rblk] * (double)P.pgroups[gg.pg].size * P.blk_size[gg.kblk] * 2.0 * m;
-    f1 += (double)P.P * 8.0 * n * (double)m * m;
-    double f2 = 0.0;
-    for (int cc = 0; cc < 2; ++cc) f2 += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
-    f2 = (double)KK1 * (f2 + 8.0 * n * (double)m * m);
-    S.flops_algorithmic = f1 + f2;
+    S.flops_algorithmic = algorithmic_flops(P);
     S.device_bytes = (long long)ctx->dev_peak;
-    S.gpu_launches = launches;
+    S.gpu_launches = ps.launches;
     S.gemm_launches = kt.launches;
     S.ms_gemm = kt.total_ms();
     S.flops_gemm_executed = kt.flops;
     S.flops_gemm_algorithmic = kt.alg;
     ctx->transformed = true;
-    for (void* p : tmp) dfree(ctx, p);
-    tmp.clear();
+    API_CATCH
+}
+
+// Ordered spinor pairs related to each Kramers-unique item u = (I,J): the
+// half-transformed integral of pair r is t_r(H_u) with
+//   (I,J): H_u,  (J,I): conj(H_u),  (Jbar,Ibar): s H_u,  (Ibar,Jbar): s conj(H_u),
+// s = sign(ITRMO(I) ITRMO(J)).  relk holds k + m l of each distinct related
+// pair (-1: none), relc the factor as +-1 (plain) or +-2 (conjugated).
+// Every ordered pair must belong to exactly one item.
+static void build_relatives(rt_ctx* c, std::vector<int4>& relk, std::vector<int4>& relc) {
+    const Plan& P = c->plan;
+    const int m = P.m;
+    const size_t KK1 = P.items.size();
+    relk.assign(KK1, make_int4(-1, -1, -1, -1));
+    relc.assign(KK1, make_int4(0, 0, 0, 0));
+    std::vector<int> cover((size_t)m * m, 0);
+    for (size_t t = 0; t < KK1; ++t) {
+        const int I = P.items[t].I, J = P.items[t].J;
+        const int Ib = std::abs(c->itrmo[I]) - 1, Jb = std::abs(c->itrmo[J]) - 1;
+        const int s = ((c->itrmo[I] > 0) == (c->itrmo[J] > 0)) ? 1 : -1;
+        const int cand[4][3] = {{I, J, 1}, {J, I, 2}, {Jb, Ib, s}, {Ib, Jb, 2 * s}};
+        int kk[4] = {-1, -1, -1, -1}, cc[4] = {0, 0, 0, 0}, nk = 0;
+        for (auto& r : cand) {
+            const int lin = r[0] + m * r[1];
+            bool seen = false;
+            for (int q = 0; q < nk; ++q) seen = seen || kk[q] == lin;
+            if (seen) continue;
+            kk[nk] = lin;
+            cc[nk] = r[2];
+            ++nk;
+            ++cover[lin];
+        }
+        relk[t] = make_int4(kk[0], kk[1], kk[2], kk[3]);
+        relc[t] = make_int4(cc[0], cc[1], cc[2], cc[3]);
+    }
+    for (int v : cover)
+        if (v != 1) throw Error(RT_ERR_INTERNAL, "Kramers items do not cover the spinor pairs once");
+}
+
+extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double* energy) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    if (!gamma || !dedc) throw Error(RT_ERR_USER, "rt_adjoint: null gamma or dEdC");
+    if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
+    if (ctx->cfg.precision != RT_PREC_FP64)
+        throw Error(RT_ERR_USER, "rt_adjoint needs a context of precision RT_PREC_FP64");
+    Plan& P = ctx->plan;
+    cudaStream_t st = ctx->stream;
+    const int n = P.n, m = P.m;
+    const int KK1 = (int)P.items.size();
+    std::vector<int4> relk, relc;
+    build_relatives(ctx, relk, relc);
+    KTimer& kt = ctx->ktimer;
+    kt.reset(st);
+    RT_CUDA(cudaEventRecord(ctx->ev[0], st));
+    flush_staged(ctx);
+    // the work arena is sized again beside the density
+    dfree(ctx, ctx->d_ha);
+    ctx->d_ha = nullptr;
+    ctx->ha_len = 0;
+    ctx->stage.pair_chunk = ctx->stage.item_chunk = 0;
+    Pass ps(ctx);
+    const size_t ng = (size_t)m * m * m * m;
+    double* d_gam = ps.alloc<double>(2 * ng);
+    RT_CUDA(cudaMemcpyAsync(d_gam, gamma, 2 * ng * sizeof(double), cudaMemcpyDefault, st));
+    launch_gamma_sym(st, d_gam, m);
+    ++ps.launches;
+    int4* d_relk = ps.upload(relk.data(), relk.size());
+    int4* d_relc = ps.upload(relc.data(), relc.size());
+    const long long nacc = (long long)n * 2 * m;
+    double* d_acc = ps.alloc<double>((size_t)nacc);
+    RT_CUDA(cudaMemsetAsync(d_acc, 0, nacc * sizeof(double), st));
+    pass_setup(ps);
+    RT_CUDA(cudaEventRecord(ctx->ev[1], st));
+    pass_bucketing(ps);
+    RT_CUDA(cudaEventRecord(ctx->ev[2], st));
+    // recompute the half-transformed integrals, unscreened
+    pass_stage_a(ps, 0.0);
+    RT_CUDA(cudaEventRecord(ctx->ev[3], st));
+    // ---- per item chunk: X_{u,plane} = h_{u,plane} C, then
+    //      S += sum_{u,plane} X_{u,plane} Ghat_{u,plane} (split-K over items) ----
+    const int G = 8;  // items per partial product
+    const int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+    const double per_item = 4.0 * n * m + 2.0 * ncmax * ncmax + 8.0 * m * m + 2.0 * n * m / G + 1.0;
+    int chunk = (int)std::min<double>(KK1, std::max(1.0, std::floor((double)ctx->ha_len / per_item)));
+    if (chunk > G) chunk -= chunk % G;
+    if ((double)chunk * per_item > (double)ctx->ha_len + 1e-9 * per_item)
+        throw Error(RT_ERR_DIM, "rt_adjoint: work arena too small for one item");
+    for (int i0 = 0; i0 < KK1; i0 += chunk) {
+        const int nij = std::min(chunk, KK1 - i0);
+        double* X = ctx->d_ha;
+        double* m3 = X + (size_t)4 * n * m * nij;
+        double* bh = m3 + (size_t)2 * ncmax * ncmax * nij;
+        double* part = bh + (size_t)8 * m * m * nij;
+        for (int cc = 0; cc < 2; ++cc) {
+            const int nc = P.ncomp[cc];
+            if (nc == 0) continue;
+            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, m3);
+            ++ps.launches;
+            EpiRowMajor ex{X + (size_t)P.comp_off[cc] * nij * 4 * m, 2LL * m, 0};
+            kt.begin();
+            gemm_f64(st, m3, nc, 0, ctx->d_qap + (long long)P.comp_off[cc] * 2 * m, 2 * m, 0,
+                     2 * nc * nij, 2 * m, nc, 1, ex);
+            kt.end(2.0 * (2.0 * nc * nij) * 2 * m * nc, 2.0 * (2.0 * nc * nij) * 2 * m * nc);
+            ++ps.launches;
+        }
+        launch_gamma_hat(st, false, d_gam, m, d_relk, d_relc, ps.d_itrmo, i0, nij, bh);
+        ++ps.launches;
+        const int nb = nij / G, rem = nij - nb * G;
+        const long long K1 = 4LL * m * G, lda = 4LL * m * nij;
+        kt.begin();
+        if (nb)
+            gemm_f64(st, X, lda, K1, bh, 2 * m, K1 * 2 * m, n, 2 * m, (int)K1, nb,
+                     EpiRowMajor{part, 2LL * m, nacc}), ++ps.launches;
+        if (rem)
+            gemm_f64(st, X + nb * K1, lda, 0, bh + (size_t)nb * K1 * 2 * m, 2 * m, 0, n, 2 * m,
+                     4 * m * rem, 1, EpiRowMajor{part + (size_t)nb * nacc, 2LL * m, 0}), ++ps.launches;
+        kt.end(2.0 * n * 2 * m * 4.0 * m * nij, 2.0 * n * 2 * m * 4.0 * m * nij);
+        launch_partial_sum(st, false, part, nb + (rem > 0 ? 1 : 0), nacc, d_acc);
+        ++ps.launches;
+    }
+    RT_CUDA(cudaGetLastError());
+    RT_CUDA(cudaEventRecord(ctx->ev[4], st));
+    std::vector<double> acc((size_t)nacc);
+    RT_CUDA(cudaMemcpyAsync(acc.data(), d_acc, nacc * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RT_CUDA(cudaEventRecord(ctx->ev[5], st));
+    RT_CUDA(cudaStreamSynchronize(st));
+    // dE/dRe C + i dE/dIm C = 4 S (rows back in the caller's AO order);
+    // E = sum conj(C) S (E is of degree 2 in conj(C))
+    std::vector<double> out((size_t)2 * n * m);
+    double e = 0.0;
+    for (int p = 0; p < n; ++p) {
+        const double* row = acc.data() + (size_t)P.ao_sorted[p] * 2 * m;
+        for (int x = 0; x < m; ++x) {
+            const double sr = row[x], si = row[m + x];
+            const size_t o = 2 * ((size_t)p + (size_t)n * x);
+            out[o] = 4.0 * sr;
+            out[o + 1] = 4.0 * si;
+            e += ctx->qa[o] * sr + ctx->qa[o + 1] * si;
+        }
+    }
+    RT_CUDA(cudaMemcpy(dedc, out.data(), out.size() * sizeof(double), cudaMemcpyDefault));
+    if (energy) *energy = e;
+    float ms[5];
+    for (int q = 0; q < 5; ++q) RT_CUDA(cudaEventElapsedTime(&ms[q], ctx->ev[q], ctx->ev[q + 1]));
+    rt_stats& S = ctx->stats;
+    S.ms_upload = ms[0];
+    S.ms_scatter = ms[1];
+    S.ms_first = ms[2];
+    S.ms_second = ms[3];
+    S.ms_output = ms[4];
+    float tot_ms = 0;
+    RT_CUDA(cudaEventElapsedTime(&tot_ms, ctx->ev[0], ctx->ev[5]));
+    S.ms_total = tot_ms;
+    double fx = 0.0;
+    for (int cc = 0; cc < 2; ++cc) fx += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
+    S.flops_algorithmic = (algorithmic_flops(P) - (double)KK1 * (fx + 8.0 * n * (double)m * m)) +
+                          (double)KK1 * (fx + 16.0 * n * (double)m * m);
+    S.device_bytes = (long long)ctx->dev_peak;
+    S.gpu_launches = ps.launches;
+    S.gemm_launches = kt.launches;
+    S.ms_gemm = kt.total_ms();
+    S.flops_gemm_executed = kt.flops;
+    S.flops_gemm_algorithmic = kt.alg;
     API_CATCH
 }
 

@@ -204,6 +204,7 @@ struct rt_ctx {
     double* d_qah = nullptr;     // [(plane',a)][(plane,r)]     (2m x 2n)
     double* d_qar[2] = {nullptr, nullptr};  // per component: [(plane,q)][(plane',k)] (2nc x 2m)
     double* d_ha = nullptr;
+    size_t ha_len = 0;  // doubles in d_ha
     double* d_ri = nullptr;
     double* d_hp = nullptr;
     double* d_m3 = nullptr;

@@ -106,12 +106,17 @@ struct F64El {
     static __device__ __forceinline__ T comb(T a, T b, double sg) { return a + sg * b; }
     static __device__ __forceinline__ double val(T a) { return a; }
     static __device__ __forceinline__ T zero() { return 0.0; }
+    static __device__ __forceinline__ T from(double v) { return v; }
 };
 struct FFEl {
     typedef float2 T;
     static __device__ __forceinline__ T comb(T a, T b, double sg) { return ff_add(a, b, (float)sg); }
     static __device__ __forceinline__ double val(T a) { return ff_to_double(a); }
     static __device__ __forceinline__ T zero() { return make_float2(0.f, 0.f); }
+    static __device__ __forceinline__ T from(double v) {
+        const float h = __double2float_rn(v);
+        return make_float2(h, __double2float_rn(v - (double)h));
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -589,6 +594,129 @@ void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const 
         default: RT_EXPAND(6); break;
     }
 #undef RT_EXPAND
+}
+
+// ===========================================================================
+// adjoint: dE/dC of E = sum_{ijkl} Gamma_ijkl (ij|kl)
+// ===========================================================================
+
+// In-place pair-exchange symmetrisation, 32 x 32 tiles of the m^2 x m^2
+// complex matrix; the block of tile pair (bi, bj), bi <= bj, owns both tiles.
+__global__ void k_gamma_sym(double2* __restrict__ g, long long M2) {
+    __shared__ double2 ta[32][33], tb[32][33];
+    const long long bi = blockIdx.y, bj = blockIdx.x;
+    if (bi > bj) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    for (int r = ty; r < 32; r += 8) {
+        const long long ra = bi * 32 + r, ca = bj * 32 + tx;  // tile (bi, bj)
+        const long long rb = bj * 32 + r, cb = bi * 32 + tx;  // tile (bj, bi)
+        ta[r][tx] = (ra < M2 && ca < M2) ? g[ca * M2 + ra] : make_double2(0.0, 0.0);
+        tb[r][tx] = (rb < M2 && cb < M2) ? g[cb * M2 + rb] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    // element (ra, ca) of tile a pairs with (ca, ra), held in tile b at [tx][r]
+    for (int r = ty; r < 32; r += 8) {
+        const long long ra = bi * 32 + r, ca = bj * 32 + tx;
+        const long long rb = bj * 32 + r, cb = bi * 32 + tx;
+        const double2 a = ta[r][tx], at = tb[tx][r];
+        const double2 b = tb[r][tx], bt = ta[tx][r];
+        if (ra < M2 && ca < M2) g[ca * M2 + ra] = make_double2(0.5 * (a.x + at.x), 0.5 * (a.y + at.y));
+        if (bi != bj && rb < M2 && cb < M2)
+            g[cb * M2 + rb] = make_double2(0.5 * (b.x + bt.x), 0.5 * (b.y + bt.y));
+    }
+}
+
+void launch_gamma_sym(cudaStream_t st, double* gamma, int m) {
+    const long long M2 = (long long)m * m;
+    const long long T = (M2 + 31) / 32;
+    if (T > 65535) throw_dim("adjoint: NSP^2 above 2^21");
+    dim3 grid((unsigned)T, (unsigned)T), block(32, 8);
+    k_gamma_sym<<<grid, block, 0, st>>>((double2*)gamma, M2);
+}
+
+// Contraction operand of item it = i0 + ij (Kramers-unique pair u = (I,J)).
+// relk: Gamma indices k + m l of the distinct ordered pairs r related to u
+// (-1: none), relc: +-1 (value s_r H_u) or +-2 (s_r conj(H_u)).  With
+// T_r(y,x) = Gs(x,y,r) + sigma_yx Gs(ybar,xbar,r):
+//   Ghat_re(y,x) = sum_r s_r T_r(y,x),  Ghat_im(y,x) = i sum_r (+-) s_r T_r(y,x)
+// (- for conjugated relatives), written real-ified as rows
+// ((ij*2 + plane)*2 + ri)*m + y, columns ri_out*m + x:  [Re Im; -Im Re].
+template <class E>
+__global__ void k_gamma_hat(const double2* __restrict__ gs, int m, const int4* __restrict__ relk,
+                            const int4* __restrict__ relc, const int* __restrict__ itrmo, int i0,
+                            typename E::T* __restrict__ out) {
+    const int ij = blockIdx.x, y = blockIdx.y;
+    const int it = i0 + ij;
+    const int4 rk = relk[it], rc = relc[it];
+    const int kr[4] = {rk.x, rk.y, rk.z, rk.w}, cr[4] = {rc.x, rc.y, rc.z, rc.w};
+    const int ty_ = itrmo[y];
+    const int yb = abs(ty_) - 1;
+    const long long M2 = (long long)m * m;
+    const long long ldo = 2LL * m;
+    for (int x = threadIdx.x; x < m; x += blockDim.x) {
+        const int tx_ = itrmo[x];
+        const int xb = abs(tx_) - 1;
+        const double sg = ((ty_ > 0) == (tx_ > 0)) ? 1.0 : -1.0;
+        double2 vr = make_double2(0.0, 0.0), vi = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if (kr[r] < 0) continue;
+            const long long base = (long long)kr[r] * M2;
+            const double2 g1 = gs[base + x + (long long)m * y];
+            const double2 g2 = gs[base + yb + (long long)m * xb];
+            const double tr = g1.x + sg * g2.x, ti = g1.y + sg * g2.y;
+            const double s = cr[r] > 0 ? 1.0 : -1.0;
+            const double si = (cr[r] == 2 || cr[r] == -2) ? -s : s;
+            vr.x += s * tr;
+            vr.y += s * ti;
+            vi.x -= si * ti;  // i * (tr + i ti) = -ti + i tr
+            vi.y += si * tr;
+        }
+        const long long row0 = ((long long)ij * 2) * 2 * m + y;  // plane 0, ri 0
+#pragma unroll
+        for (int pl = 0; pl < 2; ++pl) {
+            const double2 v = pl ? vi : vr;
+            const long long ra = row0 + (long long)pl * 2 * m, rb = ra + m;
+            out[ra * ldo + x] = E::from(v.x);
+            out[ra * ldo + m + x] = E::from(v.y);
+            out[rb * ldo + x] = E::from(-v.y);
+            out[rb * ldo + m + x] = E::from(v.x);
+        }
+    }
+}
+
+void launch_gamma_hat(cudaStream_t st, bool ff, const double* gamma, int m, const int4* relk,
+                      const int4* relc, const int* itrmo, int i0, int nij, double* out) {
+    if (m > 65535) throw_dim("adjoint: NSP above 65535");
+    dim3 grid((unsigned)nij, (unsigned)m);
+    const int threads = m < 256 ? (m + 31) / 32 * 32 : 256;
+    if (ff)
+        k_gamma_hat<FFEl><<<grid, threads, 0, st>>>((const double2*)gamma, m, relk, relc, itrmo, i0,
+                                                     (float2*)out);
+    else
+        k_gamma_hat<F64El><<<grid, threads, 0, st>>>((const double2*)gamma, m, relk, relc, itrmo, i0,
+                                                      out);
+}
+
+// Fixed-order sum of split-K partial products into the FP64 accumulator.
+template <class E>
+__global__ void k_partial_sum(const typename E::T* __restrict__ part, int nb, long long len,
+                              double* __restrict__ acc) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+         i += (long long)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nb; ++b) s += E::val(part[(long long)b * len + i]);
+        acc[i] += s;
+    }
+}
+
+void launch_partial_sum(cudaStream_t st, bool ff, const double* part, int nb, long long len,
+                        double* acc) {
+    const unsigned g = (unsigned)std::min<long long>((len + 255) / 256, 152LL * 8);
+    if (ff)
+        k_partial_sum<FFEl><<<g, 256, 0, st>>>((const float2*)part, nb, len, acc);
+    else
+        k_partial_sum<F64El><<<g, 256, 0, st>>>(part, nb, len, acc);
 }
 
 }  // namespace rt

@@ -115,4 +115,15 @@ void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, in
                  const EmitRec* rec, int nrec, const int* kra, const int* krb, const int* itrmo,
                  double throut, const OutStreams& os);
 
+// ---- adjoint (dE/dC) ----
+// Gamma <- (Gamma + Gamma^T) / 2 with Gamma seen as an m^2 x m^2 complex
+// matrix over (first pair, second pair): the pair-exchange symmetrisation.
+void launch_gamma_sym(cudaStream_t st, double* gamma, int m);
+// Contraction operand of one item chunk, real-ified (see k_gamma_hat).
+void launch_gamma_hat(cudaStream_t st, bool ff, const double* gamma, int m, const int4* relk,
+                      const int4* relc, const int* itrmo, int i0, int nij, double* out);
+// acc[i] += sum_b part[b * len + i] (FP64 or float-float partials)
+void launch_partial_sum(cudaStream_t st, bool ff, const double* part, int nb, long long len,
+                        double* acc);
+
 }  // namespace rt

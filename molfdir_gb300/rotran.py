@@ -72,7 +72,7 @@ EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_add_ao_records_bulk", "rt_read_srt_files", "rt_clear_ao_records",
            "rt_transform", "rt_result_sizes", "rt_copy_result", "rt_write_mdcint",
            "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm",
-           "rt_split_dgemm_noalloc"]
+           "rt_split_dgemm_noalloc", "rt_adjoint"]
 
 _lib = None
 
@@ -112,6 +112,7 @@ def load(build: bool = True):
     lib.rt_split_dgemm.argtypes = [C.c_int, C.c_int, C.c_int, P(C.c_double), P(C.c_double),
                                    P(C.c_double), C.c_int, C.c_int]
     lib.rt_split_dgemm_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]
+    lib.rt_adjoint.argtypes = [vp, vp, vp, P(C.c_double)]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy"):
@@ -289,6 +290,25 @@ class Rotran:
     def write_mdcint(self, path, datex="", timex=""):
         self._check(self.lib.rt_write_mdcint(self.h, os.fsencode(path), datex.encode()[:10],
                                              timex.encode()[:8]))
+
+    def adjoint(self, gamma):
+        """dE/dC and E for E = sum gamma[i,j,k,l] (ij|kl) (``rt_adjoint``).
+
+        ``gamma``: complex (m, m, m, m) numpy array indexed [i, j, k, l], or
+        the device address of an NSP^4 COMPLEX*16 array in Fortran order.
+        Returns (dEdC as a complex (n, m) array, E)."""
+        n, m = self.cfg.nsc, self.cfg.nsp
+        if isinstance(gamma, np.ndarray):
+            g = np.asfortranarray(gamma, dtype=np.complex128)
+            assert g.shape == (m, m, m, m)
+            gp = g.ctypes.data
+        else:
+            g, gp = None, int(gamma)
+        out = np.empty((m, n), dtype=np.complex128)  # Fortran (n, m)
+        e = C.c_double()
+        self._check(self.lib.rt_adjoint(self.h, C.c_void_p(gp), C.c_void_p(out.ctypes.data),
+                                         C.byref(e)))
+        return out.T.copy(), e.value
 
     def stats(self):
         s = RtStats()
