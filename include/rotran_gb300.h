@@ -142,8 +142,9 @@ int rt_transform(rt_ctx* ctx);
  * symmetric under pair exchange (ij)<->(kl) contributes.  The
  * half-transformed integrals are recomputed (without the THRGEN screen),
  * not taken from an earlier rt_transform.  Needs the context's records and
- * coefficients and precision RT_PREC_FP64; device memory: the density
- * (16 NSP^4 bytes) plus the arrays of rt_transform. */
+ * coefficients; runs in the context's precision (the split path puts the
+ * density contraction on the tensor cores as well).  Device memory: the
+ * density (16 NSP^4 bytes) plus the arrays of rt_transform. */
 int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double* energy);
 
 /* Sizes of the MDCINT record stream of the last transform (records without

@@ -1006,8 +1006,6 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     API_TRY
     if (!gamma || !dedc) throw Error(RT_ERR_USER, "rt_adjoint: null gamma or dEdC");
     if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
-    if (ctx->cfg.precision != RT_PREC_FP64)
-        throw Error(RT_ERR_USER, "rt_adjoint needs a context of precision RT_PREC_FP64");
     Plan& P = ctx->plan;
     cudaStream_t st = ctx->stream;
     const int n = P.n, m = P.m;
@@ -1035,6 +1033,10 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     double* d_acc = ps.alloc<double>((size_t)nacc);
     RT_CUDA(cudaMemsetAsync(d_acc, 0, nacc * sizeof(double), st));
     pass_setup(ps);
+    const bool split = ps.split;
+    const int s = split ? ctx->cfg.slices : 0;
+    auto gemm_begin = [&]() { if (!split) kt.begin(); };
+    auto gemm_end = [&](double fl) { if (!split) kt.end(fl, fl); };
     RT_CUDA(cudaEventRecord(ctx->ev[1], st));
     pass_bucketing(ps);
     RT_CUDA(cudaEventRecord(ctx->ev[2], st));
@@ -1043,45 +1045,92 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     RT_CUDA(cudaEventRecord(ctx->ev[3], st));
     // ---- per item chunk: X_{u,plane} = h_{u,plane} C, then
     //      S += sum_{u,plane} X_{u,plane} Ghat_{u,plane} (split-K over items) ----
-    const int G = 8;  // items per partial product
+    const int G = 8;  // items per partial product of the FP64 path
     const int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
-    const double per_item = 4.0 * n * m + 2.0 * ncmax * ncmax + 8.0 * m * m + 2.0 * n * m / G + 1.0;
-    int chunk = (int)std::min<double>(KK1, std::max(1.0, std::floor((double)ctx->ha_len / per_item)));
-    if (chunk > G) chunk -= chunk % G;
-    if ((double)chunk * per_item > (double)ctx->ha_len + 1e-9 * per_item)
-        throw Error(RT_ERR_DIM, "rt_adjoint: work arena too small for one item");
+    const double kpc = (double)((ncmax + 31) / 32 * 32);
+    // bytes per item of the chunk buffers, and per chunk
+    double per_item = 32.0 * n * m + 16.0 * ncmax * ncmax + 64.0 * m * m;
+    double fixed = 8.0 * nacc + 8192.0;
+    if (split) {
+        per_item += 4.0 * m / 1024.0 * 8.0 * nacc;                                  // partials
+        per_item += std::max(2.0 * s * n * 4.0 * m, 2.0 * s * 2.0 * ncmax * kpc);    // A slices
+        per_item += 2.0 * s * 2.0 * m * 4.0 * m + 8.0 * ncmax;                       // B slices, exps
+        per_item += 4.0 * m / 1024.0 * 4.0 * (n + 2.0 * m);                          // split exps
+        fixed += 2.0 * s * (n + 2.0 * m) * 64.0 + 8.0 * (n + 2 * m) + 8.0 * nacc + 2048.0;
+    } else {
+        per_item += 8.0 * nacc / G;
+    }
+    const double arena = 8.0 * (double)ctx->ha_len;
+    int chunk = (int)std::min<double>(KK1, std::floor((arena - fixed) / per_item));
+    if (!split && chunk > G) chunk -= chunk % G;
+    if (chunk < 1) throw Error(RT_ERR_DIM, "rt_adjoint: work arena too small for one item");
     for (int i0 = 0; i0 < KK1; i0 += chunk) {
         const int nij = std::min(chunk, KK1 - i0);
-        double* X = ctx->d_ha;
-        double* m3 = X + (size_t)4 * n * m * nij;
-        double* bh = m3 + (size_t)2 * ncmax * ncmax * nij;
-        double* part = bh + (size_t)8 * m * m * nij;
+        const long long Kx = 4LL * m * nij;
+        unsigned char* wp = (unsigned char*)ctx->d_ha;
+        auto carve = [&](double bytes) {
+            unsigned char* r = wp;
+            wp += ((size_t)std::ceil(bytes) + 255) & ~(size_t)255;
+            return r;
+        };
+        double* X = (double*)carve(8.0 * Kx * n);
+        double* m3 = (double*)carve(16.0 * ncmax * ncmax * nij);
+        double* bh = (double*)carve(64.0 * m * m * nij);
         for (int cc = 0; cc < 2; ++cc) {
             const int nc = P.ncomp[cc];
             if (nc == 0) continue;
             launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, m3);
             ++ps.launches;
-            EpiRowMajor ex{X + (size_t)P.comp_off[cc] * nij * 4 * m, 2LL * m, 0};
-            kt.begin();
-            gemm_f64(st, m3, nc, 0, ctx->d_qap + (long long)P.comp_off[cc] * 2 * m, 2 * m, 0,
-                     2 * nc * nij, 2 * m, nc, 1, ex);
-            kt.end(2.0 * (2.0 * nc * nij) * 2 * m * nc, 2.0 * (2.0 * nc * nij) * 2 * m * nc);
+            if (split) {
+                unsigned char* save = wp;
+                __nv_bfloat16* sl = (__nv_bfloat16*)carve(2.0 * s * 2.0 * nc * nij * kpc);
+                int* ex = (int*)carve(8.0 * nc * nij);
+                split_adj_x(ctx, cc, m3, nc, nij, X, sl, ex, &ps.launches);
+                wp = save;
+            } else {
+                EpiRowMajor ex{X + (size_t)P.comp_off[cc] * nij * 4 * m, 2LL * m, 0};
+                gemm_begin();
+                gemm_f64(st, m3, nc, 0, ctx->d_qap + (long long)P.comp_off[cc] * 2 * m, 2 * m, 0,
+                         2 * nc * nij, 2 * m, nc, 1, ex);
+                gemm_end(2.0 * (2.0 * nc * nij) * 2 * m * nc);
+                ++ps.launches;
+            }
+        }
+        if (split) {
+            const long long Kp = split_adj_kpad(Kx);
+            launch_gamma_hat_t(st, d_gam, m, d_relk, d_relc, ps.d_itrmo, i0, nij, Kx, bh);
+            ++ps.launches;
+            __nv_bfloat16* a_sl = (__nv_bfloat16*)carve(2.0 * s * n * Kp);
+            __nv_bfloat16* b_sl = (__nv_bfloat16*)carve(2.0 * s * 2.0 * m * Kp);
+            const double nsplit = (double)((Kp + 1023) / 1024);
+            int* a_ex = (int*)carve(4.0 * n * nsplit);
+            int* b_ex = (int*)carve(8.0 * m * nsplit);
+            double* part = (double*)carve(8.0 * nacc * ((Kp / 32 + 31) / 32));
+            if ((double)(wp - (unsigned char*)ctx->d_ha) > arena)
+                throw Error(RT_ERR_INTERNAL, "rt_adjoint: chunk buffers exceed the work arena");
+            const int ks = split_adj_contract(ctx, X, n, Kx, bh, a_sl, a_ex, b_sl, b_ex, part,
+                                              &ps.launches);
+            launch_partial_sum(st, true, part, ks, nacc, d_acc);
+            ++ps.launches;
+        } else {
+            launch_gamma_hat(st, false, d_gam, m, d_relk, d_relc, ps.d_itrmo, i0, nij, bh);
+            ++ps.launches;
+            const int nb = nij / G, rem = nij - nb * G;
+            double* part = (double*)carve(8.0 * nacc * (nb + 1));
+            if ((double)(wp - (unsigned char*)ctx->d_ha) > arena)
+                throw Error(RT_ERR_INTERNAL, "rt_adjoint: chunk buffers exceed the work arena");
+            const long long K1 = 4LL * m * G;
+            gemm_begin();
+            if (nb)
+                gemm_f64(st, X, Kx, K1, bh, 2 * m, K1 * 2 * m, n, 2 * m, (int)K1, nb,
+                         EpiRowMajor{part, 2LL * m, nacc}), ++ps.launches;
+            if (rem)
+                gemm_f64(st, X + nb * K1, Kx, 0, bh + (size_t)nb * K1 * 2 * m, 2 * m, 0, n, 2 * m,
+                         4 * m * rem, 1, EpiRowMajor{part + (size_t)nb * nacc, 2LL * m, 0}), ++ps.launches;
+            gemm_end(2.0 * n * 2 * m * (double)Kx);
+            launch_partial_sum(st, false, part, nb + (rem > 0 ? 1 : 0), nacc, d_acc);
             ++ps.launches;
         }
-        launch_gamma_hat(st, false, d_gam, m, d_relk, d_relc, ps.d_itrmo, i0, nij, bh);
-        ++ps.launches;
-        const int nb = nij / G, rem = nij - nb * G;
-        const long long K1 = 4LL * m * G, lda = 4LL * m * nij;
-        kt.begin();
-        if (nb)
-            gemm_f64(st, X, lda, K1, bh, 2 * m, K1 * 2 * m, n, 2 * m, (int)K1, nb,
-                     EpiRowMajor{part, 2LL * m, nacc}), ++ps.launches;
-        if (rem)
-            gemm_f64(st, X + nb * K1, lda, 0, bh + (size_t)nb * K1 * 2 * m, 2 * m, 0, n, 2 * m,
-                     4 * m * rem, 1, EpiRowMajor{part + (size_t)nb * nacc, 2LL * m, 0}), ++ps.launches;
-        kt.end(2.0 * n * 2 * m * 4.0 * m * nij, 2.0 * n * 2 * m * 4.0 * m * nij);
-        launch_partial_sum(st, false, part, nb + (rem > 0 ? 1 : 0), nacc, d_acc);
-        ++ps.launches;
     }
     RT_CUDA(cudaGetLastError());
     RT_CUDA(cudaEventRecord(ctx->ev[4], st));
@@ -1089,6 +1138,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     RT_CUDA(cudaMemcpyAsync(acc.data(), d_acc, nacc * sizeof(double), cudaMemcpyDeviceToHost, st));
     RT_CUDA(cudaEventRecord(ctx->ev[5], st));
     RT_CUDA(cudaStreamSynchronize(st));
+    if (split) split_check(ctx);
     // dE/dRe C + i dE/dIm C = 4 S (rows back in the caller's AO order);
     // E = sum conj(C) S (E is of degree 2 in conj(C))
     std::vector<double> out((size_t)2 * n * m);

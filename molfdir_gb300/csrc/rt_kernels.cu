@@ -698,6 +698,60 @@ void launch_gamma_hat(cudaStream_t st, bool ff, const double* gamma, int m, cons
                                                       out);
 }
 
+// The same operand transposed, as float-float rows (ri_out*m + x) of length
+// ldk over the K index ((ij*2 + plane)*2 + ri)*m + y (the K-major layout
+// the tensor-core path slices); one block per (ij, x), threads over y.
+__global__ void k_gamma_hat_t(const double2* __restrict__ gs, int m, const int4* __restrict__ relk,
+                              const int4* __restrict__ relc, const int* __restrict__ itrmo, int i0,
+                              long long ldk, float2* __restrict__ out) {
+    const int ij = blockIdx.x, x = blockIdx.y;
+    const int it = i0 + ij;
+    const int4 rk = relk[it], rc = relc[it];
+    const int kr[4] = {rk.x, rk.y, rk.z, rk.w}, cr[4] = {rc.x, rc.y, rc.z, rc.w};
+    const int tx_ = itrmo[x];
+    const int xb = abs(tx_) - 1;
+    const long long M2 = (long long)m * m;
+    for (int y = threadIdx.x; y < m; y += blockDim.x) {
+        const int ty_ = itrmo[y];
+        const int yb = abs(ty_) - 1;
+        const double sg = ((ty_ > 0) == (tx_ > 0)) ? 1.0 : -1.0;
+        double2 vr = make_double2(0.0, 0.0), vi = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if (kr[r] < 0) continue;
+            const long long base = (long long)kr[r] * M2;
+            const double2 g1 = gs[base + x + (long long)m * y];
+            const double2 g2 = gs[base + yb + (long long)m * xb];
+            const double tr = g1.x + sg * g2.x, ti = g1.y + sg * g2.y;
+            const double s = cr[r] > 0 ? 1.0 : -1.0;
+            const double si = (cr[r] == 2 || cr[r] == -2) ? -s : s;
+            vr.x += s * tr;
+            vr.y += s * ti;
+            vi.x -= si * ti;
+            vi.y += si * tr;
+        }
+#pragma unroll
+        for (int pl = 0; pl < 2; ++pl) {
+            const double2 v = pl ? vi : vr;
+            const long long ka = ((long long)(ij * 2 + pl) * 2) * m + y, kb = ka + m;
+            out[(long long)x * ldk + ka] = FFEl::from(v.x);        // (ri 0, re out)
+            out[(long long)(m + x) * ldk + ka] = FFEl::from(v.y);  // (ri 0, im out)
+            out[(long long)x * ldk + kb] = FFEl::from(-v.y);       // (ri 1, re out)
+            out[(long long)(m + x) * ldk + kb] = FFEl::from(v.x);  // (ri 1, im out)
+        }
+    }
+}
+
+void launch_gamma_hat_t(cudaStream_t st, const double* gamma, int m, const int4* relk,
+                        const int4* relc, const int* itrmo, int i0, int nij, long long ldk,
+                        double* out) {
+    if (m > 65535) throw_dim("adjoint: NSP above 65535");
+    dim3 grid((unsigned)nij, (unsigned)m);
+    const int threads = m < 256 ? (m + 31) / 32 * 32 : 256;
+    k_gamma_hat_t<<<grid, threads, 0, st>>>((const double2*)gamma, m, relk, relc, itrmo, i0, ldk,
+                                            (float2*)out);
+}
+
 // Fixed-order sum of split-K partial products into the FP64 accumulator.
 template <class E>
 __global__ void k_partial_sum(const typename E::T* __restrict__ part, int nb, long long len,

@@ -122,6 +122,10 @@ void launch_gamma_sym(cudaStream_t st, double* gamma, int m);
 // Contraction operand of one item chunk, real-ified (see k_gamma_hat).
 void launch_gamma_hat(cudaStream_t st, bool ff, const double* gamma, int m, const int4* relk,
                       const int4* relc, const int* itrmo, int i0, int nij, double* out);
+// The same operand transposed to float-float rows of length ldk (split path).
+void launch_gamma_hat_t(cudaStream_t st, const double* gamma, int m, const int4* relk,
+                        const int4* relc, const int* itrmo, int i0, int nij, long long ldk,
+                        double* out);
 // acc[i] += sum_b part[b * len + i] (FP64 or float-float partials)
 void launch_partial_sum(cudaStream_t st, bool ff, const double* part, int nb, long long len,
                         double* acc);

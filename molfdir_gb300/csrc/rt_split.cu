@@ -244,6 +244,10 @@ struct SplitArgs {
     long long M, N;
     int Kp, s;
     int tiles_m, tiles_n;
+    // split-K: K block range [ks*kcb, (ks+1)*kcb) of split ks < ksplit, with
+    // its own scales row_exp[ks*M + row], col_exp[ks*N + col]; the epilogue
+    // writes split ks as rows ks*M + row (ksplit = 1: plain GEMM)
+    int ksplit, kcb;
     const int* row_exp;
     const int* col_exp;
     int* error;
@@ -269,7 +273,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const uint32_t stage_bytes = (uint32_t)s * (slice_a + slice_b);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nkb = g.Kp / SBK;
-    const long long ntiles = (long long)g.tiles_m * g.tiles_n;
+    const long long ntiles = (long long)g.tiles_m * g.tiles_n * g.ksplit;
     if (threadIdx.x == 0) {
         for (int i = 0; i < NSTAGE; ++i) {
             mbar_init(&full[i], 1);
@@ -291,8 +295,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         if (lane == 0) {  // ---- TMA producer ----
             long long gk = 0;
             for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x) {
-                const long long tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
-                for (int kb = 0; kb < nkb; ++kb, ++gk) {
+                const long long tmn = tile / g.ksplit;
+                const int kb0 = (int)(tile - tmn * g.ksplit) * g.kcb, kb1 = min(nkb, kb0 + g.kcb);
+                const long long tm = tmn / g.tiles_n, tn = tmn - tm * g.tiles_n;
+                for (int kb = kb0; kb < kb1; ++kb, ++gk) {
                     const int st = (int)(gk % NSTAGE);
                     const uint32_t ph = (uint32_t)((gk / NSTAGE) & 1);
                     if (!mbar_wait_bounded(&empty[st], ph ^ 1u, &abort_flag, WAIT_NS)) {
@@ -325,7 +331,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 }
                 tc_fence_after();
                 bool started[4] = {false, false, false, false};
-                for (int kb = 0; kb < nkb; ++kb, ++gk) {
+                const int kb0 = (int)(tile % g.ksplit) * g.kcb, kb1 = min(nkb, kb0 + g.kcb);
+                for (int kb = kb0; kb < kb1; ++kb, ++gk) {
                     const int st = (int)(gk % NSTAGE);
                     const uint32_t ph = (uint32_t)((gk / NSTAGE) & 1);
                     if (!mbar_wait_bounded(&full[st], ph, &abort_flag, WAIT_NS)) {
@@ -363,14 +370,15 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
         int it = 0;
         for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x, ++it) {
-            const long long tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
+            const long long tmn = tile / g.ksplit, ks = tile - tmn * g.ksplit;
+            const long long tm = tmn / g.tiles_n, tn = tmn - tm * g.tiles_n;
             // column scale factors of this warp's half tile (warp-local: no
             // barrier another role could leave waiting)
             float* fcol = fcol_w[ew];
             __syncwarp();
             for (int j = lane; j < SBN / 2; j += 32) {
                 const long long col = tn * SBN + chalf * (SBN / 2) + j;
-                const int e = col < g.N ? g.col_exp[col] : -2000;
+                const int e = col < g.N ? g.col_exp[ks * g.N + col] : -2000;
                 fcol[j] = e < -1000 ? 0.0f : pow2f_safe(e);
             }
             __syncwarp();
@@ -381,9 +389,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             }
             tc_fence_after();
             const long long row = tm * SBM + lg * 32 + lane;
-            const int erow = row < g.M ? g.row_exp[row] : -2000;
+            const int erow = row < g.M ? g.row_exp[ks * g.M + row] : -2000;
             const float frow = erow < -1000 ? 0.0f : pow2f_safe(erow - 28);
-            const typename Epi::Row er = epi.row(row < g.M ? row : 0);
+            const typename Epi::Row er = epi.row(ks * g.M + (row < g.M ? row : 0));
             for (int c0 = chalf * (SBN / 2); c0 < (chalf + 1) * (SBN / 2); c0 += EC) {
                 uint32_t r0[EC], r1[EC], r2[EC], r3[EC];
                 tmem_ld16(tmem + lane_base + (uint32_t)c0, r0);
@@ -523,6 +531,7 @@ struct SplitState {
     ConstSlices qah;                 // A of GEMM2/4: rows 2m, K = 2n
     std::vector<ConstSlices> qap;    // B of GEMM1 per AO block: N = 2m, K = block size
     ConstSlices qar[2];              // B of GEMM3 per component: N = 2m, K = 2nc
+    ConstSlices qc[2];               // B of the adjoint's X GEMM per component: N = 2m, K = nc
     // work buffers
     __nv_bfloat16* a_sl = nullptr;
     int* a_exp = nullptr;
@@ -659,6 +668,15 @@ void split_prepare_constants(rt_ctx* c) {
             }
         host_slice_cols(bm.data(), 2 * nc, 2 * m, 2 * m, kpad(2 * nc), s, sl, ex);
         upload_const(S, S->qar[comp], sl, ex, 2 * m, 2 * nc);
+        // [QAr | QAi] of the component (adjoint)
+        std::vector<double> bc((size_t)nc * 2 * m);
+        for (int q = 0; q < nc; ++q)
+            for (int j = 0; j < m; ++j) {
+                bc[(size_t)q * 2 * m + j] = qr[(size_t)(off + q) * m + j];
+                bc[(size_t)q * 2 * m + m + j] = qi[(size_t)(off + q) * m + j];
+            }
+        host_slice_cols(bc.data(), nc, 2 * m, 2 * m, kpad(nc), s, sl, ex);
+        upload_const(S, S->qc[comp], sl, ex, 2 * m, nc);
     }
 }
 
@@ -723,7 +741,8 @@ static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int
 
 template <class Epi>
 static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M, const void* b_sl,
-                     const int* b_exp, long long N, int K, int Kp, Epi epi, int* launches) {
+                     const int* b_exp, long long N, int K, int Kp, Epi epi, int* launches,
+                     int ksplit = 1, int kcb = 0) {
     SplitState* S = state(c);
     if (M <= 0 || N <= 0) return;
     const int s = S->s;
@@ -736,10 +755,18 @@ static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M,
     g.s = s;
     g.tiles_m = (int)((M + SBM - 1) / SBM);
     g.tiles_n = (int)((N + SBN - 1) / SBN);
+    g.ksplit = ksplit;
+    g.kcb = ksplit > 1 ? kcb : Kp / SBK;
+    if (ksplit > 1) {  // every split non-empty, at most 1024 deep, all of K covered
+        const long long nkb = Kp / SBK;
+        if (kcb < 1 || kcb * SBK > 1024 || (long long)(ksplit - 1) * kcb >= nkb ||
+            (long long)ksplit * kcb < nkb)
+            throw Error(RT_ERR_INTERNAL, "inconsistent split-K layout");
+    }
     g.row_exp = a_exp;
     g.col_exp = b_exp;
     g.error = S->d_err;
-    const long long ntiles = (long long)g.tiles_m * g.tiles_n;
+    const long long ntiles = (long long)g.tiles_m * g.tiles_n * g.ksplit;
     const int grid = (int)std::min<long long>(ntiles, S->num_sms);
     const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
     c->ktimer.begin();
@@ -800,6 +827,111 @@ void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const E
     const ConstSlices& B = S->qar[comp];
     EpiFF_RK epi{(float2*)e.rk, e.m, e.rowoff, e.plane};
     run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * c->plan.m, K, Kp, epi, launches);
+}
+
+// ---------------------------------------------------------------------------
+// long rows (operands of the adjoint contraction, K up to ~10^8): exponents
+// by a block-parallel maximum, then the digits elementwise
+// ---------------------------------------------------------------------------
+constexpr int LONG_BLOCK = 1024;  // K per split of the contraction = per exponent
+
+// exps[kb * rows + row] = exponent of row's K block kb (LONG_BLOCK deep)
+__global__ void __launch_bounds__(256) k_rowexp_long(const float2* __restrict__ src, long long ld,
+                                                     int rows, long long K, int* __restrict__ exps) {
+    __shared__ int wmax[8];
+    const int row = blockIdx.y, kb = blockIdx.x;
+    const long long k0 = (long long)kb * LONG_BLOCK;
+    const long long k1 = min(K, k0 + LONG_BLOCK);
+    int S = -2000;
+    for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x)
+        S = max(S, scale_exp_f32(src[(long long)row * ld + k].x));
+    for (int o = 16; o; o >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = S;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; ++w) S = max(S, wmax[w]);
+        exps[(long long)kb * rows + row] = S;
+    }
+}
+
+// digits of row's K block blockIdx.x (256 threads x 4 consecutive k)
+template <int NS>
+__global__ void __launch_bounds__(256) k_slice_rows_long(const float2* __restrict__ src, long long ld,
+                                                         int rows, long long K, long long Kp,
+                                                         const int* __restrict__ exps,
+                                                         __nv_bfloat16* __restrict__ out) {
+    const int row = blockIdx.y;
+    const long long k0 = (long long)blockIdx.x * LONG_BLOCK + threadIdx.x * 4;
+    if (k0 >= Kp) return;
+    const int S = exps[(long long)blockIdx.x * rows + row];
+    const float sc = pow2f_safe(-S);
+    __nv_bfloat16 d[4][NS];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float2 v = make_float2(0.f, 0.f);
+        if (k0 + j < K && S > -1000) v = src[(long long)row * ld + k0 + j];
+        ff_digits<NS>(v.x * sc, v.y * sc, d[j]);
+    }
+#pragma unroll
+    for (int t = 0; t < NS; ++t) {
+        uint2 w = make_uint2(pack_bf16x2(d[0][t], d[1][t]), pack_bf16x2(d[2][t], d[3][t]));
+        *reinterpret_cast<uint2*>(out + ((long long)t * rows + row) * Kp + k0) = w;
+    }
+}
+
+// slices [s][rows][Kp] and exponents [Kp/LONG_BLOCK][rows] of long rows
+static void slice_long_rows(int s, const float2* src, long long ld, int rows, long long K,
+                            long long Kp, int* exps, __nv_bfloat16* out, cudaStream_t st) {
+    if (rows > 65535) throw Error(RT_ERR_DIM, "long-row slicing: more than 65535 rows");
+    dim3 g((unsigned)((Kp + LONG_BLOCK - 1) / LONG_BLOCK), (unsigned)rows);
+    k_rowexp_long<<<g, 256, 0, st>>>(src, ld, rows, K, exps);
+    switch (s) {
+        case 2: k_slice_rows_long<2><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        case 3: k_slice_rows_long<3><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        case 4: k_slice_rows_long<4><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        case 5: k_slice_rows_long<5><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        default: k_slice_rows_long<6><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+    }
+}
+
+// Adjoint X GEMM of one component: rows (p, ij, plane) of the float-float
+// M3 times [QAr | QAi] of the component, into X[a][ij][plane][ri][k].
+void split_adj_x(rt_ctx* c, int comp, const double* m3, int nc, int nij, double* x,
+                 __nv_bfloat16* sl, int* ex, int* launches) {
+    SplitState* S = state(c);
+    const int m = c->plan.m, Kp = kpad(nc);
+    const long long M = 2LL * nc * nij;
+    launch_slice_rows(S->s, RowsFF{(const float2*)m3, (long long)nc}, M, nc, Kp, sl, ex, c->stream);
+    ++*launches;
+    const ConstSlices& B = S->qc[comp];
+    EpiFF_RowMajor epi{(float2*)(x + (size_t)c->plan.comp_off[comp] * nij * 4 * m), 2LL * m};
+    run_gemm(c, sl, ex, M, B.d, B.exps, 2LL * m, nc, Kp, epi, launches);
+}
+
+long long split_adj_kpad(long long K) { return (K + SBK - 1) / SBK * SBK; }
+
+// Adjoint contraction part[ks][a][col] = sum over split ks of X(a,k) Ghat(k,col)
+// with Ghat given transposed (rows col, length Kx); every 1024-deep split
+// has its own row and column scales (a_ex: [ks][rows], b_ex: [ks][2m]).
+// Returns the split count.
+int split_adj_contract(rt_ctx* c, const double* x, int rows, long long Kx, const double* ghat_t,
+                       __nv_bfloat16* a_sl, int* a_ex, __nv_bfloat16* b_sl, int* b_ex, double* part,
+                       int* launches) {
+    SplitState* S = state(c);
+    const int m2 = 2 * c->plan.m;
+    const long long Kp = split_adj_kpad(Kx);
+    if (Kp > (1LL << 30)) throw Error(RT_ERR_DIM, "adjoint contraction: K above 2^30");
+    slice_long_rows(S->s, (const float2*)x, Kx, rows, Kx, Kp, a_ex, a_sl, c->stream);
+    slice_long_rows(S->s, (const float2*)ghat_t, Kx, m2, Kx, Kp, b_ex, b_sl, c->stream);
+    *launches += 4;
+    RT_CUDA(cudaGetLastError());
+    // one split per exponent block; K <= 1024 per split keeps the FP32 sums exact
+    const int kcb = LONG_BLOCK / SBK;
+    const int nkb = (int)(Kp / SBK);
+    const int ksplit = (nkb + kcb - 1) / kcb;
+    run_gemm(c, a_sl, a_ex, rows, b_sl, b_ex, m2, (int)Kx, (int)Kp,
+             EpiFF_RowMajor{(float2*)part, (long long)m2}, launches, ksplit, kcb);
+    return ksplit;
 }
 
 void split_release(rt_ctx* c) {
@@ -1024,6 +1156,8 @@ extern "C" int rt_split_dgemm_noalloc(int M, int N, int K, const double* A, cons
         g.s = s;
         g.tiles_m = (M + SBM - 1) / SBM;
         g.tiles_n = (N + SBN - 1) / SBN;
+        g.ksplit = 1;
+        g.kcb = Kp / SBK;
         g.row_exp = ea;
         g.col_exp = eb;
         g.error = err;

@@ -20,6 +20,13 @@ void split_gemm24(rt_ctx* c, const double* B, int K, long long N, const EpiRowMa
 void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& epi,
                  int* launches);
 void split_release(rt_ctx* c);
+// adjoint: X GEMM of one component and the split-K contraction
+void split_adj_x(rt_ctx* c, int comp, const double* m3, int nc, int nij, double* x,
+                 __nv_bfloat16* sl, int* ex, int* launches);
+long long split_adj_kpad(long long K);
+int split_adj_contract(rt_ctx* c, const double* x, int rows, long long Kx, const double* ghat_t,
+                       __nv_bfloat16* a_sl, int* a_ex, __nv_bfloat16* b_sl, int* b_ex, double* part,
+                       int* launches);
 // executed FLOPs per algorithmic FLOP of a split GEMM (slice products)
 double split_flop_factor(rt_ctx* c);
 // raise if a split GEMM gave up waiting (bounded-wait timeout)
