@@ -147,6 +147,36 @@ int rt_transform(rt_ctx* ctx);
  * density (16 NSP^4 bytes) plus the arrays of rt_transform. */
 int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double* energy);
 
+/* Batched transforms (no counterpart in the reference, which runs one
+ * transformation per process).  rt_batch_create plans every context as a
+ * single chunk (all pair groups and Kramers items resident at once; fails
+ * with RT_ERR_DIM when they do not all fit) and builds one grouped GEMM per
+ * stage over all contexts.  rt_batch_run runs the transforms; its first call
+ * times every grouped GEMM with 128- and 64-wide output tiles, keeps the
+ * faster, and captures the whole sequence as a CUDA graph that later calls
+ * replay.  The results are then read per context with rt_result_sizes /
+ * rt_copy_result / rt_write_mdcint.  All contexts: same device, precision
+ * RT_PREC_SPLIT_BF16, coefficients and records set before rt_batch_create
+ * and left unchanged while the batch lives (RT_ERR_MISMATCH otherwise). */
+typedef struct rt_batch rt_batch;
+typedef struct rt_batch_stats {
+    int instances;
+    int grouped_launches;  /* persistent grouped GEMM launches per run */
+    int kernel_launches;   /* all kernels of one run */
+    int graph_nodes;       /* nodes of the captured graph */
+    int tile128, tile64;   /* grouped launches tuned to 128- / 64-wide tiles */
+    double ms_last;        /* device time of the last run (graph launch) */
+    double ms_tune;        /* device time of the two tuning runs */
+    double flops_algorithmic;   /* summed algorithmic FLOPs of the transforms */
+    double flops_gemm_executed; /* tensor FLOPs of the grouped GEMMs per run */
+} rt_batch_stats;
+int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count);
+int rt_batch_run(rt_batch* b);
+int rt_batch_get_stats(rt_batch* b, rt_batch_stats* out);
+/* message of the last failed rt_batch_run (rt_batch_create: rt_last_error(NULL)) */
+const char* rt_batch_last_error(rt_batch* b);
+void rt_batch_destroy(rt_batch* b);
+
 /* Sizes of the MDCINT record stream of the last transform (records without
  * header and terminator; nz = total elements). */
 int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz);

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <numeric>
 #include <string>
@@ -447,6 +448,7 @@ extern "C" int rt_set_coefficients(rt_ctx* ctx, const double* qa, int ld_qa, con
     build_coef_device(ctx);
     RT_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->have_coef = true;
+    ++ctx->gen;
     API_CATCH
 }
 
@@ -507,6 +509,7 @@ extern "C" int rt_add_ao_records(rt_ctx* ctx, int file_class, int nt, int itype,
     ctx->st_l1.insert(ctx->st_l1.end(), label1, label1 + nt);
     if (ctx->st_v.size() >= (size_t)(8 << 20)) flush_staged(ctx);
     ctx->transformed = false;
+    ++ctx->gen;
     API_CATCH
 }
 
@@ -537,6 +540,7 @@ extern "C" int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* fi
     }
     ctx->n_int += tot;
     ctx->transformed = false;
+    ++ctx->gen;
     API_CATCH
 }
 
@@ -552,6 +556,7 @@ extern "C" int rt_clear_ao_records(rt_ctx* ctx) {
     ctx->rec_nt.clear();
     ctx->rec_off.clear();
     ctx->transformed = false;
+    ++ctx->gen;
     API_CATCH
 }
 
@@ -560,7 +565,7 @@ extern "C" int rt_clear_ao_records(rt_ctx* ctx) {
 // ---------------------------------------------------------------------------
 namespace {
 
-void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk) {
+void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = false) {
     Plan& P = c->plan;
     Work& w = W(c);
     const int n = P.n, m = P.m;
@@ -611,6 +616,12 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk) {
     item_chunk = (int)std::min<long long>(KK1, std::max(1LL, (long long)(usable / per_item)));
     pair_chunk = std::min(pair_chunk, 16384);
     item_chunk = std::min(item_chunk, 16384);
+    if (exact) {  // one chunk per pair group and one item chunk (batched transforms)
+        pair_chunk = maxpg;
+        item_chunk = (int)std::max(1LL, KK1);
+        if ((double)usable < per_pair * pair_chunk || (double)usable < per_item * item_chunk)
+            throw Error(RT_ERR_DIM, "device memory too small for a single-chunk (batched) transform");
+    }
     if (usable < per_pair || usable < per_item)
         throw Error(RT_ERR_DIM, "device memory budget too small for one pair / one item");
     size_t need_a = (size_t)((per_pair - (S ? split_stageA_bytes_per_pair(c) : 0)) * pair_chunk / 8) + 64;
@@ -706,14 +717,14 @@ struct Pass {
 };
 
 // Work arena, tables, item and Kramers tables on the device.
-void pass_setup(Pass& ps) {
+void pass_setup(Pass& ps, bool exact = false) {
     rt_ctx* ctx = ps.c;
     Plan& P = ctx->plan;
     Work& w = W(ctx);
     const int m = P.m, K = P.K;
     const int KK1 = (int)P.items.size();
     ps.split = ctx->cfg.precision == RT_PREC_SPLIT_BF16;
-    ensure_fixed(ctx, ps.pair_chunk, ps.item_chunk);
+    ensure_fixed(ctx, ps.pair_chunk, ps.item_chunk, exact);
     upload_tables(ctx, ps.T, ps.tmp);
     std::vector<int2> meta(ctx->rec_off.size());
     for (size_t r = 0; r < meta.size(); ++r) meta[r] = make_int2(ctx->rec_file[r], ctx->rec_it[r]);
@@ -1177,6 +1188,410 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     S.flops_gemm_executed = kt.flops;
     S.flops_gemm_algorithmic = kt.alg;
     API_CATCH
+}
+
+// ---------------------------------------------------------------------------
+// batched transforms: many contexts, each planned as a single chunk, run
+// stage by stage with one persistent grouped launch per GEMM stage, the
+// whole sequence captured once as a CUDA graph and replayed
+// ---------------------------------------------------------------------------
+namespace {
+
+struct BatchInst {
+    rt_ctx* c = nullptr;
+    std::unique_ptr<Pass> ps;
+    unsigned long long gen = 0;
+    long long* d_total = nullptr;
+    long long* d_off[4] = {nullptr, nullptr, nullptr, nullptr};
+    EmitRec* d_recs = nullptr;
+    int nrecs = 0;
+    std::vector<ExpandJob*> d_jobs;
+    std::vector<size_t> jobs_smem;
+    std::vector<int> covered;
+    OutStreams os{};
+};
+
+}  // namespace
+
+struct rt_batch {
+    std::vector<BatchInst> inst;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    int* d_err = nullptr;
+    std::vector<SplitGroup*> g1, g2;  // per pair-group stage
+    SplitGroup* g3[2] = {nullptr, nullptr};
+    SplitGroup* g4 = nullptr;
+    std::vector<SplitGroup*> all;     // enqueue order
+    std::vector<int> bn;              // tile width per group of `all`
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> gev;     // around each grouped launch (tuning)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool tuned = false;
+    int launches = 0;
+    rt_batch_stats stats{};
+    std::string err;
+    ~rt_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (SplitGroup* g : all) split_group_free(g);
+        for (auto e : ev) if (e) cudaEventDestroy(e);
+        for (auto e : gev) cudaEventDestroy(e);
+        if (d_err) cudaFree(d_err);
+        inst.clear();
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace {
+
+// All kernels of one batched run on b->st (no host synchronisation, so the
+// sequence can be captured); with `timed`, events around each grouped launch.
+void batch_enqueue(rt_batch* b, bool timed) {
+    cudaStream_t st = b->st;
+    int& L = b->launches;
+    L = 0;
+    size_t gi = 0;
+    auto group = [&](SplitGroup* g) {
+        if (!g || split_group_size(g) == 0) { ++gi; return; }
+        if (timed) RT_CUDA(cudaEventRecord(b->gev[2 * gi], st));
+        split_group_launch(g, b->bn[gi], st, b->d_err);
+        if (timed) RT_CUDA(cudaEventRecord(b->gev[2 * gi + 1], st));
+        ++L;
+        ++gi;
+    };
+    for (BatchInst& I : b->inst) {
+        RT_CUDA(cudaMemsetAsync(I.d_total, 0, 4 * sizeof(long long), st));
+        RT_CUDA(cudaMemsetAsync(I.ps->d_stat, 0, 8 * sizeof(unsigned long long), st));
+    }
+    // ---- bucketing ----
+    for (BatchInst& I : b->inst) {
+        rt_ctx* c = I.c;
+        const Plan& P = c->plan;
+        const DeviceTabs& T = I.ps->T;
+        ScatterTabs tb{P.n, c->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
+                       T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk};
+        launch_bucket(st, c->d_rint, c->d_l2, c->d_l1, c->n_int, I.ps->d_roff, I.ps->d_rmeta,
+                      (int)c->rec_off.size(), tb, P.P, c->d_bcount, c->d_boff, c->d_bval, c->d_brs,
+                      (unsigned int*)I.ps->d_stat);
+        L += c->n_int > 0 ? 3 : 1;
+    }
+    // ---- first half, pair-group stage by stage ----
+    for (size_t g = 0; g < b->g1.size(); ++g) {
+        for (BatchInst& I : b->inst) {
+            rt_ctx* c = I.c;
+            const Plan& P = c->plan;
+            if (g >= P.pgroups.size()) continue;
+            const int n = P.n, m = P.m, npc = P.pgroups[g].size;
+            if (I.covered[g] < n)
+                RT_CUDA(cudaMemsetAsync(c->d_ha, 0, (size_t)2 * n * m * npc * sizeof(double), st));
+            if (!P.pg_jobs[g].empty()) {
+                launch_expand_rows(st, c->cfg.slices, c->d_bval, c->d_brs, c->d_boff, I.d_jobs[g],
+                                   (int)P.pg_jobs[g].size(), P.pgroups[g].start, npc, I.ps->T.ao_block,
+                                   I.ps->T.ao_pos, I.jobs_smem[g], nullptr, split_a1_slices(c),
+                                   split_a1_exps(c));
+                ++L;
+            }
+        }
+        group(b->g1[g]);
+        for (BatchInst& I : b->inst) {
+            rt_ctx* c = I.c;
+            const Plan& P = c->plan;
+            if (g >= P.pgroups.size()) continue;
+            split_prep_gemm24(c, c->d_ha, 2 * P.n, (long long)P.m * P.pgroups[g].size, st, &L);
+        }
+        group(b->g2[g]);
+        for (BatchInst& I : b->inst) {
+            rt_ctx* c = I.c;
+            const Plan& P = c->plan;
+            if (g >= P.pgroups.size()) continue;
+            const int n = P.n, m = P.m, npc = P.pgroups[g].size;
+            const int KK1 = (int)P.items.size();
+            double* ri = c->d_ha + (size_t)2 * n * m * I.ps->pair_chunk;
+            launch_tr_select(st, true, ri, m, npc, P.pgroups[g].start, P.P, I.ps->d_items,
+                             I.ps->d_isign, KK1, I.ps->d_pvmx, c->cfg.thrgen, c->d_hp, I.ps->d_stat + 1);
+            L += (KK1 + 65534) / 65535;
+        }
+    }
+    // ---- second half ----
+    for (int cc = 0; cc < 2; ++cc) {
+        for (BatchInst& I : b->inst) {
+            rt_ctx* c = I.c;
+            const Plan& P = c->plan;
+            const int nc = P.ncomp[cc], KK1 = (int)P.items.size();
+            if (nc == 0) continue;
+            launch_expand(st, c->d_hp, P.P, KK1, 0, KK1, I.ps->d_pidx[cc], nc, c->d_ha);
+            ++L;
+            split_prep_gemm3(c, c->d_ha, nc, KK1, st, &L);
+        }
+        group(b->g3[cc]);
+    }
+    for (BatchInst& I : b->inst) {
+        rt_ctx* c = I.c;
+        const Plan& P = c->plan;
+        const int n = P.n, m = P.m, KK1 = (int)P.items.size();
+        const int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+        double* rk = c->d_ha + (size_t)2 * ncmax * ncmax * I.ps->item_chunk;
+        split_prep_gemm24(c, rk, 2 * n, (long long)KK1 * m, st, &L);
+    }
+    group(b->g4);
+    for (BatchInst& I : b->inst) {
+        rt_ctx* c = I.c;
+        const Plan& P = c->plan;
+        const int n = P.n, m = P.m, KK1 = (int)P.items.size();
+        const int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+        double* rlr = c->d_ha + (size_t)2 * ncmax * ncmax * I.ps->item_chunk +
+                      (size_t)2 * n * m * I.ps->item_chunk;
+        launch_emit(st, true, rlr, m, KK1, P.K, I.d_recs, I.nrecs, I.ps->d_kra, I.ps->d_krb,
+                    I.ps->d_itrmo, c->cfg.throut, I.os);
+        L += 3;
+    }
+    RT_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
+    if (!out) return RT_ERR_USER;
+    *out = nullptr;
+    std::unique_ptr<rt_batch> b(new (std::nothrow) rt_batch());
+    if (!b) return RT_ERR_PROGRAM;
+    rt_batch* B = b.get();
+    try {
+        if (count < 1 || !ctxs) throw Error(RT_ERR_USER, "empty batch");
+        RT_CUDA(cudaGetDevice(&B->device));
+        RT_CUDA(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
+        RT_CUDA(cudaMalloc(&B->d_err, sizeof(int)));
+        RT_CUDA(cudaMemset(B->d_err, 0, sizeof(int)));
+        for (int i = 0; i < 2; ++i) RT_CUDA(cudaEventCreate(&B->ev[i]));
+        size_t gmax = 0;
+        for (int i = 0; i < count; ++i) {
+            rt_ctx* c = ctxs[i];
+            if (!c) throw Error(RT_ERR_USER, "null context in batch");
+            if (c->device != B->device) throw Error(RT_ERR_USER, "batch contexts on different devices");
+            if (!c->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
+            if (c->cfg.precision != RT_PREC_SPLIT_BF16)
+                throw Error(RT_ERR_USER, "batched transforms use precision RT_PREC_SPLIT_BF16");
+            for (int j = 0; j < i; ++j)
+                if (ctxs[j] == c) throw Error(RT_ERR_USER, "context twice in one batch");
+            flush_staged(c);
+            gmax = std::max(gmax, c->plan.pgroups.size());
+        }
+        B->inst.resize(count);
+        for (int i = 0; i < count; ++i) {
+            BatchInst& I = B->inst[i];
+            rt_ctx* c = ctxs[i];
+            I.c = c;
+            I.gen = c->gen;
+            I.ps.reset(new Pass(c));
+            pass_setup(*I.ps, true);
+            Pass& ps = *I.ps;
+            Plan& P = c->plan;
+            Work& w = W(c);
+            I.d_total = ps.alloc<long long>(4);
+            for (int cc = 0; cc < 4; ++cc) I.d_off[cc] = ps.alloc<long long>(std::max(1LL, w.nrec[cc]));
+            std::vector<EmitRec> recs(w.recs);
+            for (size_t t = 0; t < P.items.size(); ++t)
+                for (int r = w.item_rec0[t]; r < w.item_rec0[t + 1]; ++r) recs[r].ijl = (int)t;
+            I.nrecs = (int)recs.size();
+            I.d_recs = ps.upload(recs.data(), recs.size());
+            for (int cc = 0; cc < 4; ++cc) {
+                I.os.cnt[cc] = c->d_hdr[cc];
+                I.os.off[cc] = I.d_off[cc];
+                I.os.idx[cc] = c->d_oidx[cc];
+                I.os.val[cc] = c->d_oval[cc];
+            }
+            I.os.total = I.d_total;
+            I.d_jobs.assign(P.pgroups.size(), nullptr);
+            I.jobs_smem.assign(P.pgroups.size(), 0);
+            I.covered.assign(P.pgroups.size(), 0);
+            for (size_t g = 0; g < P.pgroups.size(); ++g) {
+                const auto& jv = P.pg_jobs[g];
+                I.d_jobs[g] = ps.upload(jv.data(), std::max<size_t>(1, jv.size()));
+                for (auto& j : jv) I.jobs_smem[g] = std::max(I.jobs_smem[g], (size_t)(j.r_hi - j.r_lo) * j.nk * 8);
+                for (auto& gg : P.g1)
+                    if (gg.pg == (int)g) I.covered[g] += P.blk_size[gg.rblk];
+            }
+        }
+        RT_CUDA(cudaDeviceSynchronize());
+        // grouped GEMM stages
+        B->g1.assign(gmax, nullptr);
+        B->g2.assign(gmax, nullptr);
+        for (size_t g = 0; g < gmax; ++g) {
+            B->g1[g] = split_group_new(0);
+            B->all.push_back(B->g1[g]);
+            B->g2[g] = split_group_new(1);
+            B->all.push_back(B->g2[g]);
+            for (BatchInst& I : B->inst) {
+                rt_ctx* c = I.c;
+                const Plan& P = c->plan;
+                if (g >= P.pgroups.size()) continue;
+                const int n = P.n, m = P.m, npc = P.pgroups[g].size;
+                const long long plane = (long long)n * m * npc;
+                for (auto& gg : P.g1)
+                    if (gg.pg == (int)g)
+                        split_group_add_gemm1(B->g1[g], c, gg, npc, EpiHA{c->d_ha, P.blk_start[gg.rblk], m, npc, plane});
+                double* ri = c->d_ha + (size_t)2 * n * m * I.ps->pair_chunk;
+                split_group_add_gemm24(B->g2[g], c, 2 * n, (long long)m * npc, EpiRowMajor{ri, (long long)m * npc, 0});
+            }
+        }
+        for (int cc = 0; cc < 2; ++cc) {
+            B->g3[cc] = split_group_new(2);
+            B->all.push_back(B->g3[cc]);
+            for (BatchInst& I : B->inst) {
+                rt_ctx* c = I.c;
+                const Plan& P = c->plan;
+                const int n = P.n, m = P.m, nc = P.ncomp[cc], KK1 = (int)P.items.size();
+                if (nc == 0) continue;
+                const int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+                double* rk = c->d_ha + (size_t)2 * ncmax * ncmax * I.ps->item_chunk;
+                split_group_add_gemm3(B->g3[cc], c, cc, nc, KK1,
+                                      EpiRK{rk, m, (long long)P.comp_off[cc] * KK1, (long long)n * KK1 * m});
+            }
+        }
+        B->g4 = split_group_new(1);
+        B->all.push_back(B->g4);
+        for (BatchInst& I : B->inst) {
+            rt_ctx* c = I.c;
+            const Plan& P = c->plan;
+            const int n = P.n, m = P.m, KK1 = (int)P.items.size();
+            const int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
+            double* rlr = c->d_ha + (size_t)2 * ncmax * ncmax * I.ps->item_chunk +
+                          (size_t)2 * n * m * I.ps->item_chunk;
+            split_group_add_gemm24(B->g4, c, 2 * n, (long long)KK1 * m, EpiRowMajor{rlr, (long long)KK1 * m, 0});
+        }
+        for (SplitGroup* g : B->all) split_group_build(g, B->inst[0].c);
+        B->bn.assign(B->all.size(), 128);
+        B->gev.resize(2 * B->all.size());
+        for (auto& e : B->gev) RT_CUDA(cudaEventCreate(&e));
+        B->stats.instances = count;
+        for (BatchInst& I : B->inst) B->stats.flops_algorithmic += algorithmic_flops(I.c->plan);
+        for (SplitGroup* g : B->all) B->stats.flops_gemm_executed += split_group_flops(g, true);
+    } catch (const Error& e) {
+        rt::set_thread_error(e.msg);
+        return e.code;
+    } catch (const std::exception& e) {
+        rt::set_thread_error(e.what());
+        return RT_ERR_PROGRAM;
+    }
+    *out = b.release();
+    return RT_OK;
+}
+
+extern "C" int rt_batch_run(rt_batch* b) {
+    if (!b) return RT_ERR_USER;
+    try {
+        for (BatchInst& I : b->inst)
+            if (I.c->gen != I.gen)
+                throw Error(RT_ERR_MISMATCH, "a context of the batch changed after rt_batch_create");
+        if (!b->tuned) {
+            // tile width per grouped stage: time every stage at 128 and at 64
+            const double t0 = 0.0;
+            (void)t0;
+            std::vector<float> ms[2];
+            cudaEvent_t a, z;
+            RT_CUDA(cudaEventCreate(&a));
+            RT_CUDA(cudaEventCreate(&z));
+            RT_CUDA(cudaEventRecord(a, b->st));
+            for (int v = 0; v < 2; ++v) {
+                std::fill(b->bn.begin(), b->bn.end(), v == 0 ? 128 : 64);
+                batch_enqueue(b, true);
+                RT_CUDA(cudaStreamSynchronize(b->st));
+                ms[v].assign(b->all.size(), 0.f);
+                for (size_t i = 0; i < b->all.size(); ++i)
+                    if (split_group_size(b->all[i]) > 0)
+                        RT_CUDA(cudaEventElapsedTime(&ms[v][i], b->gev[2 * i], b->gev[2 * i + 1]));
+            }
+            RT_CUDA(cudaEventRecord(z, b->st));
+            RT_CUDA(cudaEventSynchronize(z));
+            float tune_ms = 0.f;
+            RT_CUDA(cudaEventElapsedTime(&tune_ms, a, z));
+            cudaEventDestroy(a);
+            cudaEventDestroy(z);
+            b->stats.tile128 = b->stats.tile64 = 0;
+            for (size_t i = 0; i < b->all.size(); ++i) {
+                if (split_group_size(b->all[i]) == 0) continue;
+                b->bn[i] = ms[1][i] < ms[0][i] ? 64 : 128;
+                ++(b->bn[i] == 64 ? b->stats.tile64 : b->stats.tile128);
+            }
+            b->stats.ms_tune = tune_ms;
+            // capture the tuned sequence once
+            RT_CUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+            try {
+                batch_enqueue(b, false);
+            } catch (...) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(b->st, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            RT_CUDA(cudaStreamEndCapture(b->st, &b->graph));
+            RT_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+            size_t nodes = 0;
+            RT_CUDA(cudaGraphGetNodes(b->graph, nullptr, &nodes));
+            b->stats.graph_nodes = (int)nodes;
+            b->stats.kernel_launches = b->launches;
+            b->tuned = true;
+        }
+        RT_CUDA(cudaEventRecord(b->ev[0], b->st));
+        RT_CUDA(cudaGraphLaunch(b->exec, b->st));
+        RT_CUDA(cudaEventRecord(b->ev[1], b->st));
+        RT_CUDA(cudaStreamSynchronize(b->st));
+        float ms = 0.f;
+        RT_CUDA(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+        b->stats.ms_last = ms;
+        int e = 0;
+        RT_CUDA(cudaMemcpy(&e, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) {
+            RT_CUDA(cudaMemset(b->d_err, 0, sizeof(int)));
+            throw Error(RT_ERR_PROGRAM, "grouped split GEMM gave up waiting (status " + std::to_string(e) + ")");
+        }
+        int grouped = 0;
+        for (SplitGroup* g : b->all) grouped += split_group_size(g) > 0 ? 1 : 0;
+        b->stats.grouped_launches = grouped;
+        for (BatchInst& I : b->inst) {
+            rt_ctx* c = I.c;
+            long long tot[4];
+            unsigned long long hs[8];
+            RT_CUDA(cudaMemcpy(tot, I.d_total, sizeof(tot), cudaMemcpyDeviceToHost));
+            RT_CUDA(cudaMemcpy(hs, I.ps->d_stat, sizeof(hs), cudaMemcpyDeviceToHost));
+            if (hs[0] & ST_BAD_LABEL)
+                throw Error(RT_ERR_USER, "integral label outside 1..NSC or pq label with q > p");
+            if (hs[0] & ST_BAD_BLOCK)
+                throw Error(RT_ERR_USER, "integral outside the (LL|LL)/(SS|LL)/(SS|SS) or irrep block structure");
+            Work& w = W(c);
+            for (int cc = 0; cc < 4; ++cc) {
+                c->out_nz[cc] = tot[cc];
+                c->out_nrec[cc] = w.nrec[cc];
+                c->stats.nfinal[cc] = tot[cc];
+                c->stats.nrec[cc] = w.nrec[cc];
+            }
+            c->stats.nhalft = (long long)hs[1];
+            c->stats.flops_algorithmic = algorithmic_flops(c->plan);
+            c->transformed = true;
+        }
+    } catch (const Error& e) {
+        b->err = e.msg;
+        return e.code;
+    } catch (const std::exception& e) {
+        b->err = e.what();
+        return RT_ERR_PROGRAM;
+    }
+    return RT_OK;
+}
+
+extern "C" int rt_batch_get_stats(rt_batch* b, rt_batch_stats* out) {
+    if (!b || !out) return RT_ERR_USER;
+    *out = b->stats;
+    return RT_OK;
+}
+
+extern "C" const char* rt_batch_last_error(rt_batch* b) { return b ? b->err.c_str() : ""; }
+
+extern "C" void rt_batch_destroy(rt_batch* b) {
+    if (!b) return;
+    if (b->st) cudaStreamSynchronize(b->st);
+    delete b;
 }
 
 extern "C" int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz) {

@@ -227,4 +227,5 @@ struct rt_ctx {
     size_t dev_bytes = 0, dev_peak = 0;
     std::vector<std::pair<void*, size_t>> allocs;
     bool transformed = false;
+    unsigned long long gen = 0;  // input generation (coefficients, records)
 };

@@ -43,7 +43,6 @@
 namespace rt {
 
 constexpr int SBM = 128, SBN = 128, SBK = 32, NSTAGE = 2, MAX_SLICES = 6;
-constexpr uint32_t TMEM_COLS = 512;
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
 enum : int { ERR_TIMEOUT_EMPTY = 1, ERR_TIMEOUT_FULL = 2, ERR_TIMEOUT_TMEM = 3 };
@@ -257,23 +256,86 @@ constexpr int EPI_WARPS = 8;                 // two per TMEM lane group
 constexpr int EC = 16;                       // epilogue columns per TMEM load
 constexpr int GEMM_THREADS = 64 + 32 * EPI_WARPS;
 
+// Where the tiles of a launch come from.  One problem: the kernel
+// parameters.  A group: tables in global memory (per problem its arguments,
+// its two tensor maps and its epilogue, and the first global tile index).
 template <class Epi>
-__global__ void __launch_bounds__(GEMM_THREADS, 1)
-    k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                 SplitArgs g, Epi epi) {
+struct OneProblem {
+    const CUtensorMap* ma;
+    const CUtensorMap* mb;
+    SplitArgs g;
+    Epi e;
+    __device__ __forceinline__ long long ntiles() const {
+        return (long long)g.tiles_m * g.tiles_n * g.ksplit;
+    }
+    __device__ __forceinline__ int find(long long) const { return 0; }
+    __device__ __forceinline__ long long first(int) const { return 0; }
+    __device__ __forceinline__ const SplitArgs& args(int) const { return g; }
+    __device__ __forceinline__ const CUtensorMap* mapA(int) const { return ma; }
+    __device__ __forceinline__ const CUtensorMap* mapB(int) const { return mb; }
+    __device__ __forceinline__ const Epi& epi(int) const { return e; }
+};
+
+template <class Epi>
+struct GroupTable {
+    const SplitArgs* g;        // [nprob]
+    const CUtensorMap* maps;   // [2 * nprob]: A, B (64-byte aligned)
+    const Epi* e;              // [nprob]
+    const long long* start;    // [nprob + 1]: first global tile of each problem
+    int nprob;
+    __device__ __forceinline__ long long ntiles() const { return start[nprob]; }
+    __device__ __forceinline__ int find(long long t) const {
+        int lo = 0, hi = nprob - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (start[mid] <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    }
+    __device__ __forceinline__ long long first(int p) const { return start[p]; }
+    __device__ __forceinline__ const SplitArgs& args(int p) const { return g[p]; }
+    __device__ __forceinline__ const CUtensorMap* mapA(int p) const { return maps + 2 * p; }
+    __device__ __forceinline__ const CUtensorMap* mapB(int p) const { return maps + 2 * p + 1; }
+    __device__ __forceinline__ Epi epi(int p) const { return e[p]; }
+};
+
+// tile t of a launch: problem, output tile (tm, tn), K split and K blocks
+struct TileRef {
+    int p, ks, kb0, kb1;
+    long long tm, tn;
+};
+
+template <class Tab>
+__device__ __forceinline__ TileRef tile_ref(const Tab& tab, long long t) {
+    TileRef r;
+    r.p = tab.find(t);
+    const SplitArgs& g = tab.args(r.p);
+    const long long l = t - tab.first(r.p);
+    const long long tmn = l / g.ksplit;
+    r.ks = (int)(l - tmn * g.ksplit);
+    r.kb0 = r.ks * g.kcb;
+    r.kb1 = min(g.Kp / SBK, r.kb0 + g.kcb);
+    r.tm = tmn / g.tiles_n;
+    r.tn = tmn - r.tm * g.tiles_n;
+    return r;
+}
+
+// The GEMM body: BN = output tile width (128 or 64), s slices.
+template <int BN, class Epi, class Tab>
+__device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* error) {
+    constexpr uint32_t TCOLS = 4 * BN;  // four accumulators of BN columns
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[NSTAGE], empty[NSTAGE], tfull, tempty;
     __shared__ uint32_t tbase;
     __shared__ volatile int abort_flag;
     __shared__ int issued[NSTAGE];
-    __shared__ float fcol_w[EPI_WARPS][SBN / 2];  // per epilogue warp: 2^ecol of its columns
+    __shared__ float fcol_w[EPI_WARPS][BN / 2];  // per epilogue warp: 2^ecol of its columns
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const int s = g.s;
-    const uint32_t slice_a = SBM * SBK * 2, slice_b = SBN * SBK * 2;
+    const uint32_t slice_a = SBM * SBK * 2, slice_b = BN * SBK * 2;
     const uint32_t stage_bytes = (uint32_t)s * (slice_a + slice_b);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nkb = g.Kp / SBK;
-    const long long ntiles = (long long)g.tiles_m * g.tiles_n * g.ksplit;
+    const long long ntiles = tab.ntiles();
     if (threadIdx.x == 0) {
         for (int i = 0; i < NSTAGE; ++i) {
             mbar_init(&full[i], 1);
@@ -285,7 +347,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         abort_flag = 0;
         mbar_fence_init();
     }
-    if (warp == 0) tmem_alloc(&tbase, TMEM_COLS);
+    if (warp == 0) tmem_alloc(&tbase, TCOLS);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -295,24 +357,25 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         if (lane == 0) {  // ---- TMA producer ----
             long long gk = 0;
             for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x) {
-                const long long tmn = tile / g.ksplit;
-                const int kb0 = (int)(tile - tmn * g.ksplit) * g.kcb, kb1 = min(nkb, kb0 + g.kcb);
-                const long long tm = tmn / g.tiles_n, tn = tmn - tm * g.tiles_n;
-                for (int kb = kb0; kb < kb1; ++kb, ++gk) {
+                const TileRef r = tile_ref(tab, tile);
+                const SplitArgs& g = tab.args(r.p);
+                const CUtensorMap* ma = tab.mapA(r.p);
+                const CUtensorMap* mb = tab.mapB(r.p);
+                for (int kb = r.kb0; kb < r.kb1; ++kb, ++gk) {
                     const int st = (int)(gk % NSTAGE);
                     const uint32_t ph = (uint32_t)((gk / NSTAGE) & 1);
                     if (!mbar_wait_bounded(&empty[st], ph ^ 1u, &abort_flag, WAIT_NS)) {
-                        if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_EMPTY);
+                        if (!abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_EMPTY);
                         abort_flag = 1;
                         break;
                     }
                     unsigned char* base = smem + (size_t)st * stage_bytes;
                     mbar_expect_tx(&full[st], stage_bytes);
                     for (int t = 0; t < s; ++t) {
-                        tma_load_2d(base + t * slice_a, &mapA, &full[st], kb * SBK,
-                                    (int)(t * g.M + tm * SBM));
-                        tma_load_2d(base + (size_t)s * slice_a + t * slice_b, &mapB, &full[st],
-                                    kb * SBK, (int)(t * g.N + tn * SBN));
+                        tma_load_2d(base + t * slice_a, ma, &full[st], kb * SBK,
+                                    (int)(t * g.M + r.tm * SBM));
+                        tma_load_2d(base + (size_t)s * slice_a + t * slice_b, mb, &full[st],
+                                    kb * SBK, (int)(t * g.N + r.tn * BN));
                     }
                     issued[st] = 1 + (int)ph;  // phase parity of the outstanding load
                 }
@@ -320,23 +383,23 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---- MMA issuer ----
-            const uint32_t idesc = umma_idesc_bf16(SBM, SBN);
+            const uint32_t idesc = umma_idesc_bf16(SBM, BN);
             long long gk = 0;
             int it = 0;
             for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x, ++it) {
                 if (it > 0 && !mbar_wait_bounded(&tempty, (uint32_t)((it - 1) & 1), &abort_flag, WAIT_NS)) {
-                    if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_TMEM);
+                    if (!abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_TMEM);
                     abort_flag = 1;
                     break;
                 }
                 tc_fence_after();
                 bool started[4] = {false, false, false, false};
-                const int kb0 = (int)(tile % g.ksplit) * g.kcb, kb1 = min(nkb, kb0 + g.kcb);
-                for (int kb = kb0; kb < kb1; ++kb, ++gk) {
+                const TileRef r = tile_ref(tab, tile);
+                for (int kb = r.kb0; kb < r.kb1; ++kb, ++gk) {
                     const int st = (int)(gk % NSTAGE);
                     const uint32_t ph = (uint32_t)((gk / NSTAGE) & 1);
                     if (!mbar_wait_bounded(&full[st], ph, &abort_flag, WAIT_NS)) {
-                        if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_FULL);
+                        if (!abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_FULL);
                         abort_flag = 1;
                         break;
                     }
@@ -346,7 +409,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     for (int t = 0; t < s; ++t)
                         for (int u = 0; u + t < s; ++u) {
                             const int acc = t + u < 3 ? t + u : 3;
-                            const uint32_t dt = tmem + (uint32_t)(acc * SBN);
+                            const uint32_t dt = tmem + (uint32_t)(acc * BN);
                             const uint64_t da = umma_sdesc(base + t * slice_a, 512, UMMA_SWIZZLE_64B);
                             const uint64_t db = umma_sdesc(base + (size_t)s * slice_a + u * slice_b, 512,
                                                            UMMA_SWIZZLE_64B);
@@ -370,20 +433,21 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
         int it = 0;
         for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x, ++it) {
-            const long long tmn = tile / g.ksplit, ks = tile - tmn * g.ksplit;
-            const long long tm = tmn / g.tiles_n, tn = tmn - tm * g.tiles_n;
+            const TileRef r = tile_ref(tab, tile);
+            const SplitArgs& g = tab.args(r.p);
+            const long long ks = r.ks, tm = r.tm, tn = r.tn;
             // column scale factors of this warp's half tile (warp-local: no
             // barrier another role could leave waiting)
             float* fcol = fcol_w[ew];
             __syncwarp();
-            for (int j = lane; j < SBN / 2; j += 32) {
-                const long long col = tn * SBN + chalf * (SBN / 2) + j;
+            for (int j = lane; j < BN / 2; j += 32) {
+                const long long col = tn * BN + chalf * (BN / 2) + j;
                 const int e = col < g.N ? g.col_exp[ks * g.N + col] : -2000;
                 fcol[j] = e < -1000 ? 0.0f : pow2f_safe(e);
             }
             __syncwarp();
             if (!mbar_wait_bounded(&tfull, (uint32_t)(it & 1), &abort_flag, WAIT_NS)) {
-                if (!abort_flag) atomicCAS(g.error, 0, ERR_TIMEOUT_TMEM);
+                if (!abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_TMEM);
                 abort_flag = 1;
                 break;
             }
@@ -391,15 +455,16 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             const long long row = tm * SBM + lg * 32 + lane;
             const int erow = row < g.M ? g.row_exp[ks * g.M + row] : -2000;
             const float frow = erow < -1000 ? 0.0f : pow2f_safe(erow - 28);
+            const auto& epi = tab.epi(r.p);
             const typename Epi::Row er = epi.row(ks * g.M + (row < g.M ? row : 0));
-            for (int c0 = chalf * (SBN / 2); c0 < (chalf + 1) * (SBN / 2); c0 += EC) {
+            for (int c0 = chalf * (BN / 2); c0 < (chalf + 1) * (BN / 2); c0 += EC) {
                 uint32_t r0[EC], r1[EC], r2[EC], r3[EC];
                 tmem_ld16(tmem + lane_base + (uint32_t)c0, r0);
-                if (s >= 2) tmem_ld16(tmem + lane_base + (uint32_t)(SBN + c0), r1);
-                if (s >= 3) tmem_ld16(tmem + lane_base + (uint32_t)(2 * SBN + c0), r2);
-                if (s >= 4) tmem_ld16(tmem + lane_base + (uint32_t)(3 * SBN + c0), r3);
+                if (s >= 2) tmem_ld16(tmem + lane_base + (uint32_t)(BN + c0), r1);
+                if (s >= 3) tmem_ld16(tmem + lane_base + (uint32_t)(2 * BN + c0), r2);
+                if (s >= 4) tmem_ld16(tmem + lane_base + (uint32_t)(3 * BN + c0), r3);
                 tmem_ld_wait();
-                if (c0 + EC == (chalf + 1) * (SBN / 2)) {  // this warp's accumulators drained
+                if (c0 + EC == (chalf + 1) * (BN / 2)) {  // this warp's accumulators drained
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty);
@@ -417,11 +482,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     two_sum(s1, a2, s2, e2);
                     two_sum(s2, a3, s3, e3);
                     fast_two_sum(s3, (e1 + e2) + e3, hi, lo);
-                    const float f = fcol[c0 - chalf * (SBN / 2) + j] * frow;  // 2^(erow+ecol-28)
+                    const float f = fcol[c0 - chalf * (BN / 2) + j] * frow;  // 2^(erow+ecol-28)
                     r0[j] = __float_as_uint(hi * f);   // the accumulator registers now hold
                     r1[j] = __float_as_uint(lo * f);   // the float-float result
                 }
-                epi.store(er, tn * SBN + c0, g.N, r0, r1);
+                epi.store(er, tn * BN + c0, g.N, r0, r1);
             }
         }
     }
@@ -434,7 +499,23 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             if (issued[st]) mbar_wait_bounded(&full[st], (uint32_t)(issued[st] - 1), &never, WAIT_NS);
     }
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
+    if (warp == 0) tmem_dealloc(tmem, TCOLS);
+}
+
+// One problem: operands through kernel-parameter tensor maps.
+template <int BN, class Epi>
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                 SplitArgs g, Epi epi) {
+    const OneProblem<Epi> tab{&mapA, &mapB, g, epi};
+    split_gemm_body<BN, Epi>(tab, g.s, g.error);
+}
+
+// A group of problems (one persistent launch over all their tiles).
+template <int BN, class Epi>
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    k_split_gemm_grouped(GroupTable<Epi> tab, int s, int* error) {
+    split_gemm_body<BN, Epi>(tab, s, error);
 }
 
 // ---------------------------------------------------------------------------
@@ -590,9 +671,9 @@ static SplitState* state(rt_ctx* c) {
         S->d_err = (int*)salloc(S, sizeof(int));
         RT_CUDA(cudaMemset(S->d_err, 0, sizeof(int)));
         const size_t need = (size_t)NSTAGE * S->s * (SBM + SBN) * SBK * 2 + 1024;
-        set_smem_limit(k_split_gemm<EpiFF_HA>, need, prop);
-        set_smem_limit(k_split_gemm<EpiFF_RowMajor>, need, prop);
-        set_smem_limit(k_split_gemm<EpiFF_RK>, need, prop);
+        set_smem_limit(k_split_gemm<128, EpiFF_HA>, need, prop);
+        set_smem_limit(k_split_gemm<128, EpiFF_RowMajor>, need, prop);
+        set_smem_limit(k_split_gemm<128, EpiFF_RK>, need, prop);
         c->split = S;
     }
     return c->split;
@@ -726,11 +807,12 @@ double split_flop_factor(rt_ctx* c) {
     return s * (s + 1) / 2.0;
 }
 
-static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int Kp) {
+static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int Kp,
+                            int box_rows = SBM) {
     CUtensorMap m;
     cuuint64_t gd[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
     cuuint64_t gs[1] = {(cuuint64_t)Kp * 2};
-    cuuint32_t box[2] = {(cuuint32_t)SBK, (cuuint32_t)SBM};
+    cuuint32_t box[2] = {(cuuint32_t)SBK, (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = S->encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), gd, gs,
                            box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
@@ -770,7 +852,7 @@ static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M,
     const int grid = (int)std::min<long long>(ntiles, S->num_sms);
     const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
     c->ktimer.begin();
-    k_split_gemm<Epi><<<grid, GEMM_THREADS, smem, c->stream>>>(ma, mb, g, epi);
+    k_split_gemm<128, Epi><<<grid, GEMM_THREADS, smem, c->stream>>>(ma, mb, g, epi);
     // executed tensor FLOPs: s(s+1)/2 digit products over the padded K
     c->ktimer.end(2.0 * M * (double)N * Kp * (s * (s + 1) / 2), 2.0 * M * (double)N * K);
     ++*launches;
@@ -805,13 +887,28 @@ void split_gemm1(rt_ctx* c, const G1Group& gg, int npc, const EpiHA& e, int* lau
              Kp, epi, launches);
 }
 
+// operand slicing of GEMM2/4 (B = float-float K x N) and GEMM3 (A = M3 rows)
+void split_prep_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, cudaStream_t st,
+                       int* launches) {
+    SplitState* S = state(c);
+    launch_slice_cols(S->s, (const float2*)Bsrc, N, K, N, kpad(K), S->b_exp, S->a_sl, st);
+    ++*launches;
+}
+
+void split_prep_gemm3(rt_ctx* c, const double* m3, int nc, int nij, cudaStream_t st,
+                      int* launches) {
+    SplitState* S = state(c);
+    const int K = 2 * nc;
+    launch_slice_rows(S->s, RowsFF{(const float2*)m3, (long long)K}, (long long)nc * nij, K, kpad(K),
+                      S->a_sl, S->a_exp, st);
+    ++*launches;
+}
+
 void split_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRowMajor& e,
                   int* launches) {
     SplitState* S = state(c);
     const int Kp = kpad(K);
-    const float2* src = (const float2*)Bsrc;
-    launch_slice_cols(S->s, src, N, K, N, Kp, S->b_exp, S->a_sl, c->stream);
-    *launches += 1;
+    split_prep_gemm24(c, Bsrc, K, N, c->stream, launches);
     EpiFF_RowMajor epi{(float2*)e.c, e.ldc};
     run_gemm(c, S->qah.d, S->qah.exps, S->qah.rows, S->a_sl, S->b_exp, N, K, Kp, epi, launches);
 }
@@ -821,12 +918,187 @@ void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const E
     SplitState* S = state(c);
     const int K = 2 * nc, Kp = kpad(K);
     const long long M = (long long)nc * nij;
-    RowsFF src{(const float2*)m3, (long long)K};
-    launch_slice_rows(S->s, src, M, K, Kp, S->a_sl, S->a_exp, c->stream);
-    ++*launches;
+    split_prep_gemm3(c, m3, nc, nij, c->stream, launches);
     const ConstSlices& B = S->qar[comp];
     EpiFF_RK epi{(float2*)e.rk, e.m, e.rowoff, e.plane};
     run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * c->plan.m, K, Kp, epi, launches);
+}
+
+// ---------------------------------------------------------------------------
+// grouped launches: the same GEMM stage of many transforms in one
+// persistent launch over all their tiles (tables built once, launched many
+// times; tile width 128 or 64 chosen per group)
+// ---------------------------------------------------------------------------
+struct GroupProblem {
+    const void* a_sl;
+    const int* a_exp;
+    long long M;
+    const void* b_sl;
+    const int* b_exp;
+    long long N;
+    int K, Kp;
+};
+
+struct SplitGroup {
+    int kind = 0;  // 0: GEMM1 (EpiFF_HA), 1: GEMM2/4 (EpiFF_RowMajor), 2: GEMM3 (EpiFF_RK)
+    int s = 6;
+    std::vector<GroupProblem> probs;
+    std::vector<EpiFF_HA> e1;
+    std::vector<EpiFF_RowMajor> e24;
+    std::vector<EpiFF_RK> e3;
+    PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    int num_sms = 152;
+    // device tables per tile width (index 0: 128, 1: 64)
+    void* d_args[2] = {nullptr, nullptr};
+    void* d_maps[2] = {nullptr, nullptr};
+    void* d_start[2] = {nullptr, nullptr};
+    void* d_epi = nullptr;
+    long long ntiles[2] = {0, 0};
+    double flops_exec = 0.0, flops_alg = 0.0;
+};
+
+SplitGroup* split_group_new(int kind) {
+    SplitGroup* g = new SplitGroup();
+    g->kind = kind;
+    return g;
+}
+
+void split_group_add_gemm1(SplitGroup* G, rt_ctx* c, const G1Group& gg, int npc, const EpiHA& e) {
+    SplitState* S = state(c);
+    const Plan& P = c->plan;
+    const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk];
+    const ConstSlices& B = S->qap[gg.kblk];
+    G->probs.push_back({S->a_sl + gg.a_pp * npc, S->a_exp + gg.e_pp * npc, (long long)nr * npc, B.d,
+                        B.exps, 2LL * P.m, nk, kpad(nk)});
+    G->e1.push_back(EpiFF_HA{(float2*)e.ha, e.r0, e.m, e.npc, e.plane});
+    G->s = S->s;
+}
+
+void split_group_add_gemm24(SplitGroup* G, rt_ctx* c, int K, long long N, const EpiRowMajor& e) {
+    SplitState* S = state(c);
+    G->probs.push_back({S->qah.d, S->qah.exps, (long long)S->qah.rows, S->a_sl, S->b_exp, N, K,
+                        kpad(K)});
+    G->e24.push_back(EpiFF_RowMajor{(float2*)e.c, e.ldc});
+    G->s = S->s;
+}
+
+void split_group_add_gemm3(SplitGroup* G, rt_ctx* c, int comp, int nc, int nij, const EpiRK& e) {
+    SplitState* S = state(c);
+    const ConstSlices& B = S->qar[comp];
+    G->probs.push_back({S->a_sl, S->a_exp, (long long)nc * nij, B.d, B.exps, 2LL * c->plan.m, 2 * nc,
+                        kpad(2 * nc)});
+    G->e3.push_back(EpiFF_RK{(float2*)e.rk, e.m, e.rowoff, e.plane});
+    G->s = S->s;
+}
+
+template <class Epi>
+static void set_group_smem(const cudaDeviceProp& prop) {
+    set_smem_limit(k_split_gemm_grouped<128, Epi>, (size_t)NSTAGE * MAX_SLICES * (SBM + 128) * SBK * 2 + 1024, prop);
+    set_smem_limit(k_split_gemm_grouped<64, Epi>, (size_t)NSTAGE * MAX_SLICES * (SBM + 64) * SBK * 2 + 1024, prop);
+}
+
+// Encode the tensor maps of both tile widths and upload the tables.
+void split_group_build(SplitGroup* G, rt_ctx* c0) {
+    SplitState* S = state(c0);
+    G->encode = S->encode;
+    G->num_sms = S->num_sms;
+    static bool smem_set[64] = {};
+    int dev = 0;
+    RT_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && !smem_set[dev]) {
+        cudaDeviceProp prop;
+        RT_CUDA(cudaGetDeviceProperties(&prop, dev));
+        set_group_smem<EpiFF_HA>(prop);
+        set_group_smem<EpiFF_RowMajor>(prop);
+        set_group_smem<EpiFF_RK>(prop);
+        smem_set[dev] = true;
+    }
+    const int np = (int)G->probs.size();
+    if (np == 0) return;
+    SplitState tmp;
+    tmp.encode = G->encode;
+    for (int v = 0; v < 2; ++v) {
+        const int bn = v == 0 ? 128 : 64;
+        std::vector<SplitArgs> args(np);
+        std::vector<CUtensorMap> maps(2 * (size_t)np);
+        std::vector<long long> start(np + 1, 0);
+        for (int p = 0; p < np; ++p) {
+            const GroupProblem& q = G->probs[p];
+            SplitArgs& a = args[p];
+            a.M = q.M;
+            a.N = q.N;
+            a.Kp = q.Kp;
+            a.s = G->s;
+            a.tiles_m = (int)((q.M + SBM - 1) / SBM);
+            a.tiles_n = (int)((q.N + bn - 1) / bn);
+            a.ksplit = 1;
+            a.kcb = q.Kp / SBK;
+            a.row_exp = q.a_exp;
+            a.col_exp = q.b_exp;
+            a.error = nullptr;
+            maps[2 * p] = make_map(&tmp, q.a_sl, (long long)G->s * q.M, q.Kp, SBM);
+            maps[2 * p + 1] = make_map(&tmp, q.b_sl, (long long)G->s * q.N, q.Kp, bn);
+            start[p + 1] = start[p] + (q.M > 0 && q.N > 0 ? (long long)a.tiles_m * a.tiles_n : 0);
+            if (v == 0) {
+                G->flops_exec += 2.0 * q.M * (double)q.N * q.Kp * (G->s * (G->s + 1) / 2);
+                G->flops_alg += 2.0 * q.M * (double)q.N * q.K;
+            }
+        }
+        G->ntiles[v] = start[np];
+        RT_CUDA(cudaMalloc(&G->d_args[v], args.size() * sizeof(SplitArgs)));
+        RT_CUDA(cudaMalloc(&G->d_maps[v], maps.size() * sizeof(CUtensorMap)));
+        RT_CUDA(cudaMalloc(&G->d_start[v], start.size() * sizeof(long long)));
+        RT_CUDA(cudaMemcpy(G->d_args[v], args.data(), args.size() * sizeof(SplitArgs), cudaMemcpyHostToDevice));
+        RT_CUDA(cudaMemcpy(G->d_maps[v], maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+        RT_CUDA(cudaMemcpy(G->d_start[v], start.data(), start.size() * sizeof(long long), cudaMemcpyHostToDevice));
+    }
+    size_t eb = 0;
+    const void* src = nullptr;
+    if (G->kind == 0) { eb = G->e1.size() * sizeof(EpiFF_HA); src = G->e1.data(); }
+    if (G->kind == 1) { eb = G->e24.size() * sizeof(EpiFF_RowMajor); src = G->e24.data(); }
+    if (G->kind == 2) { eb = G->e3.size() * sizeof(EpiFF_RK); src = G->e3.data(); }
+    RT_CUDA(cudaMalloc(&G->d_epi, eb));
+    RT_CUDA(cudaMemcpy(G->d_epi, src, eb, cudaMemcpyHostToDevice));
+}
+
+template <int BN, class Epi>
+static void group_launch(SplitGroup* G, int v, cudaStream_t st, int* err) {
+    GroupTable<Epi> tab;
+    tab.g = (const SplitArgs*)G->d_args[v];
+    tab.maps = (const CUtensorMap*)G->d_maps[v];
+    tab.e = (const Epi*)G->d_epi;
+    tab.start = (const long long*)G->d_start[v];
+    tab.nprob = (int)G->probs.size();
+    const int grid = (int)std::min<long long>(G->ntiles[v], G->num_sms);
+    const size_t smem = (size_t)NSTAGE * G->s * (SBM + BN) * SBK * 2 + 1024;
+    k_split_gemm_grouped<BN, Epi><<<grid, GEMM_THREADS, smem, st>>>(tab, G->s, err);
+}
+
+// One persistent launch over all tiles of the group, tile width bn (128/64).
+void split_group_launch(SplitGroup* G, int bn, cudaStream_t st, int* err) {
+    if (G->probs.empty()) return;
+    const int v = bn == 64 ? 1 : 0;
+    if (G->ntiles[v] == 0) return;
+    if (G->kind == 0) (v ? group_launch<64, EpiFF_HA> : group_launch<128, EpiFF_HA>)(G, v, st, err);
+    if (G->kind == 1) (v ? group_launch<64, EpiFF_RowMajor> : group_launch<128, EpiFF_RowMajor>)(G, v, st, err);
+    if (G->kind == 2) (v ? group_launch<64, EpiFF_RK> : group_launch<128, EpiFF_RK>)(G, v, st, err);
+    RT_CUDA(cudaGetLastError());
+}
+
+int split_group_size(const SplitGroup* G) { return (int)G->probs.size(); }
+double split_group_flops(const SplitGroup* G, bool executed) {
+    return executed ? G->flops_exec : G->flops_alg;
+}
+
+void split_group_free(SplitGroup* G) {
+    if (!G) return;
+    for (int v = 0; v < 2; ++v) {
+        cudaFree(G->d_args[v]);
+        cudaFree(G->d_maps[v]);
+        cudaFree(G->d_start[v]);
+    }
+    cudaFree(G->d_epi);
+    delete G;
 }
 
 // ---------------------------------------------------------------------------
@@ -1089,7 +1361,7 @@ static const NoallocDevice& noalloc_setup(int dev) {
     RT_CUDA(cudaGetDeviceProperties(&prop, dev));
     if (prop.major * 10 + prop.minor != 103)
         throw Error(RT_ERR_PROGRAM, "rt_split_dgemm_noalloc needs an sm_103 device");
-    set_smem_limit(k_split_gemm<EpiF64_RowMajor>,
+    set_smem_limit(k_split_gemm<128, EpiF64_RowMajor>,
                    (size_t)NSTAGE * MAX_SLICES * (SBM + SBN) * SBK * 2 + 1024, prop);
     void* p = nullptr;
     RT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
@@ -1163,7 +1435,7 @@ extern "C" int rt_split_dgemm_noalloc(int M, int N, int K, const double* A, cons
         g.error = err;
         const int grid = std::min(g.tiles_m * g.tiles_n, D.num_sms);
         const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
-        k_split_gemm<EpiF64_RowMajor><<<grid, GEMM_THREADS, smem, st>>>(ma, mb, g, EpiF64_RowMajor{C, N});
+        k_split_gemm<128, EpiF64_RowMajor><<<grid, GEMM_THREADS, smem, st>>>(ma, mb, g, EpiF64_RowMajor{C, N});
         RT_CUDA(cudaGetLastError());
         int e = 0;
         RT_CUDA(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -20,6 +20,23 @@ void split_gemm24(rt_ctx* c, const double* B, int K, long long N, const EpiRowMa
 void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& epi,
                  int* launches);
 void split_release(rt_ctx* c);
+// operand slicing of GEMM2/4 and GEMM3 on stream st (the GEMM itself apart)
+void split_prep_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, cudaStream_t st,
+                       int* launches);
+void split_prep_gemm3(rt_ctx* c, const double* m3, int nc, int nij, cudaStream_t st,
+                      int* launches);
+// grouped launches of one GEMM stage over many transforms (kind 0: GEMM1,
+// 1: GEMM2/4, 2: GEMM3); tables are built once and launched many times
+struct SplitGroup;
+SplitGroup* split_group_new(int kind);
+void split_group_add_gemm1(SplitGroup* g, rt_ctx* c, const G1Group& gg, int npc, const EpiHA& e);
+void split_group_add_gemm24(SplitGroup* g, rt_ctx* c, int K, long long N, const EpiRowMajor& e);
+void split_group_add_gemm3(SplitGroup* g, rt_ctx* c, int comp, int nc, int nij, const EpiRK& e);
+void split_group_build(SplitGroup* g, rt_ctx* c0);
+void split_group_launch(SplitGroup* g, int bn, cudaStream_t st, int* err);
+int split_group_size(const SplitGroup* g);
+double split_group_flops(const SplitGroup* g, bool executed);
+void split_group_free(SplitGroup* g);
 // adjoint: X GEMM of one component and the split-K contraction
 void split_adj_x(rt_ctx* c, int comp, const double* m3, int nc, int nij, double* x,
                  __nv_bfloat16* sl, int* ex, int* launches);

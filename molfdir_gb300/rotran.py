@@ -36,6 +36,16 @@ class RotranError(RuntimeError):
         self.code = code
 
 
+class RtBatchStats(C.Structure):
+    _fields_ = [("instances", C.c_int), ("grouped_launches", C.c_int),
+                ("kernel_launches", C.c_int), ("graph_nodes", C.c_int), ("tile128", C.c_int),
+                ("tile64", C.c_int), ("ms_last", C.c_double), ("ms_tune", C.c_double),
+                ("flops_algorithmic", C.c_double), ("flops_gemm_executed", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class RtConfig(C.Structure):
     _fields_ = [("nsc", C.c_int), ("nsc1", C.c_int), ("nsp", C.c_int), ("nkr", C.c_int),
                 ("mfil", C.c_int), ("breit", C.c_int), ("thrgen", C.c_double),
@@ -72,7 +82,8 @@ EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_add_ao_records_bulk", "rt_read_srt_files", "rt_clear_ao_records",
            "rt_transform", "rt_result_sizes", "rt_copy_result", "rt_write_mdcint",
            "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm",
-           "rt_split_dgemm_noalloc", "rt_adjoint"]
+           "rt_split_dgemm_noalloc", "rt_adjoint", "rt_batch_create", "rt_batch_run",
+           "rt_batch_get_stats", "rt_batch_last_error", "rt_batch_destroy"]
 
 _lib = None
 
@@ -113,9 +124,16 @@ def load(build: bool = True):
                                    P(C.c_double), C.c_int, C.c_int]
     lib.rt_split_dgemm_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]
     lib.rt_adjoint.argtypes = [vp, vp, vp, P(C.c_double)]
+    lib.rt_batch_create.argtypes = [P(vp), P(vp), C.c_int]
+    lib.rt_batch_run.argtypes = [vp]
+    lib.rt_batch_get_stats.argtypes = [vp, P(RtBatchStats)]
+    lib.rt_batch_last_error.argtypes = [vp]
+    lib.rt_batch_last_error.restype = C.c_char_p
+    lib.rt_batch_destroy.argtypes = [vp]
+    lib.rt_batch_destroy.restype = None
     for name in EXPORTS:
         f = getattr(lib, name)
-        if name not in ("rt_last_error", "rt_destroy"):
+        if name not in ("rt_last_error", "rt_destroy", "rt_batch_last_error", "rt_batch_destroy"):
             f.restype = C.c_int
     _lib = lib
     return lib
@@ -343,3 +361,48 @@ def split_dgemm_noalloc(m: int, n: int, k: int, a_ptr: int, b_ptr: int, c_ptr: i
                                     C.c_void_p(c_ptr), slices, C.c_void_p(stream or None))
     if rc:
         raise RotranError(rc, lib.rt_last_error(None).decode())
+
+
+class Batch:
+    """Batched transforms of several split-precision contexts (``rt_batch_*``):
+    one grouped GEMM launch per stage, captured as a CUDA graph on the first
+    ``run()`` (after tuning the tile width per stage) and replayed after."""
+
+    def __init__(self, rts):
+        self.lib = load()
+        self.rts = list(rts)  # keep the contexts alive
+        arr = (C.c_void_p * len(self.rts))(*[r.h for r in self.rts])
+        h = C.c_void_p()
+        rc = self.lib.rt_batch_create(C.byref(h), arr, len(self.rts))
+        if rc:
+            raise RotranError(rc, self.lib.rt_last_error(None).decode())
+        self.h = h
+
+    def run(self):
+        rc = self.lib.rt_batch_run(self.h)
+        if rc:
+            raise RotranError(rc, self.lib.rt_batch_last_error(self.h).decode())
+
+    def stats(self) -> RtBatchStats:
+        s = RtBatchStats()
+        rc = self.lib.rt_batch_get_stats(self.h, C.byref(s))
+        if rc:
+            raise RotranError(rc, "rt_batch_get_stats failed")
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rt_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
