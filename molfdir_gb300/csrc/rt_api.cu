@@ -1225,6 +1225,10 @@ struct rt_batch {
     std::vector<int> bn;              // tile width per group of `all`
     cudaEvent_t ev[2] = {nullptr, nullptr};
     std::vector<cudaEvent_t> gev;     // around each grouped launch (tuning)
+    // per-instance kernels of a stage run on side streams forked from st
+    static constexpr int NSIDE = 8;
+    cudaStream_t side[NSIDE] = {};
+    cudaEvent_t fork = nullptr, join[NSIDE] = {};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool tuned = false;
@@ -1237,6 +1241,11 @@ struct rt_batch {
         for (SplitGroup* g : all) split_group_free(g);
         for (auto e : ev) if (e) cudaEventDestroy(e);
         for (auto e : gev) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        for (int i = 0; i < NSIDE; ++i) {
+            if (join[i]) cudaEventDestroy(join[i]);
+            if (side[i]) cudaStreamDestroy(side[i]);
+        }
         if (d_err) cudaFree(d_err);
         inst.clear();
         if (st) cudaStreamDestroy(st);
@@ -1260,92 +1269,100 @@ void batch_enqueue(rt_batch* b, bool timed) {
         ++L;
         ++gi;
     };
-    for (BatchInst& I : b->inst) {
-        RT_CUDA(cudaMemsetAsync(I.d_total, 0, 4 * sizeof(long long), st));
-        RT_CUDA(cudaMemsetAsync(I.ps->d_stat, 0, 8 * sizeof(unsigned long long), st));
-    }
+    // run fn(instance, stream) for every instance on the side streams
+    auto each = [&](auto fn) {
+        RT_CUDA(cudaEventRecord(b->fork, st));
+        for (int s = 0; s < rt_batch::NSIDE; ++s) RT_CUDA(cudaStreamWaitEvent(b->side[s], b->fork, 0));
+        for (size_t i = 0; i < b->inst.size(); ++i) fn(b->inst[i], b->side[i % rt_batch::NSIDE]);
+        for (int s = 0; s < rt_batch::NSIDE; ++s) {
+            RT_CUDA(cudaEventRecord(b->join[s], b->side[s]));
+            RT_CUDA(cudaStreamWaitEvent(st, b->join[s], 0));
+        }
+    };
     // ---- bucketing ----
-    for (BatchInst& I : b->inst) {
+    each([&](BatchInst& I, cudaStream_t ss) {
         rt_ctx* c = I.c;
         const Plan& P = c->plan;
         const DeviceTabs& T = I.ps->T;
+        RT_CUDA(cudaMemsetAsync(I.d_total, 0, 4 * sizeof(long long), ss));
+        RT_CUDA(cudaMemsetAsync(I.ps->d_stat, 0, 8 * sizeof(unsigned long long), ss));
         ScatterTabs tb{P.n, c->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
                        T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk};
-        launch_bucket(st, c->d_rint, c->d_l2, c->d_l1, c->n_int, I.ps->d_roff, I.ps->d_rmeta,
+        launch_bucket(ss, c->d_rint, c->d_l2, c->d_l1, c->n_int, I.ps->d_roff, I.ps->d_rmeta,
                       (int)c->rec_off.size(), tb, P.P, c->d_bcount, c->d_boff, c->d_bval, c->d_brs,
                       (unsigned int*)I.ps->d_stat);
         L += c->n_int > 0 ? 3 : 1;
-    }
+    });
     // ---- first half, pair-group stage by stage ----
     for (size_t g = 0; g < b->g1.size(); ++g) {
-        for (BatchInst& I : b->inst) {
+        each([&](BatchInst& I, cudaStream_t ss) {
             rt_ctx* c = I.c;
             const Plan& P = c->plan;
-            if (g >= P.pgroups.size()) continue;
+            if (g >= P.pgroups.size()) return;
             const int n = P.n, m = P.m, npc = P.pgroups[g].size;
             if (I.covered[g] < n)
-                RT_CUDA(cudaMemsetAsync(c->d_ha, 0, (size_t)2 * n * m * npc * sizeof(double), st));
+                RT_CUDA(cudaMemsetAsync(c->d_ha, 0, (size_t)2 * n * m * npc * sizeof(double), ss));
             if (!P.pg_jobs[g].empty()) {
-                launch_expand_rows(st, c->cfg.slices, c->d_bval, c->d_brs, c->d_boff, I.d_jobs[g],
+                launch_expand_rows(ss, c->cfg.slices, c->d_bval, c->d_brs, c->d_boff, I.d_jobs[g],
                                    (int)P.pg_jobs[g].size(), P.pgroups[g].start, npc, I.ps->T.ao_block,
                                    I.ps->T.ao_pos, I.jobs_smem[g], nullptr, split_a1_slices(c),
                                    split_a1_exps(c));
                 ++L;
             }
-        }
+        });
         group(b->g1[g]);
-        for (BatchInst& I : b->inst) {
+        each([&](BatchInst& I, cudaStream_t ss) {
             rt_ctx* c = I.c;
             const Plan& P = c->plan;
-            if (g >= P.pgroups.size()) continue;
-            split_prep_gemm24(c, c->d_ha, 2 * P.n, (long long)P.m * P.pgroups[g].size, st, &L);
-        }
+            if (g >= P.pgroups.size()) return;
+            split_prep_gemm24(c, c->d_ha, 2 * P.n, (long long)P.m * P.pgroups[g].size, ss, &L);
+        });
         group(b->g2[g]);
-        for (BatchInst& I : b->inst) {
+        each([&](BatchInst& I, cudaStream_t ss) {
             rt_ctx* c = I.c;
             const Plan& P = c->plan;
-            if (g >= P.pgroups.size()) continue;
+            if (g >= P.pgroups.size()) return;
             const int n = P.n, m = P.m, npc = P.pgroups[g].size;
             const int KK1 = (int)P.items.size();
             double* ri = c->d_ha + (size_t)2 * n * m * I.ps->pair_chunk;
-            launch_tr_select(st, true, ri, m, npc, P.pgroups[g].start, P.P, I.ps->d_items,
+            launch_tr_select(ss, true, ri, m, npc, P.pgroups[g].start, P.P, I.ps->d_items,
                              I.ps->d_isign, KK1, I.ps->d_pvmx, c->cfg.thrgen, c->d_hp, I.ps->d_stat + 1);
             L += (KK1 + 65534) / 65535;
-        }
+        });
     }
     // ---- second half ----
     for (int cc = 0; cc < 2; ++cc) {
-        for (BatchInst& I : b->inst) {
+        each([&](BatchInst& I, cudaStream_t ss) {
             rt_ctx* c = I.c;
             const Plan& P = c->plan;
             const int nc = P.ncomp[cc], KK1 = (int)P.items.size();
-            if (nc == 0) continue;
-            launch_expand(st, c->d_hp, P.P, KK1, 0, KK1, I.ps->d_pidx[cc], nc, c->d_ha);
+            if (nc == 0) return;
+            launch_expand(ss, c->d_hp, P.P, KK1, 0, KK1, I.ps->d_pidx[cc], nc, c->d_ha);
             ++L;
-            split_prep_gemm3(c, c->d_ha, nc, KK1, st, &L);
-        }
+            split_prep_gemm3(c, c->d_ha, nc, KK1, ss, &L);
+        });
         group(b->g3[cc]);
     }
-    for (BatchInst& I : b->inst) {
+    each([&](BatchInst& I, cudaStream_t ss) {
         rt_ctx* c = I.c;
         const Plan& P = c->plan;
         const int n = P.n, m = P.m, KK1 = (int)P.items.size();
         const int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
         double* rk = c->d_ha + (size_t)2 * ncmax * ncmax * I.ps->item_chunk;
-        split_prep_gemm24(c, rk, 2 * n, (long long)KK1 * m, st, &L);
-    }
+        split_prep_gemm24(c, rk, 2 * n, (long long)KK1 * m, ss, &L);
+    });
     group(b->g4);
-    for (BatchInst& I : b->inst) {
+    each([&](BatchInst& I, cudaStream_t ss) {
         rt_ctx* c = I.c;
         const Plan& P = c->plan;
         const int n = P.n, m = P.m, KK1 = (int)P.items.size();
         const int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
         double* rlr = c->d_ha + (size_t)2 * ncmax * ncmax * I.ps->item_chunk +
                       (size_t)2 * n * m * I.ps->item_chunk;
-        launch_emit(st, true, rlr, m, KK1, P.K, I.d_recs, I.nrecs, I.ps->d_kra, I.ps->d_krb,
+        launch_emit(ss, true, rlr, m, KK1, P.K, I.d_recs, I.nrecs, I.ps->d_kra, I.ps->d_krb,
                     I.ps->d_itrmo, c->cfg.throut, I.os);
         L += 3;
-    }
+    });
     RT_CUDA(cudaGetLastError());
 }
 
@@ -1364,6 +1381,11 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
         RT_CUDA(cudaMalloc(&B->d_err, sizeof(int)));
         RT_CUDA(cudaMemset(B->d_err, 0, sizeof(int)));
         for (int i = 0; i < 2; ++i) RT_CUDA(cudaEventCreate(&B->ev[i]));
+        RT_CUDA(cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming));
+        for (int i = 0; i < rt_batch::NSIDE; ++i) {
+            RT_CUDA(cudaStreamCreateWithFlags(&B->side[i], cudaStreamNonBlocking));
+            RT_CUDA(cudaEventCreateWithFlags(&B->join[i], cudaEventDisableTiming));
+        }
         size_t gmax = 0;
         for (int i = 0; i < count; ++i) {
             rt_ctx* c = ctxs[i];
