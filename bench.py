@@ -144,6 +144,24 @@ def cpu_sample(work, steps=1, warmup=0, seconds=15.0):
     return res, cores
 
 
+def run_gemm_case(args, rank):
+    """One split GEMM of the shape of the second and fourth quarter steps at
+    n = 400, 120 Kramers pairs (M = 2m = 480, K = 2n = 800), N = 32768, for
+    kernel profiling (float-float operands sliced on the device, 6 slices)."""
+    from molfdir_gb300 import rotran
+    rng = np.random.default_rng(0)
+    m_, k_, n_ = 480, 800, 32768
+    a = rng.standard_normal((m_, k_))
+    b = rng.standard_normal((k_, n_))
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        rotran.split_dgemm(a, b, slices=args.slices, mode=1)
+        dt = time.perf_counter() - t0
+    if rank == 0:
+        print(json.dumps({"workload": "gemm_m480_k800_n32768", "slices": args.slices,
+                          "seconds_per_call_with_host_work": dt}))
+
+
 def run_batched(args, rank, world, local, bf16_peak, peak_kind):
     """48 independent transforms of uneven size (n_AO ~ U[40,200], 60% small
     component, 16..80 Kramers pairs, seeds 0..47): split precision as one
@@ -259,7 +277,7 @@ def main():
     ap.add_argument("--slices", type=int, default=6)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "c1", "profile", "large", "batched"])
+                    choices=["precision", "c1", "profile", "large", "batched", "gemm"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -267,6 +285,8 @@ def main():
     hbm_peak, bf16_peak, peak_kind = peaks()
     if args.workload == "batched":
         return run_batched(args, rank, world, local, bf16_peak, peak_kind)
+    if args.workload == "gemm":
+        return run_gemm_case(args, rank)
     work = {"precision": WORKLOAD, "c1": SMALL, "profile": PROFILE, "large": LARGE}[args.workload]
 
     if args.impl == "reference":

@@ -167,13 +167,15 @@ __global__ void k_tr_select(const typename E::T* __restrict__ ri, int m, int npc
 // block (the role of MATMUL3's two updates, matmul3.F:75-82):
 //   M3[p][ij][plane][q] = Hp[plane][ij][pair(p,q)]
 // ---------------------------------------------------------------------------
+// The row blocks of one item are adjacent in launch order (blockIdx.x), so
+// the item's half-transformed row stays in L2 while they gather from it.
 __global__ void k_expand(const double* __restrict__ hp, int P, int nitems, int it0, int nij,
                          const int* __restrict__ pidx, int nc, double* __restrict__ m3) {
-    const int ijl = blockIdx.x;
+    const int ijl = blockIdx.y;
     const int it = it0 + ijl;
     const double* hr = hp + (long long)it * P;
     const double* hi = hp + (long long)nitems * P + (long long)it * P;
-    for (int p = blockIdx.y; p < nc; p += gridDim.y) {
+    for (int p = blockIdx.x; p < nc; p += gridDim.x) {
         double* row = m3 + ((long long)p * nij + ijl) * (2LL * nc);
         for (int q = threadIdx.x; q < nc; q += blockDim.x) {
             int pq = pidx[p * nc + q];
@@ -321,7 +323,8 @@ void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc
 
 void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
                    const int* pidx, int nc, double* m3) {
-    dim3 grid(nij, nc < 64 ? nc : 64);
+    if (nij > 65535) throw_dim("expansion: more than 65535 items per chunk");
+    dim3 grid(nc < 64 ? nc : 64, nij);
     k_expand<<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nc, m3);
 }
 

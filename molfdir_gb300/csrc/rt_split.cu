@@ -316,6 +316,13 @@ __device__ __forceinline__ TileRef tile_ref(const Tab& tab, long long t) {
     r.ks = (int)(l - tmn * g.ksplit);
     r.kb0 = r.ks * g.kcb;
     r.kb1 = min(g.Kp / SBK, r.kb0 + g.kcb);
+    if (g.tiles_m < g.tiles_n) {
+        // fewer row tiles: they vary fastest, so the CTAs that share a tile of
+        // the large B operand run at the same time and read it once from DRAM
+        r.tn = tmn / g.tiles_m;
+        r.tm = tmn - r.tn * g.tiles_m;
+        return r;
+    }
     r.tm = tmn / g.tiles_n;
     r.tn = tmn - r.tm * g.tiles_n;
     return r;
