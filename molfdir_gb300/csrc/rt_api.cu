@@ -741,6 +741,18 @@ void pass_setup(Pass& ps, bool exact = false) {
     RT_CUDA(cudaMemsetAsync(ps.d_stat, 0, 8 * sizeof(unsigned long long), ctx->stream));
 }
 
+// THRGEN / VMX(p) VMX(q) per pair (+inf below THRGEN): the split path's
+// FP32 screening threshold.
+float* pass_pair_thr(Pass& ps, double thrgen) {
+    const Work& w = W(ps.c);
+    std::vector<float> t(w.pair_vmx.size());
+    for (size_t i = 0; i < t.size(); ++i) {
+        const double vv = w.pair_vmx[i];
+        t[i] = vv < thrgen ? INFINITY : (float)(thrgen / vv);
+    }
+    return ps.upload(t.data(), t.size());
+}
+
 // Sort the records into pq buckets (SORT1) and check their labels.
 void pass_bucketing(Pass& ps) {
     rt_ctx* ctx = ps.c;
@@ -788,6 +800,7 @@ void pass_stage_a(Pass& ps, double thrgen) {
             RT_CUDA(cudaMemcpyAsync(d_jobs[g], jv.data(), jv.size() * sizeof(ExpandJob), cudaMemcpyHostToDevice, st));
     }
     const int nsl = split ? ctx->cfg.slices : 0;
+    float* d_pthr = pass_pair_thr(ps, thrgen);
     double* ha = ctx->d_ha;
     double* ri = ha + (size_t)2 * n * m * pair_chunk;
     double* a1 = ri + (size_t)2 * m * m * pair_chunk;  // FP64 GEMM1 operand (plain path)
@@ -832,7 +845,7 @@ void pass_stage_a(Pass& ps, double thrgen) {
                 gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2), ++ps.launches;
             gemm_end(2.0 * 2 * m * (double)m * npc * 2 * n);
             launch_tr_select(st, split, ri, m, npc, pg.start + c0, P.P, ps.d_items, ps.d_isign, KK1,
-                             ps.d_pvmx, thrgen, ctx->d_hp, ps.d_stat + 1);
+                             ps.d_pvmx, d_pthr, thrgen, ctx->d_hp, ps.d_stat + 1);
             ps.launches += (KK1 + 65534) / 65535;
         }
     }
@@ -1207,6 +1220,7 @@ struct BatchInst {
     int nrecs = 0;
     std::vector<ExpandJob*> d_jobs;
     std::vector<size_t> jobs_smem;
+    float* d_pthr = nullptr;
     std::vector<int> covered;
     OutStreams os{};
 };
@@ -1326,7 +1340,8 @@ void batch_enqueue(rt_batch* b, bool timed) {
             const int KK1 = (int)P.items.size();
             double* ri = c->d_ha + (size_t)2 * n * m * I.ps->pair_chunk;
             launch_tr_select(ss, true, ri, m, npc, P.pgroups[g].start, P.P, I.ps->d_items,
-                             I.ps->d_isign, KK1, I.ps->d_pvmx, c->cfg.thrgen, c->d_hp, I.ps->d_stat + 1);
+                             I.ps->d_isign, KK1, I.ps->d_pvmx, I.d_pthr, c->cfg.thrgen, c->d_hp,
+                             I.ps->d_stat + 1);
             L += (KK1 + 65534) / 65535;
         });
     }
@@ -1411,6 +1426,7 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
             Plan& P = c->plan;
             Work& w = W(c);
             I.d_total = ps.alloc<long long>(4);
+            I.d_pthr = pass_pair_thr(ps, c->cfg.thrgen);
             for (int cc = 0; cc < 4; ++cc) I.d_off[cc] = ps.alloc<long long>(std::max(1LL, w.nrec[cc]));
             std::vector<EmitRec> recs(w.recs);
             for (size_t t = 0; t < P.items.size(); ++t)

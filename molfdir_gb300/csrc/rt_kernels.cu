@@ -101,18 +101,45 @@ template void gemm_f64<EpiRK>(cudaStream_t, const double*, long long, long long,
 
 // Element formats of the intermediate arrays: FP64 (plain path) and
 // float-float (split path).  comb(a, b, sg) = a + sg*b.
+// magnitude of the complex number a + ib in FP32 without underflow of the squares
+__device__ __forceinline__ float mag32(float a, float b) {
+    a = fabsf(a);
+    b = fabsf(b);
+    const float mx = fmaxf(a, b), mn = fminf(a, b);
+    if (mx == 0.f) return 0.f;
+    const float r = __fdividef(mn, mx);
+    return mx * sqrtf(fmaf(r, r, 1.f));
+}
+
+// Threshold tests: |re + i im| compared with a threshold, in FP64 on the
+// plain path, in FP32 on the leading parts on the split path (the float-float
+// values carry their magnitude in .x; FP64 arithmetic runs at about 1/70 of
+// the FP32 rate on GB300).
 struct F64El {
     typedef double T;
     static __device__ __forceinline__ T comb(T a, T b, double sg) { return a + sg * b; }
     static __device__ __forceinline__ double val(T a) { return a; }
     static __device__ __forceinline__ T zero() { return 0.0; }
     static __device__ __forceinline__ T from(double v) { return v; }
+    static __device__ __forceinline__ bool nonzero(T re, T im) { return re != 0.0 || im != 0.0; }
+    static __device__ __forceinline__ bool above(T re, T im, double thr) { return hypot(re, im) > thr; }
+    // TROUT's screen (trout.F:194-207): kept unless VMX product or value too small
+    static __device__ __forceinline__ bool screen(T re, T im, double vv, float, double thrgen) {
+        return !(vv < thrgen) && !(hypot(re, im) < thrgen / vv);
+    }
 };
 struct FFEl {
     typedef float2 T;
     static __device__ __forceinline__ T comb(T a, T b, double sg) { return ff_add(a, b, (float)sg); }
     static __device__ __forceinline__ double val(T a) { return ff_to_double(a); }
     static __device__ __forceinline__ T zero() { return make_float2(0.f, 0.f); }
+    static __device__ __forceinline__ bool nonzero(T re, T im) { return re.x != 0.f || im.x != 0.f; }
+    static __device__ __forceinline__ bool above(T re, T im, double thr) {
+        return mag32(re.x, im.x) > (float)thr;
+    }
+    static __device__ __forceinline__ bool screen(T re, T im, double, float thr, double) {
+        return !(mag32(re.x, im.x) < thr);
+    }
     static __device__ __forceinline__ T from(double v) {
         const float h = __double2float_rn(v);
         return make_float2(h, __double2float_rn(v - (double)h));
@@ -128,12 +155,14 @@ struct FFEl {
 // RI = QA^H G_pq QA.  The screening test of TROUT (trout.F:194-207) is
 // applied to these values.
 // ---------------------------------------------------------------------------
+// pair_thr: THRGEN / VMX(p) VMX(q) per pair (+inf where the product is below
+// THRGEN), the threshold of the split path's FP32 test.
 template <class E>
 __global__ void k_tr_select(const typename E::T* __restrict__ ri, int m, int npc, int pq0, int P,
                             const int4* __restrict__ items, const float* __restrict__ item_sign,
                             int it0, int nitems, const double* __restrict__ pair_vmx,
-                            double thrgen, typename E::T* __restrict__ hp,
-                            unsigned long long* __restrict__ kept) {
+                            const float* __restrict__ pair_thr, double thrgen,
+                            typename E::T* __restrict__ hp, unsigned long long* __restrict__ kept) {
     typedef typename E::T T;
     const int it = it0 + blockIdx.y;
     const int pql = blockIdx.x * blockDim.x + threadIdx.x;
@@ -147,13 +176,9 @@ __global__ void k_tr_select(const typename E::T* __restrict__ ri, int m, int npc
         T re = E::comb(ri[a], ri[b], s);
         T im = E::comb(ri[plane + a], ri[plane + b], s);
         const int pq = pq0 + pql;
-        const double vv = pair_vmx[pq];
-        const double vr = E::val(re), vi = E::val(im);
-        bool pass;
-        if (vv < thrgen) pass = false;
-        else pass = !(hypot(vr, vi) < thrgen / vv);
+        const bool pass = E::screen(re, im, pair_vmx[pq], pair_thr ? pair_thr[pq] : 0.f, thrgen);
         if (!pass) { re = E::zero(); im = E::zero(); }
-        keep = pass && (vr != 0.0 || vi != 0.0);
+        keep = pass && E::nonzero(re, im);
         const long long o = (long long)it * P + pq;
         hp[o] = re;
         hp[(long long)nitems * P + o] = im;
@@ -236,6 +261,7 @@ __global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ 
         if (pos < KK) {
             x = pos / K + 1;
             y = pos - (x - 1) * K + 1;
+            typename E::T vr = E::zero(), vi = E::zero();
             if (in_set(cls, x, y, i, j)) {
                 const int Ks = (ks < 0 ? krb[x - 1] : kra[x - 1]) - 1;
                 const int Ls = (ls < 0 ? krb[y - 1] : kra[y - 1]) - 1;
@@ -243,10 +269,14 @@ __global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ 
                 const double sg = ((itrmo[Ks] > 0) == (itrmo[Ls] > 0)) ? 1.0 : -1.0;
                 const long long a = ((long long)Ks * nij + ijl) * m + Ls;
                 const long long b = ((long long)Lb * nij + ijl) * m + Kb;
-                re = E::val(E::comb(rlr[a], rlr[b], sg));
-                im = E::val(E::comb(rlr[plane + a], rlr[plane + b], sg));
+                vr = E::comb(rlr[a], rlr[b], sg);
+                vi = E::comb(rlr[plane + a], rlr[plane + b], sg);
             }
-            emit = hypot(re, im) > throut;
+            emit = E::above(vr, vi, throut);
+            if (emit && mode == 1) {  // FP64 values only for the elements written
+                re = E::val(vr);
+                im = E::val(vi);
+            }
         }
         const unsigned bal = __ballot_sync(0xffffffffu, emit);
         if (lane == 0) wsum[warp] = __popc(bal);
@@ -306,18 +336,18 @@ __global__ void __launch_bounds__(1024) k_scan_records(const EmitRec* __restrict
 // ---------------------------------------------------------------------------
 void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc, int pq0, int P,
                       const int4* items, const float* item_sign, int nitems,
-                      const double* pair_vmx, double thrgen, double* hp,
+                      const double* pair_vmx, const float* pair_thr, double thrgen, double* hp,
                       unsigned long long* kept) {
     for (int y0 = 0; y0 < nitems; y0 += 65535) {
         int ny = nitems - y0 < 65535 ? nitems - y0 : 65535;
         dim3 grid((npc + 255) / 256, ny);
         if (ff)
             k_tr_select<FFEl><<<grid, 256, 0, st>>>((const float2*)ri, m, npc, pq0, P, items,
-                                                   item_sign, y0, nitems, pair_vmx, thrgen,
-                                                   (float2*)hp, kept);
+                                                   item_sign, y0, nitems, pair_vmx, pair_thr,
+                                                   thrgen, (float2*)hp, kept);
         else
             k_tr_select<F64El><<<grid, 256, 0, st>>>(ri, m, npc, pq0, P, items, item_sign, y0,
-                                                    nitems, pair_vmx, thrgen, hp, kept);
+                                                    nitems, pair_vmx, nullptr, thrgen, hp, kept);
     }
 }
 

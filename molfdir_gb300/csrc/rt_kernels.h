@@ -107,7 +107,7 @@ void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const 
                         __nv_bfloat16* out_sl, int* out_exp);
 void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc, int pq0, int P,
                       const int4* items, const float* item_sign, int nitems,
-                      const double* pair_vmx, double thrgen, double* hp,
+                      const double* pair_vmx, const float* pair_thr, double thrgen, double* hp,
                       unsigned long long* kept);
 void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
                    const int* pidx, int nc, double* m3);
