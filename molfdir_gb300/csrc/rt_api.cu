@@ -195,15 +195,21 @@ void plan_ao(rt_ctx* c) {
 void plan_expand(rt_ctx* c, int nslices) {
     Plan& P = c->plan;
     if (P.expand_kp_slices == nslices) return;
-    P.pg_jobs.assign(P.pgroups.size(), {});
-    P.pg_a_pp.assign(P.pgroups.size(), 0);
-    P.pg_e_pp.assign(P.pgroups.size(), 0);
+    const int npg = (int)P.pgroups.size();
+    P.pg_jobs.assign(npg, {});
+    P.pg_a_pp.assign(npg, 0);
+    P.pg_e_pp.assign(npg, 0);
+    P.jb_base.assign((size_t)npg * P.nblk, -1);
+    P.jb_band.assign((size_t)npg * P.nblk, 1);
     for (auto& gg : P.g1) {
         const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk];
         const int kp = (nk + 31) / 32 * 32;
         gg.a_pp = P.pg_a_pp[gg.pg];
         gg.e_pp = P.pg_e_pp[gg.pg];
-        const int band = std::max(1, std::min(nr, (int)(204800 / (8 * nk))));
+        // bands of at most 48 KB of FP64 G_pq(r,s): several CTAs per SM
+        const int band = std::max(1, std::min(nr, (int)(49152 / (8 * nk))));
+        P.jb_base[(size_t)gg.pg * P.nblk + gg.rblk] = (int)P.pg_jobs[gg.pg].size();
+        P.jb_band[(size_t)gg.pg * P.nblk + gg.rblk] = band;
         for (int r0 = 0; r0 < nr; r0 += band) {
             ExpandJob j;
             j.rblk = gg.rblk;
@@ -219,6 +225,18 @@ void plan_expand(rt_ctx* c, int nslices) {
         P.pg_a_pp[gg.pg] += nslices ? (long long)nslices * nr * kp : (long long)nr * nk;
         P.pg_e_pp[gg.pg] += nr;
     }
+    P.pg_njobs.assign(npg, 0);
+    P.pg_bbase.assign(npg, 0);
+    long long nb = 0;
+    for (int g = 0; g < npg; ++g) {
+        P.pg_njobs[g] = (int)P.pg_jobs[g].size();
+        P.pg_bbase[g] = nb;
+        nb += (long long)P.pgroups[g].size * P.pg_njobs[g];
+    }
+    if (nb >= (1LL << 31)) throw Error(RT_ERR_DIM, "more than 2^31 expansion buckets");
+    for (int g = 0; g < npg; ++g)
+        if (P.pg_njobs[g] > 1024) throw Error(RT_ERR_DIM, "more than 1024 expansion bands per pair");
+    P.nbuckets = nb;
     P.expand_kp_slices = nslices;
 }
 
@@ -233,7 +251,8 @@ long long set_size(int cls, int i, int j, int K, bool all) {
 struct DeviceTabs {
     unsigned char* pq_read;
     int *pair_of_orig, *pair_group, *pg_start, *pg_size, *ao_block, *ao_pos, *blk_size, *g1_of,
-        *g1_kblk;
+        *g1_kblk, *jb_base, *jb_band, *pg_njobs;
+    long long* pg_bbase;
 };
 
 }  // namespace
@@ -576,12 +595,24 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = fals
         c->d_bcount = dalloc<int>(c, (size_t)P.P + 1);
         c->d_boff = dalloc<long long>(c, (size_t)P.P + 1);
     }
+    if (!c->d_jstart || c->bucket_n != P.nbuckets) {
+        dfree(c, c->d_jstart);
+        dfree(c, c->d_jcount);
+        c->d_jstart = dalloc<long long>(c, (size_t)std::max(1LL, P.nbuckets));
+        c->d_jcount = dalloc<int>(c, (size_t)std::max(1LL, P.nbuckets));
+        c->bucket_n = P.nbuckets;
+    }
+    // pq buckets: up to two entries per integral; (pq, job) buckets: four
     if (c->bucket_cap < 2 * c->n_int) {
         dfree(c, c->d_bval);
         dfree(c, c->d_brs);
+        dfree(c, c->d_jval);
+        dfree(c, c->d_jrs);
         c->bucket_cap = std::max(1LL, 2 * c->n_int);
         c->d_bval = dalloc<double>(c, (size_t)c->bucket_cap);
         c->d_brs = dalloc<int>(c, (size_t)c->bucket_cap);
+        c->d_jval = dalloc<double>(c, (size_t)2 * c->bucket_cap);
+        c->d_jrs = dalloc<int>(c, (size_t)2 * c->bucket_cap);
     }
     if (!c->d_hp) c->d_hp = dalloc<double>(c, (size_t)2 * KK1 * P.P);
     for (int cc = 0; cc < 4; ++cc) {
@@ -677,6 +708,10 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
     up(P.blk_size.data(), P.blk_size.size(), T.blk_size);
     up(g1of.data(), g1of.size(), T.g1_of);
     up(g1k.data(), g1k.size(), T.g1_kblk);
+    up(P.jb_base.data(), P.jb_base.size(), T.jb_base);
+    up(P.jb_band.data(), P.jb_band.size(), T.jb_band);
+    up(P.pg_njobs.data(), P.pg_njobs.size(), T.pg_njobs);
+    up(P.pg_bbase.data(), P.pg_bbase.size(), T.pg_bbase);
 }
 
 namespace {
@@ -760,10 +795,12 @@ void pass_bucketing(Pass& ps) {
     cudaStream_t st = ctx->stream;
     const DeviceTabs& T = ps.T;
     ScatterTabs tb{P.n, ctx->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
-                   T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk};
+                   T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk,
+                   T.jb_base, T.jb_band, T.pg_bbase, T.pg_njobs};
     launch_bucket(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, ctx->n_int, ps.d_roff, ps.d_rmeta,
                   (int)ctx->rec_off.size(), tb, P.P, ctx->d_bcount, ctx->d_boff, ctx->d_bval,
-                  ctx->d_brs, (unsigned int*)ps.d_stat);
+                  ctx->d_brs, P.nbuckets, ctx->d_jstart, ctx->d_jcount, ctx->d_jval, ctx->d_jrs,
+                  (unsigned int*)ps.d_stat);
     ps.launches += ctx->n_int > 0 ? 3 : 1;
     RT_CUDA(cudaGetLastError());
     unsigned long long hstat[8];
@@ -818,9 +855,9 @@ void pass_stage_a(Pass& ps, double thrgen) {
             if (covered < n) RT_CUDA(cudaMemsetAsync(ha, 0, 2 * plane * sizeof(double), st));
             // G_pq(r,s) of the chunk from the buckets
             if (!P.pg_jobs[g].empty()) {
-                launch_expand_rows(st, nsl, ctx->d_bval, ctx->d_brs, ctx->d_boff, d_jobs[g],
-                                   (int)P.pg_jobs[g].size(), pg.start + c0, npc, ps.T.ao_block,
-                                   ps.T.ao_pos, smem, a1, split ? split_a1_slices(ctx) : nullptr,
+                launch_expand_rows(st, nsl, ctx->d_jval, ctx->d_jrs, ctx->d_jstart, ctx->d_jcount, d_jobs[g],
+                                   P.pg_njobs[g], P.pg_bbase[g] + (long long)c0 * P.pg_njobs[g], npc,
+                                   smem, a1, split ? split_a1_slices(ctx) : nullptr,
                                    split ? split_a1_exps(ctx) : nullptr);
                 ++ps.launches;
             }
@@ -1301,9 +1338,11 @@ void batch_enqueue(rt_batch* b, bool timed) {
         RT_CUDA(cudaMemsetAsync(I.d_total, 0, 4 * sizeof(long long), ss));
         RT_CUDA(cudaMemsetAsync(I.ps->d_stat, 0, 8 * sizeof(unsigned long long), ss));
         ScatterTabs tb{P.n, c->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
-                       T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk};
+                       T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk,
+                       T.jb_base, T.jb_band, T.pg_bbase, T.pg_njobs};
         launch_bucket(ss, c->d_rint, c->d_l2, c->d_l1, c->n_int, I.ps->d_roff, I.ps->d_rmeta,
-                      (int)c->rec_off.size(), tb, P.P, c->d_bcount, c->d_boff, c->d_bval, c->d_brs,
+                      (int)c->rec_off.size(), tb, P.P, c->d_bcount, c->d_boff, c->d_bval,
+                      c->d_brs, P.nbuckets, c->d_jstart, c->d_jcount, c->d_jval, c->d_jrs,
                       (unsigned int*)I.ps->d_stat);
         L += c->n_int > 0 ? 3 : 1;
     });
@@ -1317,10 +1356,10 @@ void batch_enqueue(rt_batch* b, bool timed) {
             if (I.covered[g] < n)
                 RT_CUDA(cudaMemsetAsync(c->d_ha, 0, (size_t)2 * n * m * npc * sizeof(double), ss));
             if (!P.pg_jobs[g].empty()) {
-                launch_expand_rows(ss, c->cfg.slices, c->d_bval, c->d_brs, c->d_boff, I.d_jobs[g],
-                                   (int)P.pg_jobs[g].size(), P.pgroups[g].start, npc, I.ps->T.ao_block,
-                                   I.ps->T.ao_pos, I.jobs_smem[g], nullptr, split_a1_slices(c),
-                                   split_a1_exps(c));
+                launch_expand_rows(ss, c->cfg.slices, c->d_jval, c->d_jrs, c->d_jstart, c->d_jcount,
+                                   I.d_jobs[g],
+                                   P.pg_njobs[g], P.pg_bbase[g], npc, I.jobs_smem[g], nullptr,
+                                   split_a1_slices(c), split_a1_exps(c));
                 ++L;
             }
         });

@@ -100,6 +100,12 @@ struct Plan {
     std::vector<long long> pg_a_pp;                // operand elements per pair (all groups)
     std::vector<long long> pg_e_pp;                // row exponents per pair
     int expand_kp_slices = -1;                     // slice count the jobs were laid out for
+    // pq buckets are split by expansion job: bucket of (pair, job) =
+    // pg_bbase[pg] + (pair - pg start) * pg_njobs[pg] + job
+    std::vector<int> pg_njobs;
+    std::vector<long long> pg_bbase;
+    std::vector<int> jb_base, jb_band;             // [npg * nblk]: first job, band rows (-1: none)
+    long long nbuckets = 0;
     std::vector<Item> items;      // K(K+1) items in TRANS2 order
     std::vector<int> cls1_rank;   // record position of each item within its class stream(s)
     int n_cls1 = 0, n_cls234 = 0;
@@ -203,6 +209,12 @@ struct rt_ctx {
     double* d_qap = nullptr;     // [s_sorted][plane*m + b]     (n x 2m)
     double* d_qah = nullptr;     // [(plane',a)][(plane,r)]     (2m x 2n)
     double* d_qar[2] = {nullptr, nullptr};  // per component: [(plane,q)][(plane',k)] (2nc x 2m)
+    // second bucket level: (pq, expansion job) buckets
+    long long* d_jstart = nullptr;
+    int* d_jcount = nullptr;
+    double* d_jval = nullptr;
+    int* d_jrs = nullptr;
+    long long bucket_n = 0;  // (pq, job) buckets allocated
     double* d_ha = nullptr;
     size_t ha_len = 0;  // doubles in d_ha
     double* d_ri = nullptr;

@@ -400,20 +400,37 @@ __device__ __forceinline__ long long warp_agg_add(int* counter, int key, bool ac
     return active ? (long long)atomicAdd(&counter[key], 1) : -1;
 }
 
-// Decode integral x; returns the number of bucket entries (0..2) with their
-// pq buckets and (r,s) labels and the value.
-__device__ __forceinline__ int decode_integral(long long x, const double* __restrict__ rint,
-                                               const int* __restrict__ l2, const int* __restrict__ l1,
-                                               const long long* __restrict__ rec_off,
-                                               const int2* __restrict__ rec_meta, int nrec,
-                                               const ScatterTabs& tb, unsigned int* status,
-                                               int* pqs, int* rss, double& v) {
+// Decode integral x; returns the number of pq bucket entries (0..2) with
+// their pq buckets and packed (r, s) labels and the value.
+// record holding integral x (binary search over the record offsets)
+__device__ __forceinline__ int find_record(long long x, const long long* __restrict__ rec_off,
+                                           int nrec) {
     int lo = 0, hi = nrec - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (rec_off[mid] <= x) lo = mid; else hi = mid - 1;
     }
-    const int2 meta = rec_meta[lo];
+    return lo;
+}
+
+// Record of integral x for a warp handling 32 consecutive integrals: one
+// search by the first lane, shared when the whole warp lies in that record.
+__device__ __forceinline__ int warp_record(long long x, long long x0, long long nint,
+                                           const long long* __restrict__ rec_off, int nrec) {
+    int r0 = 0;
+    if ((threadIdx.x & 31) == 0) r0 = find_record(x0, rec_off, nrec);
+    r0 = __shfl_sync(0xffffffffu, r0, 0);
+    const long long end = r0 + 1 < nrec ? rec_off[r0 + 1] : nint;
+    if (__all_sync(0xffffffffu, x >= nint || x < end)) return r0;
+    return x < nint ? find_record(x, rec_off, nrec) : r0;
+}
+
+__device__ __forceinline__ int decode_integral(long long x, int rec, const double* __restrict__ rint,
+                                               const int* __restrict__ l2, const int* __restrict__ l1,
+                                               const int2* __restrict__ rec_meta,
+                                               const ScatterTabs& tb, unsigned int* status,
+                                               int* pqs, int* rss, double& v) {
+    const int2 meta = rec_meta[rec];
     if (meta.x < 1 || meta.x > tb.mfil) return 0;  // SORT1 reads files 1..MFIL only
     const int L2 = l2[x], L1 = l1[x];
     int a = (L2 >> 16) & 0xFFFF, b = L2 & 0xFFFF;
@@ -438,8 +455,9 @@ __device__ __forceinline__ int decode_integral(long long x, const double* __rest
         const int pg = tb.pair_group[pq];
         const int g = tb.g1_of[pg * tb.nblk + tb.ao_block[r]];
         if (g < 0 || tb.g1_kblk[g] != tb.ao_block[s]) { atomicOr(status, ST_BAD_BLOCK); return 0; }
+        if (tb.jb_base[pg * tb.nblk + tb.ao_block[s]] < 0) { atomicOr(status, ST_BAD_BLOCK); return 0; }
         pqs[ne] = pq;
-        // (block, position) of r and s: the expansion needs no table lookups
+        // (block, position) of r and s, and whether r == s
         rss[ne] = (int)(((unsigned)tb.ao_block[r] << 29) | ((unsigned)tb.ao_pos[r] << 19) |
                         ((unsigned)tb.ao_block[s] << 16) | ((unsigned)tb.ao_pos[s] << 6) |
                         (r == s ? 1u : 0u));
@@ -460,7 +478,8 @@ __global__ void __launch_bounds__(256) k_bucket_count(const double* __restrict__
         const long long x = xb + (threadIdx.x & 31);
         int pqs[2], rss[2], ne = 0;
         double v;
-        if (x < nint) ne = decode_integral(x, rint, l2, l1, rec_off, rec_meta, nrec, tb, status, pqs, rss, v);
+        const int rec = warp_record(x, xb, nint, rec_off, nrec);
+        if (x < nint) ne = decode_integral(x, rec, rint, l2, l1, rec_meta, tb, status, pqs, rss, v);
         warp_agg_add(count, ne > 0 ? pqs[0] : 0, ne > 0);
         warp_agg_add(count, ne > 1 ? pqs[1] : 0, ne > 1);
     }
@@ -479,7 +498,8 @@ __global__ void __launch_bounds__(256) k_bucket_place(const double* __restrict__
         const long long x = xb + (threadIdx.x & 31);
         int pqs[2], rss[2], ne = 0;
         double v = 0.0;
-        if (x < nint) ne = decode_integral(x, rint, l2, l1, rec_off, rec_meta, nrec, tb, status, pqs, rss, v);
+        const int rec = warp_record(x, xb, nint, rec_off, nrec);
+        if (x < nint) ne = decode_integral(x, rec, rint, l2, l1, rec_meta, tb, status, pqs, rss, v);
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
             const long long p = warp_agg_add(fill, ne > e ? pqs[e] : 0, ne > e);
@@ -493,13 +513,14 @@ __global__ void __launch_bounds__(256) k_bucket_place(const double* __restrict__
 }
 
 // exclusive scan of n ints into long long offsets (single block)
-__global__ void __launch_bounds__(1024) k_scan_counts(const int* __restrict__ cnt, int n,
+__global__ void __launch_bounds__(1024) k_scan_counts(const int* __restrict__ cnt, long long n,
                                                       long long* __restrict__ off) {
     __shared__ long long part[1024];
-    const int t = threadIdx.x, per = (n + 1023) / 1024;
-    const int a = t * per, b = min(n, a + per);
+    const int t = threadIdx.x;
+    const long long per = (n + 1023) / 1024;
+    const long long a = t * per, b = min(n, a + per);
     long long s = 0;
-    for (int i = a; i < b; ++i) s += cnt[i];
+    for (long long i = a; i < b; ++i) s += cnt[i];
     part[t] = s;
     __syncthreads();
     if (t == 0) {
@@ -508,43 +529,128 @@ __global__ void __launch_bounds__(1024) k_scan_counts(const int* __restrict__ cn
     }
     __syncthreads();
     long long o = part[t];
-    for (int i = a; i < b; ++i) { off[i] = o; o += cnt[i]; }
+    for (long long i = a; i < b; ++i) { off[i] = o; o += cnt[i]; }
     if (t == 1023) off[n] = o;
 }
 
+// Second level: one CTA per pq splits its bucket into the buckets of its
+// expansion jobs, writing each element G_pq(r,s) under the job owning row r
+// and, off the diagonal, G_pq(s,r) under the job owning row s, as
+// (row position << 16 | column position).  The output of pq occupies
+// [2 off[pq], 2 off[pq+1]); start and count of every (pq, job) bucket go to
+// jstart / jcount at pg_bbase[pg] + (pq - pg start) * njobs + job.
+constexpr int MAX_JOBS = 1024;
+
+// expansion job of a row (block, position); -1 outside the pair group's jobs
+__device__ __forceinline__ int job_of(const int* jbb, const int* jbd, int nblk, int nj, int blk,
+                                      int pos) {
+    if (blk >= nblk || jbb[blk] < 0) return -1;
+    const int j = jbb[blk] + pos / jbd[blk];
+    return j < nj ? j : -1;
+}
+
+__device__ __forceinline__ int smem_agg_add(int* ctr, int key, bool active) {
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    if (!active) return -1;
+    const unsigned peers = __match_any_sync(mask, key);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&ctr[key], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(256) k_bucket_split(const long long* __restrict__ off,
+                                                      const double* __restrict__ bval,
+                                                      const int* __restrict__ brs, ScatterTabs tb,
+                                                      long long* __restrict__ jstart,
+                                                      int* __restrict__ jcount,
+                                                      double* __restrict__ oval,
+                                                      int* __restrict__ ors) {
+    __shared__ int cnt[MAX_JOBS], cur[MAX_JOBS];
+    __shared__ int jbb[8], jbd[8];
+    const int pq = blockIdx.x;
+    const int pg = tb.pair_group[pq];
+    const int nj = tb.pg_njobs[pg];
+    const long long bb = tb.pg_bbase[pg] + (long long)(pq - tb.pg_start[pg]) * nj;
+    for (int j = threadIdx.x; j < nj; j += blockDim.x) cnt[j] = 0;
+    if (threadIdx.x < tb.nblk) {
+        jbb[threadIdx.x] = tb.jb_base[pg * tb.nblk + threadIdx.x];
+        jbd[threadIdx.x] = tb.jb_band[pg * tb.nblk + threadIdx.x];
+    }
+    __syncthreads();
+    const long long e0 = off[pq], e1 = off[pq + 1];
+    // the loops run in whole warps (the aggregated atomics use all lanes)
+    const long long n = e1 - e0, nr = (n + 31) / 32 * 32;
+    for (long long t = threadIdx.x; t < nr; t += blockDim.x) {
+        const bool on = t < n;
+        const unsigned rs = on ? (unsigned)brs[e0 + t] : 0u;
+        const int br = (int)(rs >> 29), pr = (int)((rs >> 19) & 0x3FF);
+        const int bs = (int)((rs >> 16) & 0x7), ps = (int)((rs >> 6) & 0x3FF);
+        const int j1 = on ? job_of(jbb, jbd, tb.nblk, nj, br, pr) : -1;
+        smem_agg_add(cnt, j1 >= 0 ? j1 : 0, j1 >= 0);
+        const int j2 = on && !(rs & 1u) ? job_of(jbb, jbd, tb.nblk, nj, bs, ps) : -1;
+        smem_agg_add(cnt, j2 >= 0 ? j2 : 0, j2 >= 0);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int j = 0; j < nj; ++j) {
+            jstart[bb + j] = 2 * e0 + run;
+            jcount[bb + j] = cnt[j];
+            cur[j] = run;
+            run += cnt[j];
+        }
+    }
+    __syncthreads();
+    for (long long t = threadIdx.x; t < nr; t += blockDim.x) {
+        const bool on = t < n;
+        const unsigned rs = on ? (unsigned)brs[e0 + t] : 0u;
+        const double v = on ? bval[e0 + t] : 0.0;
+        const int br = (int)(rs >> 29), pr = (int)((rs >> 19) & 0x3FF);
+        const int bs = (int)((rs >> 16) & 0x7), ps = (int)((rs >> 6) & 0x3FF);
+        const int j1 = on ? job_of(jbb, jbd, tb.nblk, nj, br, pr) : -1;
+        const int s1 = smem_agg_add(cur, j1 >= 0 ? j1 : 0, j1 >= 0);
+        if (j1 >= 0) {
+            oval[2 * e0 + s1] = v;
+            ors[2 * e0 + s1] = (pr << 16) | ps;
+        }
+        const int j2 = on && !(rs & 1u) ? job_of(jbb, jbd, tb.nblk, nj, bs, ps) : -1;
+        const int s2 = smem_agg_add(cur, j2 >= 0 ? j2 : 0, j2 >= 0);
+        if (j2 >= 0) {
+            oval[2 * e0 + s2] = v;
+            ors[2 * e0 + s2] = (ps << 16) | pr;
+        }
+    }
+}
+
 // One CTA per (job, pq of the chunk): job = (GEMM1 group, band of r rows).
-// The band of G_pq(r,s) is accumulated in shared memory from the pq bucket,
-// then written as GEMM1 operand rows: FP64 [r][pql][nk] (nslices == 0) or
-// BF16 digit slices [t][r*npc + pql][Kp] with row exponents (split path).
+// The band of G_pq(r,s) is accumulated in shared memory from the bucket of
+// (pq, job) -- exactly the elements of this band -- then written as GEMM1
+// operand rows: FP64 [r][pql][nk] (nslices == 0) or BF16 digit slices
+// [t][r*npc + pql][Kp] with row exponents (split path).
 template <int NS>
-__global__ void __launch_bounds__(512) k_expand_rows(const double* __restrict__ bval,
+__global__ void __launch_bounds__(256) k_expand_rows(const double* __restrict__ bval,
                                                      const int* __restrict__ brs,
-                                                     const long long* __restrict__ off,
-                                                     const ExpandJob* __restrict__ jobs, int pq0,
-                                                     int npc, const int* __restrict__ ao_block,
-                                                     const int* __restrict__ ao_pos,
+                                                     const long long* __restrict__ jstart,
+                                                     const int* __restrict__ jcount,
+                                                     const ExpandJob* __restrict__ jobs,
+                                                     long long bbase, int npc,
                                                      double* __restrict__ out_f64,
                                                      __nv_bfloat16* __restrict__ out_sl,
                                                      int* __restrict__ out_exp) {
     extern __shared__ double tile[];
     const ExpandJob J = jobs[blockIdx.x];
-    const int pql = blockIdx.y, pq = pq0 + pql;
+    const int pql = blockIdx.y;
     const int rows = J.r_hi - J.r_lo, nk = J.nk;
     for (int i = threadIdx.x; i < rows * nk; i += blockDim.x) tile[i] = 0.0;
     __syncthreads();
-    const long long e0 = off[pq], e1 = off[pq + 1];
+    const long long bk = bbase + (long long)pql * gridDim.x + blockIdx.x;
+    const long long e0 = jstart[bk], e1 = e0 + jcount[bk];
     for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const unsigned rs = (unsigned)brs[e];
-        const int br = (int)(rs >> 29), pr0 = (int)((rs >> 19) & 0x3FF);
-        const int bs = (int)((rs >> 16) & 0x7), ps0 = (int)((rs >> 6) & 0x3FF);
-        if (br == J.rblk) {
-            const int pr = pr0 - J.r_lo;
-            if (pr >= 0 && pr < rows) atomicAdd(&tile[pr * nk + ps0], bval[e]);
-        }
-        if (!(rs & 1u) && bs == J.rblk) {
-            const int ps = ps0 - J.r_lo;
-            if (ps >= 0 && ps < rows) atomicAdd(&tile[ps * nk + pr0], bval[e]);
-        }
+        const int rs = brs[e];
+        const int pr = (rs >> 16) - J.r_lo, ps = rs & 0xFFFF;
+        if (pr >= 0 && pr < rows && ps < nk) atomicAdd(&tile[pr * nk + ps], bval[e]);
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -587,8 +693,10 @@ __global__ void __launch_bounds__(512) k_expand_rows(const double* __restrict__ 
 
 void launch_bucket(cudaStream_t st, const double* rint, const int* l2, const int* l1, long long nint,
                    const long long* rec_off, const int2* rec_meta, int nrec, const ScatterTabs& tb,
-                   int P, int* count, long long* off, double* bval, int* brs,
+                   int P, int* count, long long* off, double* bval, int* brs, long long nb,
+                   long long* jstart, int* jcount, double* jval, int* jrs,
                    unsigned int* status) {
+    cudaMemsetAsync(jcount, 0, sizeof(int) * (nb > 0 ? nb : 1), st);
     cudaMemsetAsync(count, 0, sizeof(int) * (P + 1), st);
     if (nint > 0) {
         long long blocks = (nint + 255) / 256;
@@ -604,19 +712,21 @@ void launch_bucket(cudaStream_t st, const double* rint, const int* l2, const int
         k_bucket_place<<<(unsigned)blocks, 256, 0, st>>>(rint, l2, l1, nint, rec_off, rec_meta,
                                                          nrec, tb, off, count, bval, brs, status);
     }
+    if (nint > 0)
+        k_bucket_split<<<(unsigned)P, 256, 0, st>>>(off, bval, brs, tb, jstart, jcount, jval, jrs);
 }
 
 void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const int* brs,
-                        const long long* off, const ExpandJob* jobs, int njobs, int pq0, int npc,
-                        const int* ao_block, const int* ao_pos, size_t smem, double* out_f64,
+                        const long long* jstart, const int* jcount, const ExpandJob* jobs, int njobs,
+                        long long bbase, int npc, size_t smem, double* out_f64,
                         __nv_bfloat16* out_sl, int* out_exp) {
     dim3 grid(njobs, npc);
 #define RT_EXPAND(NSV)                                                                          \
     do {                                                                                        \
         cudaFuncSetAttribute(k_expand_rows<NSV>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                              (int)smem);                                                        \
-        k_expand_rows<NSV><<<grid, 512, smem, st>>>(bval, brs, off, jobs, pq0, npc, ao_block,   \
-                                                    ao_pos, out_f64, out_sl, out_exp);          \
+        k_expand_rows<NSV><<<grid, 256, smem, st>>>(bval, brs, jstart, jcount, jobs, bbase, npc, \
+                                                    out_f64, out_sl, out_exp);                  \
     } while (0)
     switch (nslices) {
         case 0: RT_EXPAND(0); break;

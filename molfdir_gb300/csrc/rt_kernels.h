@@ -25,6 +25,10 @@ struct ScatterTabs {
     const int* blk_size;           // [nblk]
     const int* g1_of;              // [npg*nblk] GEMM1 group of (pair group, r block) or -1
     const int* g1_kblk;            // [ng1] partner block of the group
+    const int* jb_base;            // [npg*nblk] first expansion job of (pair group, r block)
+    const int* jb_band;            // [npg*nblk] rows per band of those jobs
+    const long long* pg_bbase;     // [npg] first bucket of the pair group
+    const int* pg_njobs;           // [npg] expansion jobs per pair
 };
 
 // One MDCINT record of the current item chunk.
@@ -98,12 +102,17 @@ template <class Epi>
 void gemm_f64(cudaStream_t st, const double* A, long long lda, long long sA, const double* B,
               long long ldb, long long sB, int M, int N, int K, int batch, Epi epi);
 
+// Buckets in two levels: by pq (count, off[P+1], bval/brs, up to two
+// entries per integral), then by (pq, expansion job) (jstart/jcount[nb],
+// jval/jrs, up to four entries per integral: element and mirror).
 void launch_bucket(cudaStream_t st, const double* rint, const int* l2, const int* l1, long long nint,
                    const long long* rec_off, const int2* rec_meta, int nrec, const ScatterTabs& tb,
-                   int P, int* count, long long* off, double* bval, int* brs, unsigned int* status);
+                   int P, int* count, long long* off, double* bval, int* brs, long long nb,
+                   long long* jstart, int* jcount, double* jval, int* jrs, unsigned int* status);
+// expansion of one pair chunk: bucket of (pair pql, job j) = bbase + pql * njobs + j
 void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const int* brs,
-                        const long long* off, const ExpandJob* jobs, int njobs, int pq0, int npc,
-                        const int* ao_block, const int* ao_pos, size_t smem, double* out_f64,
+                        const long long* jstart, const int* jcount, const ExpandJob* jobs, int njobs,
+                        long long bbase, int npc, size_t smem, double* out_f64,
                         __nv_bfloat16* out_sl, int* out_exp);
 void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc, int pq0, int P,
                       const int4* items, const float* item_sign, int nitems,
