@@ -274,7 +274,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
-    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", default="precision",
                     choices=["precision", "c1", "profile", "large", "batched", "gemm"])

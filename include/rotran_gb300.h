@@ -55,7 +55,7 @@ typedef struct rt_config {
     double thrgen;    /* THRGEN (readin.F:93) */
     double throut;    /* THROUT (readin.F:94): |x| > THROUT is written to MDCINT */
     int precision;    /* RT_PREC_FP64 or RT_PREC_SPLIT_BF16 */
-    int slices;       /* split path: BF16 slices per operand, 2..6 (0: default 6) */
+    int slices;       /* split path: BF16 slices per operand, 2..6 (0: default 5) */
     int n_irrep;      /* 1, or 4: AO functions carry the labels in ao_irrep and
                          (pq|rs) vanishes unless irr(p)^irr(q) == irr(r)^irr(s) */
     const int* ao_irrep; /* NSC labels 0..n_irrep-1 (NULL when n_irrep == 1) */

@@ -400,7 +400,7 @@ extern "C" int rt_create(rt_ctx** out, const rt_config* cfg) {
     ctx->cfg = *cfg;
     if (cfg->n_irrep == 4) ctx->ao_irrep.assign(cfg->ao_irrep, cfg->ao_irrep + cfg->nsc);
     ctx->cfg.ao_irrep = nullptr;
-    if (ctx->cfg.slices == 0) ctx->cfg.slices = 6;
+    if (ctx->cfg.slices == 0) ctx->cfg.slices = 5;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();

@@ -334,7 +334,7 @@ class Rotran:
         return s
 
 
-def split_dgemm(a: np.ndarray, b: np.ndarray, slices: int = 7, mode: int = 0) -> np.ndarray:
+def split_dgemm(a: np.ndarray, b: np.ndarray, slices: int = 5, mode: int = 0) -> np.ndarray:
     """C = A B through the split-precision tensor-core engine (``rt_split_dgemm``)."""
     lib = load()
     a = np.ascontiguousarray(a, np.float64)

@@ -89,7 +89,7 @@ def fortran_ptr(gamma):
 
 FP64, SPLIT = rotran.RT_PREC_FP64, rotran.RT_PREC_SPLIT_BF16
 # relative error bounds of E and of max|dE/dC| against the FP64 reference
-TOL = {FP64: (1e-10, 1e-10), SPLIT: (2e-10, 2e-10)}
+TOL = {FP64: (1e-10, 1e-10), SPLIT: (1e-8, 1e-8)}  # split: default 5 slices
 
 
 def run_case(prob, records_on_device, seed, ndir, check_lib_fd=0, fd_tol=1e-7, precision=FP64):
