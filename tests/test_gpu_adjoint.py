@@ -89,15 +89,18 @@ def fortran_ptr(gamma):
 
 FP64, SPLIT = rotran.RT_PREC_FP64, rotran.RT_PREC_SPLIT_BF16
 # relative error bounds of E and of max|dE/dC| against the FP64 reference
-TOL = {FP64: (1e-10, 1e-10), SPLIT: (1e-8, 1e-8)}  # split: default 5 slices
+TOL = {FP64: (1e-10, 1e-10), SPLIT: (2e-10, 2e-10)}  # split: 6 slices
 
 
-def run_case(prob, records_on_device, seed, ndir, check_lib_fd=0, fd_tol=1e-7, precision=FP64):
+def run_case(prob, records_on_device, seed, ndir, check_lib_fd=0, fd_tol=1e-7, precision=FP64,
+             slices=6, tol=None, rich_tol=1e-8):
     dev = "cuda"
     m = prob.m
     gamma = make_gamma(m, seed, dev)
     gf, gptr = fortran_ptr(gamma)
-    rt = rotran.Rotran.for_problem(prob, precision=precision)
+    rt = rotran.Rotran.for_problem(prob, precision=precision,
+                                   slices=slices if precision == SPLIT else 0)
+    tol = tol or TOL[precision]
     if records_on_device:
         cls, its, nts, dv, dl2, dl1 = synth.device_records(prob, prob.mfil, device=dev)
         rt.add_records_bulk_device(cls, nts, its, dv, dl2, dl1)
@@ -122,8 +125,8 @@ def run_case(prob, records_on_device, seed, ndir, check_lib_fd=0, fd_tol=1e-7, p
           f"grad max rel {rel_g:.2e}, adjoint {st.ms_total:.1f} ms, "
           f"{st.flops_algorithmic / st.ms_total / 1e9:.3f} TFLOP/s "
           f"(stage A {st.ms_first:.1f} ms, contraction {st.ms_second:.1f} ms)")
-    assert rel_e <= TOL[precision][0]
-    assert rel_g <= TOL[precision][1]
+    assert rel_e <= tol[0]
+    assert rel_g <= tol[1]
 
     # central differences of E along random complex directions, h = 1e-5
     gen = torch.Generator(device="cpu").manual_seed(1000 + seed)
@@ -149,11 +152,13 @@ def run_case(prob, records_on_device, seed, ndir, check_lib_fd=0, fd_tol=1e-7, p
                                     prob.ikrmo, prob.imoras_pairs())
                 _, em = rt.adjoint(gptr)
                 fdl = (ep - em) / (2 * h)
-                assert abs(fdl - an) / abs(an) <= 1e-7
+                # the split path's E carries ~1e-12 relative rounding that is
+                # not smooth in C; differences divide it by h
+                assert abs(fdl - an) / abs(an) <= (1e-7 if precision == FP64 else 1e-5)
     print(f"  central differences (h = 1e-5): worst relative error {worst:.2e}, "
           f"Richardson {worst_rich:.2e}, over {ndir} directions")
     assert worst <= fd_tol
-    assert worst_rich <= 1e-8  # rounding floor: eps |E| / h relative to the derivative
+    assert worst_rich <= rich_tol  # rounding floor: eps |E| / h relative to the derivative
     rt.close()
     del gf
 
@@ -163,6 +168,13 @@ def test_adjoint_small(precision):
     prob = synth.make_problem(5, 7, 3, seed=11)
     run_case(prob, records_on_device=False, seed=1, ndir=20, check_lib_fd=3, fd_tol=1e-6,
              precision=precision)
+
+
+def test_adjoint_small_default_slices():
+    # 5 slices: errors about 2^7 larger than at 6
+    prob = synth.make_problem(5, 7, 3, seed=11)
+    run_case(prob, records_on_device=False, seed=1, ndir=10, check_lib_fd=2, fd_tol=1e-6,
+             precision=SPLIT, slices=0, tol=(5e-8, 5e-8), rich_tol=1e-7)
 
 
 @pytest.mark.parametrize("precision", [FP64, SPLIT], ids=["fp64", "split"])
