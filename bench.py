@@ -376,15 +376,24 @@ def main():
         evalt = torch.empty((nz, 2), dtype=torch.float64).pin_memory()
         eidx_np, eval_np = eidx.numpy(), evalt.numpy().view(np.complex128).reshape(-1)
 
+        phase = [0.0, 0.0, 0.0]
+
         def e2e_step():
+            a = time.perf_counter()
             rt.clear_records()
             rt.add_records_bulk_ptr(cls, nts, its, hv.data_ptr(), h2.data_ptr(), h1.data_ptr())
+            b = time.perf_counter()
             rt.transform()
+            c = time.perf_counter()
             rt.result(ehdr, eidx_np, eval_np)
+            d = time.perf_counter()
+            for i, v in enumerate((b - a, c - b, d - c)):
+                phase[i] += v
 
         e2e_step()
         barrier()
         ne = max(1, min(args.steps, 3))
+        phase[:] = [0.0, 0.0, 0.0]
         t0 = time.perf_counter()
         for _ in range(ne):
             e2e_step()
@@ -392,7 +401,9 @@ def main():
         esec = barrier_max((t1 - t0) / ne, world)
         e2e = {"value": flops * world / esec / 1e12, "unit": "TFLOP/s",
                "h2d_bytes_per_step": nint * 16, "d2h_bytes_per_step": nz * 24 + nrec * 12,
-               "ms_per_step": esec * 1e3}
+               "ms_per_step": esec * 1e3,
+               "ms_records_in": phase[0] * 1e3 / ne, "ms_transform": phase[1] * 1e3 / ne,
+               "ms_results_out": phase[2] * 1e3 / ne}
         rt.close()
         del hv, h2, h1, eidx, evalt
 

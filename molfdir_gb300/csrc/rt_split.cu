@@ -378,12 +378,11 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
                     }
                     unsigned char* base = smem + (size_t)st * stage_bytes;
                     mbar_expect_tx(&full[st], stage_bytes);
-                    for (int t = 0; t < s; ++t) {
-                        tma_load_2d(base + t * slice_a, ma, &full[st], kb * SBK,
-                                    (int)(t * g.M + r.tm * SBM));
-                        tma_load_2d(base + (size_t)s * slice_a + t * slice_b, mb, &full[st],
-                                    kb * SBK, (int)(t * g.N + r.tn * BN));
-                    }
+                    // all s slices of each operand tile in one 3D box
+                    tma_load_3d(base, ma, &full[st], kb * SBK, (int)(r.tm * SBM), 0);
+                    tma_load_3d(base + (size_t)s * slice_a, mb, &full[st], kb * SBK,
+                                (int)(r.tn * BN), 0);
+
                     issued[st] = 1 + (int)ph;  // phase parity of the outstanding load
                 }
             }
@@ -814,14 +813,17 @@ double split_flop_factor(rt_ctx* c) {
     return s * (s + 1) / 2.0;
 }
 
-static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int Kp,
+// Tensor map of an operand stored as s slices [t][rows][Kp]: one box of
+// 32 k x box_rows rows x all s slices per load, landing in shared memory as
+// s consecutive 64-byte-swizzled tiles.
+static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int Kp, int s,
                             int box_rows = SBM) {
     CUtensorMap m;
-    cuuint64_t gd[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
-    cuuint64_t gs[1] = {(cuuint64_t)Kp * 2};
-    cuuint32_t box[2] = {(cuuint32_t)SBK, (cuuint32_t)box_rows};
-    cuuint32_t es[2] = {1, 1};
-    CUresult r = S->encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), gd, gs,
+    cuuint64_t gd[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)s};
+    cuuint64_t gs[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows * Kp * 2};
+    cuuint32_t box[3] = {(cuuint32_t)SBK, (cuuint32_t)box_rows, (cuuint32_t)s};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = S->encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), gd, gs,
                            box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(RT_ERR_PROGRAM, "cuTensorMapEncodeTiled failed");
@@ -835,8 +837,8 @@ static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M,
     SplitState* S = state(c);
     if (M <= 0 || N <= 0) return;
     const int s = S->s;
-    CUtensorMap ma = make_map(S, a_sl, (long long)s * M, Kp);
-    CUtensorMap mb = make_map(S, b_sl, (long long)s * N, Kp);
+    CUtensorMap ma = make_map(S, a_sl, M, Kp, s);
+    CUtensorMap mb = make_map(S, b_sl, N, Kp, s);
     SplitArgs g;
     g.M = M;
     g.N = N;
@@ -1043,8 +1045,8 @@ void split_group_build(SplitGroup* G, rt_ctx* c0) {
             a.row_exp = q.a_exp;
             a.col_exp = q.b_exp;
             a.error = nullptr;
-            maps[2 * p] = make_map(&tmp, q.a_sl, (long long)G->s * q.M, q.Kp, SBM);
-            maps[2 * p + 1] = make_map(&tmp, q.b_sl, (long long)G->s * q.N, q.Kp, bn);
+            maps[2 * p] = make_map(&tmp, q.a_sl, q.M, q.Kp, G->s, SBM);
+            maps[2 * p + 1] = make_map(&tmp, q.b_sl, q.N, q.Kp, G->s, bn);
             start[p + 1] = start[p] + (q.M > 0 && q.N > 0 ? (long long)a.tiles_m * a.tiles_n : 0);
             if (v == 0) {
                 G->flops_exec += 2.0 * q.M * (double)q.N * q.Kp * (G->s * (G->s + 1) / 2);
@@ -1426,8 +1428,8 @@ extern "C" int rt_split_dgemm_noalloc(int M, int N, int K, const double* A, cons
         RT_CUDA(cudaGetLastError());
         SplitState S;
         S.encode = g_noalloc_encode;
-        CUtensorMap ma = make_map(&S, da, (long long)s * M, Kp);
-        CUtensorMap mb = make_map(&S, db, (long long)s * N, Kp);
+        CUtensorMap ma = make_map(&S, da, M, Kp, s);
+        CUtensorMap mb = make_map(&S, db, N, Kp, s);
         SplitArgs g;
         g.M = M;
         g.N = N;
