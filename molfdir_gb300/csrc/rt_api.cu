@@ -318,10 +318,16 @@ static void plan_items(rt_ctx* c) {
     Work& w = W(c);
     const int m = P.m, K = P.K;
     P.items.clear();
-    for (int I = 0; I < m; ++I) {
+    // TRANS2's loops over the caller's spinor numbers (trans2.F:230-239) set
+    // the record order; the items hold internal spinor indices
+    std::vector<int> u2i(m);
+    for (int i = 0; i < m; ++i) u2i[c->spin_user[i]] = i;
+    for (int Iu = 0; Iu < m; ++Iu) {
+        const int I = u2i[Iu];
         int ikr = c->ikrmo[I];
         if (ikr > 0) continue;  // records are written for barred I only
-        for (int J = 0; J < m; ++J) {
+        for (int Ju = 0; Ju < m; ++Ju) {
+            const int J = u2i[Ju];
             int jkr = c->ikrmo[J];
             if (std::abs(jkr) > std::abs(ikr)) continue;
             P.items.push_back({I, J, std::abs(ikr), std::abs(jkr), jkr < 0 ? 1 : 0});
@@ -450,15 +456,32 @@ extern "C" int rt_set_coefficients(rt_ctx* ctx, const double* qa, int ld_qa, con
             ikrmo[b - 1] != -(k + 1))
             throw Error(RT_ERR_PROGRAM, "KRA/KRB/IKRMO inconsistent with ITRMO");
     }
+    // Internal spinor order: the unbarred members KRA(1..K), then the barred
+    // members KRB(1..K).  All device work runs in this Kramers-sorted basis;
+    // MDCINT labels are Kramers indices and do not depend on it.
+    ctx->spin_user.assign(m, 0);
+    for (int q = 0; q < K; ++q) {
+        ctx->spin_user[q] = kra[q] - 1;
+        ctx->spin_user[K + q] = krb[q] - 1;
+    }
     ctx->qa.assign((size_t)2 * n * m, 0.0);
     for (int i = 0; i < m; ++i)
-        std::memcpy(&ctx->qa[(size_t)2 * i * n], qa + (size_t)2 * i * ld_qa, sizeof(double) * 2 * n);
+        std::memcpy(&ctx->qa[(size_t)2 * i * n], qa + (size_t)2 * ctx->spin_user[i] * ld_qa,
+                    sizeof(double) * 2 * n);
     for (double v : ctx->qa)
         if (!std::isfinite(v)) throw Error(RT_ERR_USER, "non-finite spinor coefficient");
-    ctx->itrmo.assign(itrmo, itrmo + m);
-    ctx->kra.assign(kra, kra + K);
-    ctx->krb.assign(krb, krb + K);
-    ctx->ikrmo.assign(ikrmo, ikrmo + m);
+    ctx->itrmo.assign(m, 0);
+    ctx->ikrmo.assign(m, 0);
+    ctx->kra.assign(K, 0);
+    ctx->krb.assign(K, 0);
+    for (int q = 0; q < K; ++q) {
+        ctx->itrmo[q] = K + q + 1;   // ITRMO(KRA) = +KRB
+        ctx->itrmo[K + q] = -(q + 1);  // ITRMO(KRB) = -KRA
+        ctx->ikrmo[q] = q + 1;
+        ctx->ikrmo[K + q] = -(q + 1);
+        ctx->kra[q] = q + 1;
+        ctx->krb[q] = K + q + 1;
+    }
     ctx->imoras.assign(2 * K, 0);
     if (imoras_pairs) ctx->imoras.assign(imoras_pairs, imoras_pairs + 2 * K);
     else
@@ -507,6 +530,24 @@ static void flush_staged(rt_ctx* c) {
     c->st_l1.clear();
 }
 
+// Copy of `bytes` split over the context's copy streams (created on first
+// use); sync_pieces waits for all of them.
+static void copy_pieces(rt_ctx* c, void* dst, const void* src, size_t bytes) {
+    const int ns = (int)(sizeof(c->cstream) / sizeof(c->cstream[0]));
+    if (!c->cstream[0])
+        for (int i = 0; i < ns; ++i) RT_CUDA(cudaStreamCreateWithFlags(&c->cstream[i], cudaStreamNonBlocking));
+    const size_t piece = std::max<size_t>((size_t)64 << 20, (bytes + ns - 1) / ns);
+    int i = 0;
+    for (size_t o = 0; o < bytes; o += piece, ++i)
+        RT_CUDA(cudaMemcpyAsync((char*)dst + o, (const char*)src + o, std::min(piece, bytes - o),
+                                cudaMemcpyDefault, c->cstream[i % ns]));
+}
+
+static void sync_pieces(rt_ctx* c) {
+    for (auto s : c->cstream)
+        if (s) RT_CUDA(cudaStreamSynchronize(s));
+}
+
 static void add_record_meta(rt_ctx* c, int file, int it, long long nt, long long off) {
     c->rec_file.push_back(file);
     c->rec_it.push_back(it);
@@ -552,10 +593,11 @@ extern "C" int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* fi
     }
     ensure_record_capacity(ctx, ctx->n_int + tot);
     if (tot > 0) {
-        RT_CUDA(cudaMemcpyAsync(ctx->d_rint + ctx->n_int, rint, tot * sizeof(double), cudaMemcpyDefault, ctx->stream));
-        RT_CUDA(cudaMemcpyAsync(ctx->d_l2 + ctx->n_int, label2, tot * sizeof(int), cudaMemcpyDefault, ctx->stream));
-        RT_CUDA(cudaMemcpyAsync(ctx->d_l1 + ctx->n_int, label1, tot * sizeof(int), cudaMemcpyDefault, ctx->stream));
-        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        // large transfers in pieces on several streams (several copy engines)
+        copy_pieces(ctx, ctx->d_rint + ctx->n_int, rint, tot * sizeof(double));
+        copy_pieces(ctx, ctx->d_l2 + ctx->n_int, label2, tot * sizeof(int));
+        copy_pieces(ctx, ctx->d_l1 + ctx->n_int, label1, tot * sizeof(int));
+        sync_pieces(ctx);
     }
     ctx->n_int += tot;
     ctx->transformed = false;
@@ -1085,7 +1127,17 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     Pass ps(ctx);
     const size_t ng = (size_t)m * m * m * m;
     double* d_gam = ps.alloc<double>(2 * ng);
-    RT_CUDA(cudaMemcpyAsync(d_gam, gamma, 2 * ng * sizeof(double), cudaMemcpyDefault, st));
+    {
+        // the density into the internal spinor order
+        double* d_tmp = ps.alloc<double>(2 * ng);
+        int* d_su = ps.upload(ctx->spin_user.data(), (size_t)m);
+        RT_CUDA(cudaMemcpyAsync(d_tmp, gamma, 2 * ng * sizeof(double), cudaMemcpyDefault, st));
+        launch_gamma_permute(st, d_tmp, d_su, m, d_gam);
+        RT_CUDA(cudaStreamSynchronize(st));
+        dfree(ctx, d_tmp);
+        ps.tmp.erase(std::find(ps.tmp.begin(), ps.tmp.end(), (void*)d_tmp));
+        ps.launches += 1;
+    }
     launch_gamma_sym(st, d_gam, m);
     ++ps.launches;
     int4* d_relk = ps.upload(relk.data(), relk.size());
@@ -1209,8 +1261,9 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
         for (int x = 0; x < m; ++x) {
             const double sr = row[x], si = row[m + x];
             const size_t o = 2 * ((size_t)p + (size_t)n * x);
-            out[o] = 4.0 * sr;
-            out[o + 1] = 4.0 * si;
+            const size_t ou = 2 * ((size_t)p + (size_t)n * ctx->spin_user[x]);  // caller's column
+            out[ou] = 4.0 * sr;
+            out[ou + 1] = 4.0 * si;
             e += ctx->qa[o] * sr + ctx->qa[o + 1] * si;
         }
     }
@@ -1727,6 +1780,11 @@ extern "C" const char* rt_last_error(rt_ctx* ctx) {
 extern "C" void rt_destroy(rt_ctx* ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto s : ctx->cstream)
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
     for (auto& a : ctx->allocs) cudaFree(a.first);
     ctx->allocs.clear();
     split_release(ctx);

@@ -175,11 +175,13 @@ struct rt_ctx {
     std::string err;
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t cstream[4] = {};  // host <-> device copies in pieces
     cudaEvent_t ev[8] = {};
     bool have_coef = false;
     // host copies of the tables
     std::vector<double> qa;   // n x m complex, column-major, interleaved
-    std::vector<int> itrmo, kra, krb, ikrmo, imoras;
+    std::vector<int> itrmo, kra, krb, ikrmo, imoras;  // in the internal spinor order
+    std::vector<int> spin_user;  // internal spinor -> caller's spinor (0-based)
     rt::Plan plan;
     rt::Stage stage;
     rt::Work work;

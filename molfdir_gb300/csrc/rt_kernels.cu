@@ -769,6 +769,24 @@ __global__ void k_gamma_sym(double2* __restrict__ g, long long M2) {
     }
 }
 
+__global__ void k_gamma_permute(const double2* __restrict__ in, const int* __restrict__ u, int m,
+                                double2* __restrict__ out) {
+    // block (j, k) of the output, looping over l, threads over i
+    const long long mm = m;
+    const int j = (int)(blockIdx.x % (unsigned)m), kk = (int)(blockIdx.x / (unsigned)m);
+    for (int l = 0; l < m; ++l) {
+        const long long src = (((long long)u[l] * mm + u[kk]) * mm + u[j]) * mm;
+        const long long dst = (((long long)l * mm + kk) * mm + j) * mm;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) out[dst + i] = in[src + u[i]];
+    }
+}
+
+void launch_gamma_permute(cudaStream_t st, const double* in, const int* u, int m, double* out) {
+    const long long nb = (long long)m * m;
+    if (nb > 0x7fffffffLL) throw_dim("adjoint: NSP too large");
+    k_gamma_permute<<<(unsigned)nb, 128, 0, st>>>((const double2*)in, u, m, (double2*)out);
+}
+
 void launch_gamma_sym(cudaStream_t st, double* gamma, int m) {
     const long long M2 = (long long)m * m;
     const long long T = (M2 + 31) / 32;

@@ -128,6 +128,8 @@ void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, in
 // Gamma <- (Gamma + Gamma^T) / 2 with Gamma seen as an m^2 x m^2 complex
 // matrix over (first pair, second pair): the pair-exchange symmetrisation.
 void launch_gamma_sym(cudaStream_t st, double* gamma, int m);
+// out(i,j,k,l) = in(u[i],u[j],u[k],u[l]) (complex, Fortran order)
+void launch_gamma_permute(cudaStream_t st, const double* in, const int* u, int m, double* out);
 // Contraction operand of one item chunk, real-ified (see k_gamma_hat).
 void launch_gamma_hat(cudaStream_t st, bool ff, const double* gamma, int m, const int4* relk,
                       const int4* relc, const int* itrmo, int i0, int nij, double* out);
