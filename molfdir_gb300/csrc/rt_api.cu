@@ -919,7 +919,7 @@ void pass_stage_a(Pass& ps, double thrgen) {
             EpiRowMajor e2{ri, (long long)m * npc, 0};
             gemm_begin();
             if (split)
-                split_gemm24(ctx, ha, 2 * n, (long long)m * npc, e2, &ps.launches);
+                split_gemm2_kramers(ctx, ha, 2 * n, (long long)m * npc, e2, &ps.launches);
             else
                 gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2), ++ps.launches;
             gemm_end(2.0 * 2 * m * (double)m * npc * 2 * n);

@@ -553,8 +553,15 @@ struct EpiFF_HA {  // GEMM1: row = r*npc + pql, col = plane*m + b -> HA[plane][r
 struct EpiFF_RowMajor {  // C[row][col], leading dimension ldc
     float2* c;
     long long ldc;
+    // optional row map: with rblk > 0, row i is output row
+    // (i / rblk) * mrow + rblk + i % rblk (the barred half of each plane);
+    // columns start at col_off
+    long long rblk = 0, mrow = 0, col_off = 0;
     typedef float2* Row;
-    __device__ __forceinline__ Row row(long long i) const { return c + i * ldc; }
+    __device__ __forceinline__ Row row(long long i) const {
+        const long long r = rblk ? (i / rblk) * mrow + rblk + i % rblk : i;
+        return c + r * ldc + col_off;
+    }
     __device__ __forceinline__ void store(Row p, long long col0, long long N, const uint32_t (&h)[EC],
                                          const uint32_t (&l)[EC]) const {
         if (col0 + EC <= N && (((uintptr_t)(p + col0)) & 15) == 0) {
@@ -616,6 +623,7 @@ struct SplitState {
     int num_sms = 152;
     // constant operands
     ConstSlices qah;                 // A of GEMM2/4: rows 2m, K = 2n
+    ConstSlices qahB;                // the barred rows of qah (both planes): rows m
     std::vector<ConstSlices> qap;    // B of GEMM1 per AO block: N = 2m, K = block size
     ConstSlices qar[2];              // B of GEMM3 per component: N = 2m, K = 2nc
     ConstSlices qc[2];               // B of the adjoint's X GEMM per component: N = 2m, K = nc
@@ -726,6 +734,15 @@ void split_prepare_constants(rt_ctx* c) {
             }
         host_slice_rows(a, 2 * m, 2 * n, kpad(2 * n), s, sl, ex);
         upload_const(S, S->qah, sl, ex, 2 * m, 2 * n);
+        // rows (plane, x) with x in the barred half [m/2, m) of the internal order
+        const int K = m / 2;
+        std::vector<double> ab((size_t)m * 2 * n);
+        for (int pl = 0; pl < 2; ++pl)
+            for (int j = 0; j < K; ++j)
+                std::memcpy(&ab[((size_t)pl * K + j) * 2 * n], &a[((size_t)pl * m + K + j) * 2 * n],
+                            sizeof(double) * 2 * n);
+        host_slice_rows(ab, m, 2 * n, kpad(2 * n), s, sl, ex);
+        upload_const(S, S->qahB, sl, ex, m, 2 * n);
     }
     // qap per AO block: B = rows s in block, cols (plane, b)
     S->qap.resize(P.nblk);
@@ -817,10 +834,11 @@ double split_flop_factor(rt_ctx* c) {
 // 32 k x box_rows rows x all s slices per load, landing in shared memory as
 // s consecutive 64-byte-swizzled tiles.
 static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int Kp, int s,
-                            int box_rows = SBM) {
+                            int box_rows = SBM, long long slice_rows = 0) {
     CUtensorMap m;
+    if (slice_rows <= 0) slice_rows = rows;  // rows between consecutive slices
     cuuint64_t gd[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)s};
-    cuuint64_t gs[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows * Kp * 2};
+    cuuint64_t gs[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)slice_rows * Kp * 2};
     cuuint32_t box[3] = {(cuuint32_t)SBK, (cuuint32_t)box_rows, (cuuint32_t)s};
     cuuint32_t es[3] = {1, 1, 1};
     CUresult r = S->encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), gd, gs,
@@ -833,12 +851,12 @@ static CUtensorMap make_map(SplitState* S, const void* base, long long rows, int
 template <class Epi>
 static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M, const void* b_sl,
                      const int* b_exp, long long N, int K, int Kp, Epi epi, int* launches,
-                     int ksplit = 1, int kcb = 0) {
+                     int ksplit = 1, int kcb = 0, long long b_slice_rows = 0) {
     SplitState* S = state(c);
     if (M <= 0 || N <= 0) return;
     const int s = S->s;
     CUtensorMap ma = make_map(S, a_sl, M, Kp, s);
-    CUtensorMap mb = make_map(S, b_sl, N, Kp, s);
+    CUtensorMap mb = make_map(S, b_sl, N, Kp, s, SBN, b_slice_rows);
     SplitArgs g;
     g.M = M;
     g.N = N;
@@ -920,6 +938,25 @@ void split_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRo
     split_prep_gemm24(c, Bsrc, K, N, c->stream, launches);
     EpiFF_RowMajor epi{(float2*)e.c, e.ldc};
     run_gemm(c, S->qah.d, S->qah.exps, S->qah.rows, S->a_sl, S->b_exp, N, K, Kp, epi, launches);
+}
+
+// GEMM2 restricted to the blocks of RI = QA^H G QA that the Kramers
+// selection reads (internal order: unbarred spinors [0, m/2), barred
+// [m/2, m)): all rows against the unbarred columns, the barred rows against
+// the barred columns; the unbarred-row x barred-column block is not formed.
+// N = m * npc columns ordered (b, pq).
+void split_gemm2_kramers(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRowMajor& e,
+                         int* launches) {
+    SplitState* S = state(c);
+    const int m = c->plan.m, Kh = m / 2, Kp = kpad(K);
+    const long long npc = N / m, nh = (long long)Kh * npc;
+    split_prep_gemm24(c, Bsrc, K, N, c->stream, launches);
+    EpiFF_RowMajor e1{(float2*)e.c, e.ldc};
+    run_gemm(c, S->qah.d, S->qah.exps, S->qah.rows, S->a_sl, S->b_exp, nh, K, Kp, e1, launches, 1, 0,
+             N);
+    EpiFF_RowMajor e2{(float2*)e.c, e.ldc, Kh, m, nh};
+    run_gemm(c, S->qahB.d, S->qahB.exps, S->qahB.rows, S->a_sl + (size_t)nh * Kp, S->b_exp + nh, nh,
+             K, Kp, e2, launches, 1, 0, N);
 }
 
 void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& e,

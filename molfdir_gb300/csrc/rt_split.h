@@ -19,6 +19,9 @@ void split_gemm24(rt_ctx* c, const double* B, int K, long long N, const EpiRowMa
                   int* launches);
 void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const EpiRK& epi,
                  int* launches);
+// GEMM2 over the RI blocks the Kramers selection reads (3/4 of the full product)
+void split_gemm2_kramers(rt_ctx* c, const double* B, int K, long long N, const EpiRowMajor& epi,
+                         int* launches);
 void split_release(rt_ctx* c);
 // operand slicing of GEMM2/4 and GEMM3 on stream st (the GEMM itself apart)
 void split_prep_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, cudaStream_t st,
