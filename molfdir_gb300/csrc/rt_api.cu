@@ -1562,7 +1562,8 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
                     if (gg.pg == (int)g)
                         split_group_add_gemm1(B->g1[g], c, gg, npc, EpiHA{c->d_ha, P.blk_start[gg.rblk], m, npc, plane});
                 double* ri = c->d_ha + (size_t)2 * n * m * I.ps->pair_chunk;
-                split_group_add_gemm24(B->g2[g], c, 2 * n, (long long)m * npc, EpiRowMajor{ri, (long long)m * npc, 0});
+                split_group_add_gemm2_kramers(B->g2[g], c, 2 * n, (long long)m * npc,
+                                              EpiRowMajor{ri, (long long)m * npc, 0});
             }
         }
         for (int cc = 0; cc < 2; ++cc) {

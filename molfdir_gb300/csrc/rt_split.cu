@@ -983,6 +983,7 @@ struct GroupProblem {
     const int* b_exp;
     long long N;
     int K, Kp;
+    long long b_slice_rows;  // rows between B slices (0: N)
 };
 
 struct SplitGroup {
@@ -1015,7 +1016,7 @@ void split_group_add_gemm1(SplitGroup* G, rt_ctx* c, const G1Group& gg, int npc,
     const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk];
     const ConstSlices& B = S->qap[gg.kblk];
     G->probs.push_back({S->a_sl + gg.a_pp * npc, S->a_exp + gg.e_pp * npc, (long long)nr * npc, B.d,
-                        B.exps, 2LL * P.m, nk, kpad(nk)});
+                        B.exps, 2LL * P.m, nk, kpad(nk), 0});
     G->e1.push_back(EpiFF_HA{(float2*)e.ha, e.r0, e.m, e.npc, e.plane});
     G->s = S->s;
 }
@@ -1023,8 +1024,21 @@ void split_group_add_gemm1(SplitGroup* G, rt_ctx* c, const G1Group& gg, int npc,
 void split_group_add_gemm24(SplitGroup* G, rt_ctx* c, int K, long long N, const EpiRowMajor& e) {
     SplitState* S = state(c);
     G->probs.push_back({S->qah.d, S->qah.exps, (long long)S->qah.rows, S->a_sl, S->b_exp, N, K,
-                        kpad(K)});
+                        kpad(K), 0});
     G->e24.push_back(EpiFF_RowMajor{(float2*)e.c, e.ldc});
+    G->s = S->s;
+}
+
+// the two launches of split_gemm2_kramers as two problems of a group
+void split_group_add_gemm2_kramers(SplitGroup* G, rt_ctx* c, int K, long long N, const EpiRowMajor& e) {
+    SplitState* S = state(c);
+    const int m = c->plan.m, Kh = m / 2, Kp = kpad(K);
+    const long long nh = (long long)Kh * (N / m);
+    G->probs.push_back({S->qah.d, S->qah.exps, (long long)S->qah.rows, S->a_sl, S->b_exp, nh, K, Kp, N});
+    G->e24.push_back(EpiFF_RowMajor{(float2*)e.c, e.ldc});
+    G->probs.push_back({S->qahB.d, S->qahB.exps, (long long)S->qahB.rows, S->a_sl + (size_t)nh * Kp,
+                        S->b_exp + nh, nh, K, Kp, N});
+    G->e24.push_back(EpiFF_RowMajor{(float2*)e.c, e.ldc, Kh, m, nh});
     G->s = S->s;
 }
 
@@ -1032,7 +1046,7 @@ void split_group_add_gemm3(SplitGroup* G, rt_ctx* c, int comp, int nc, int nij, 
     SplitState* S = state(c);
     const ConstSlices& B = S->qar[comp];
     G->probs.push_back({S->a_sl, S->a_exp, (long long)nc * nij, B.d, B.exps, 2LL * c->plan.m, 2 * nc,
-                        kpad(2 * nc)});
+                        kpad(2 * nc), 0});
     G->e3.push_back(EpiFF_RK{(float2*)e.rk, e.m, e.rowoff, e.plane});
     G->s = S->s;
 }
@@ -1083,7 +1097,7 @@ void split_group_build(SplitGroup* G, rt_ctx* c0) {
             a.col_exp = q.b_exp;
             a.error = nullptr;
             maps[2 * p] = make_map(&tmp, q.a_sl, q.M, q.Kp, G->s, SBM);
-            maps[2 * p + 1] = make_map(&tmp, q.b_sl, q.N, q.Kp, G->s, bn);
+            maps[2 * p + 1] = make_map(&tmp, q.b_sl, q.N, q.Kp, G->s, bn, q.b_slice_rows);
             start[p + 1] = start[p] + (q.M > 0 && q.N > 0 ? (long long)a.tiles_m * a.tiles_n : 0);
             if (v == 0) {
                 G->flops_exec += 2.0 * q.M * (double)q.N * q.Kp * (G->s * (G->s + 1) / 2);

@@ -35,6 +35,7 @@ SplitGroup* split_group_new(int kind);
 void split_group_add_gemm1(SplitGroup* g, rt_ctx* c, const G1Group& gg, int npc, const EpiHA& e);
 void split_group_add_gemm24(SplitGroup* g, rt_ctx* c, int K, long long N, const EpiRowMajor& e);
 void split_group_add_gemm3(SplitGroup* g, rt_ctx* c, int comp, int nc, int nij, const EpiRK& e);
+void split_group_add_gemm2_kramers(SplitGroup* g, rt_ctx* c, int K, long long N, const EpiRowMajor& e);
 void split_group_build(SplitGroup* g, rt_ctx* c0);
 void split_group_launch(SplitGroup* g, int bn, cudaStream_t st, int* err);
 int split_group_size(const SplitGroup* g);
