@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -49,6 +50,41 @@ void dfree(rt_ctx* c, void* p) {
             break;
         }
     cudaFree(p);
+}
+
+// Per-call temporaries (tables, offsets, job lists: a few dozen small arrays
+// per transform) come from a pool that keeps released blocks for the next
+// call, so a repeated transform makes no cudaMalloc / cudaFree: cudaFree
+// synchronises the device and a fresh cudaMalloc maps new pages.
+constexpr size_t POOL_BLOCK_MAX = (size_t)16 << 20, POOL_TOTAL_MAX = (size_t)128 << 20;
+
+void* tmp_alloc(rt_ctx* c, size_t bytes) {
+    if (bytes == 0) bytes = 1;
+    int best = -1;
+    for (int i = 0; i < (int)c->pool.size(); ++i) {  // smallest block that fits, at most 2x
+        const size_t b = c->pool[i].second;
+        if (b >= bytes && b <= 2 * bytes + 4096 && (best < 0 || b < c->pool[best].second)) best = i;
+    }
+    if (best < 0) return dalloc<unsigned char>(c, bytes);
+    void* p = c->pool[best].first;
+    c->pool_bytes -= c->pool[best].second;
+    c->pool.erase(c->pool.begin() + best);
+    return p;
+}
+
+// Return temporaries; `settled` says no queued work still uses them.
+void tmp_release(rt_ctx* c, const std::vector<void*>& tmp, bool settled) {
+    for (void* p : tmp) {
+        size_t bytes = 0;
+        for (auto& a : c->allocs)
+            if (a.first == p) bytes = a.second;
+        if (!settled || bytes == 0 || bytes > POOL_BLOCK_MAX || c->pool_bytes + bytes > POOL_TOTAL_MAX) {
+            dfree(c, p);
+        } else {
+            c->pool.push_back({p, bytes});
+            c->pool_bytes += bytes;
+        }
+    }
 }
 
 template <class T>
@@ -420,6 +456,8 @@ extern "C" int rt_create(rt_ctx** out, const rt_config* cfg) {
                                         prop.name);
     RT_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     for (auto& e : ctx->ev) RT_CUDA(cudaEventCreate(&e));
+    const char* trace = std::getenv("RT_TRACE");
+    ctx->trace.on = trace && *trace && std::strcmp(trace, "0") != 0;
     plan_ao(ctx);
     *out = ctx;
     return RT_OK;
@@ -668,8 +706,12 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = fals
     // work arena from the memory budget
     size_t freeb = 0, totb = 0;
     RT_CUDA(cudaMemGetInfo(&freeb, &totb));
-    long long budget = c->cfg.mem_budget > 0 ? c->cfg.mem_budget - (long long)c->dev_bytes
-                                            : (long long)(0.85 * (double)freeb);
+    // the work arena held from the previous call is given back before a
+    // resize, so it counts as free (else chunks would shrink on every call)
+    const size_t held = c->ha_len * sizeof(double) + split_work_bytes(c);
+    long long budget = c->cfg.mem_budget > 0
+                           ? c->cfg.mem_budget - (long long)c->dev_bytes + (long long)c->ha_len * 8
+                           : (long long)(0.85 * (double)(freeb + held));
     const int S = c->cfg.precision == RT_PREC_SPLIT_BF16 ? c->cfg.slices : 0;
     // bytes per pair of stage A and per item of stage B
     long long a_pp = 0;
@@ -701,12 +743,16 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = fals
     size_t need_b = (size_t)((per_item - (S ? split_stageB_bytes_per_item(c) : 0)) * item_chunk / 8) + 64;
     size_t need = std::max(need_a, need_b);
     if (!c->d_ha || c->stage.pair_chunk != pair_chunk || c->stage.item_chunk != item_chunk) {
+        // both old arenas go before either new one is allocated
         dfree(c, c->d_ha);
+        c->d_ha = nullptr;
+        c->ha_len = 0;
+        c->stage.pair_chunk = c->stage.item_chunk = 0;
+        if (S) split_alloc_work(c, pair_chunk, item_chunk);
         c->d_ha = dalloc<double>(c, need);
         c->ha_len = need;
         c->stage.pair_chunk = pair_chunk;
         c->stage.item_chunk = item_chunk;
-        if (S) split_alloc_work(c, pair_chunk, item_chunk);
     }
 }
 
@@ -716,7 +762,7 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
     Plan& P = c->plan;
     auto up = [&](auto* hostp, size_t count, auto*& devp) {
         using TT = std::remove_const_t<std::remove_pointer_t<decltype(hostp)>>;
-        TT* d = dalloc<TT>(c, count);
+        TT* d = static_cast<TT*>(tmp_alloc(c, count * sizeof(TT)));
         if (count) RT_CUDA(cudaMemcpyAsync(d, hostp, count * sizeof(TT), cudaMemcpyHostToDevice, c->stream));
         devp = d;
         tmp.push_back(d);
@@ -777,11 +823,13 @@ struct Pass {
     bool split = false;
     explicit Pass(rt_ctx* ctx) : c(ctx) {}
     ~Pass() {
-        for (void* p : tmp) dfree(c, p);
+        // kernels of this pass may still be queued (an error path, or a batch
+        // whose launches ran on other streams); pooled blocks must be idle
+        tmp_release(c, tmp, cudaDeviceSynchronize() == cudaSuccess);
     }
     template <class T>
     T* alloc(size_t count) {
-        T* p = dalloc<T>(c, count);
+        T* p = static_cast<T*>(tmp_alloc(c, count * sizeof(T)));
         tmp.push_back(p);
         return p;
     }
@@ -845,6 +893,7 @@ void pass_bucketing(Pass& ps) {
                   (unsigned int*)ps.d_stat);
     ps.launches += ctx->n_int > 0 ? 3 : 1;
     RT_CUDA(cudaGetLastError());
+    ctx->trace.mark("bucketing kernels");
     unsigned long long hstat[8];
     RT_CUDA(cudaMemcpyAsync(hstat, ps.d_stat, sizeof(hstat), cudaMemcpyDeviceToHost, st));
     RT_CUDA(cudaStreamSynchronize(st));
@@ -853,6 +902,7 @@ void pass_bucketing(Pass& ps) {
     if (hstat[0] & ST_BAD_BLOCK)
         throw Error(RT_ERR_USER, "integral outside the (LL|LL)/(SS|LL)/(SS|SS) or irrep block structure");
     RT_CUDA(cudaMemsetAsync(ps.d_stat, 0, 8 * sizeof(unsigned long long), st));
+    ctx->trace.mark("bucketing status check");
 }
 
 // First half-transformation (TRANS1 + MTIMHER + TROUT) into the resident
@@ -866,6 +916,7 @@ void pass_stage_a(Pass& ps, double thrgen) {
     const bool split = ps.split;
     const int pair_chunk = ps.pair_chunk;
     KTimer& kt = ctx->ktimer;
+    PhaseTrace& tr = ctx->trace;
     // the FP64 GEMMs are timed here; the split path times its tensor-core
     // kernels itself (rt_split.cu), without the slicing kernels around them
     auto gemm_begin = [&]() { if (!split) kt.begin(); };
@@ -880,6 +931,7 @@ void pass_stage_a(Pass& ps, double thrgen) {
     }
     const int nsl = split ? ctx->cfg.slices : 0;
     float* d_pthr = pass_pair_thr(ps, thrgen);
+    tr.mark("A: job and threshold tables");
     double* ha = ctx->d_ha;
     double* ri = ha + (size_t)2 * n * m * pair_chunk;
     double* a1 = ri + (size_t)2 * m * m * pair_chunk;  // FP64 GEMM1 operand (plain path)
@@ -903,6 +955,7 @@ void pass_stage_a(Pass& ps, double thrgen) {
                                    split ? split_a1_exps(ctx) : nullptr);
                 ++ps.launches;
             }
+            tr.mark("A: expand G_pq(r,s)");
             for (auto& gg : P.g1) {
                 if (gg.pg != (int)g) continue;
                 const int nr = P.blk_size[gg.rblk], nk = P.blk_size[gg.kblk];
@@ -916,6 +969,7 @@ void pass_stage_a(Pass& ps, double thrgen) {
                              nr, epi), ++ps.launches;
                 gemm_end(2.0 * npc * 2.0 * m * nk * nr);
             }
+            tr.mark("A: GEMM1");
             EpiRowMajor e2{ri, (long long)m * npc, 0};
             gemm_begin();
             if (split)
@@ -923,9 +977,11 @@ void pass_stage_a(Pass& ps, double thrgen) {
             else
                 gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2), ++ps.launches;
             gemm_end(2.0 * 2 * m * (double)m * npc * 2 * n);
+            tr.mark("A: slice HA + GEMM2");
             launch_tr_select(st, split, ri, m, npc, pg.start + c0, P.P, ps.d_items, ps.d_isign, KK1,
                              ps.d_pvmx, d_pthr, thrgen, ctx->d_hp, ps.d_stat + 1);
             ps.launches += (KK1 + 65534) / 65535;
+            tr.mark("A: Kramers selection");
         }
     }
     RT_CUDA(cudaGetLastError());
@@ -959,11 +1015,16 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     const int KK1 = (int)P.items.size();
     KTimer& kt = ctx->ktimer;
     kt.reset(st);
+    PhaseTrace& tr = ctx->trace;
+    tr.reset(st);
+    tr.mark("start");
     RT_CUDA(cudaEventRecord(ctx->ev[0], st));
     flush_staged(ctx);
     RT_CUDA(cudaEventRecord(ctx->ev[1], st));
+    tr.mark("staged records");
     Pass ps(ctx);
     pass_setup(ps);
+    tr.mark("tables and work arena");
     const bool split = ps.split;
     auto gemm_begin = [&]() { if (!split) kt.begin(); };
     auto gemm_end = [&](double fl) { if (!split) kt.end(fl, fl); };
@@ -978,6 +1039,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     // ---- stage A: first half-transformation (TRANS1) per pair chunk ----
     pass_stage_a(ps, ctx->cfg.thrgen);
     RT_CUDA(cudaEventRecord(ctx->ev[3], st));
+    tr.mark("stage A tail");
     // ---- stage B: second half-transformation (TRANS2) + PPSYM per item chunk ----
     double* m3 = ctx->d_ha;
     int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
@@ -1001,6 +1063,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             if (nc == 0) continue;
             launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, m3);
             ++ps.launches;
+            tr.mark("B: expand M_ij(p,q)");
             EpiRK e3{rk, m, (long long)P.comp_off[cc] * nij, rkplane};
             gemm_begin();
             if (split)
@@ -1008,6 +1071,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             else
                 gemm_f64(st, m3, 2 * nc, 0, ctx->d_qar[cc], 2 * m, 0, nc * nij, 2 * m, 2 * nc, 1, e3), ++ps.launches;
             gemm_end(2.0 * nc * (double)nij * 2 * m * 2 * nc);
+            tr.mark("B: GEMM3");
         }
         EpiRowMajor e4{rlr, (long long)nij * m, 0};
         gemm_begin();
@@ -1016,6 +1080,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         else
             gemm_f64(st, ctx->d_qah, 2 * n, 0, rk, (long long)nij * m, 0, 2 * m, nij * m, 2 * n, 1, e4), ++ps.launches;
         gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
+        tr.mark("B: slice RK + GEMM4");
         // MDCINT selection for the records of this chunk
         chunk_recs.assign(w.recs.begin() + w.item_rec0[i0], w.recs.begin() + w.item_rec0[i0 + nij]);
         for (int t = i0; t < i0 + nij; ++t)
@@ -1027,6 +1092,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         ps.launches += 3;
         // the host copy of chunk_recs must outlive the async copy
         RT_CUDA(cudaStreamSynchronize(st));
+        tr.mark("B: MDCINT selection");
     }
     RT_CUDA(cudaGetLastError());
     RT_CUDA(cudaEventRecord(ctx->ev[4], st));
@@ -1065,6 +1131,8 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     S.flops_gemm_executed = kt.flops;
     S.flops_gemm_algorithmic = kt.alg;
     ctx->transformed = true;
+    tr.mark("counts read back");
+    tr.print("rt_transform");
     API_CATCH
 }
 
@@ -1117,6 +1185,8 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     build_relatives(ctx, relk, relc);
     KTimer& kt = ctx->ktimer;
     kt.reset(st);
+    ctx->trace.reset(st);
+    ctx->trace.mark("start");
     RT_CUDA(cudaEventRecord(ctx->ev[0], st));
     flush_staged(ctx);
     // the work arena is sized again beside the density
@@ -1269,6 +1339,8 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     }
     RT_CUDA(cudaMemcpy(dedc, out.data(), out.size() * sizeof(double), cudaMemcpyDefault));
     if (energy) *energy = e;
+    ctx->trace.mark("dE/dC to the caller");
+    ctx->trace.print("rt_adjoint");
     float ms[5];
     for (int q = 0; q < 5; ++q) RT_CUDA(cudaEventElapsedTime(&ms[q], ctx->ev[q], ctx->ev[q + 1]));
     rt_stats& S = ctx->stats;

@@ -32,6 +32,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <chrono>
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -167,6 +169,51 @@ struct KTimer {
     }
 };
 
+// Phase trace of a transform, on when RT_TRACE is set (and not "0") at
+// rt_create: events on the context stream at each mark give the device time
+// between marks, a steady clock the host time at which each mark was issued.
+// Printed to stderr after the call, like rotran's per-step timing lines.
+struct PhaseTrace {
+    bool on = false;
+    cudaStream_t st = nullptr;
+    std::vector<cudaEvent_t> ev;
+    std::vector<const char*> what;
+    std::vector<double> host_ms;
+    std::chrono::steady_clock::time_point t0;
+    void reset(cudaStream_t s) {
+        st = s;
+        what.clear();
+        host_ms.clear();
+        t0 = std::chrono::steady_clock::now();
+    }
+    void mark(const char* w) {
+        if (!on) return;
+        const size_t i = what.size();
+        if (i == ev.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            ev.push_back(e);
+        }
+        cudaEventRecord(ev[i], st);
+        what.push_back(w);
+        host_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+    }
+    void print(const char* title) const {
+        if (!on || what.size() < 2) return;
+        cudaEventSynchronize(ev[what.size() - 1]);
+        std::fprintf(stderr, "rotran-gb300 %s trace: phase, device ms since the previous mark, host ms at the mark\n",
+                     title);
+        for (size_t i = 1; i < what.size(); ++i) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[i - 1], ev[i]);
+            std::fprintf(stderr, "  %-34s %10.3f %10.3f\n", what[i], ms, host_ms[i]);
+        }
+    }
+    ~PhaseTrace() {
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+};
+
 }  // namespace rt
 
 struct rt_ctx {
@@ -187,6 +234,7 @@ struct rt_ctx {
     rt::Work work;
     rt::SplitState* split = nullptr;
     rt::KTimer ktimer;
+    rt::PhaseTrace trace;
     // records
     std::vector<int> rec_file, rec_it;
     std::vector<long long> rec_off, rec_nt;
@@ -240,6 +288,9 @@ struct rt_ctx {
     rt_stats stats{};
     size_t dev_bytes = 0, dev_peak = 0;
     std::vector<std::pair<void*, size_t>> allocs;
+    // released per-call temporaries kept for the next call (still in allocs)
+    std::vector<std::pair<void*, size_t>> pool;
+    size_t pool_bytes = 0;
     bool transformed = false;
     unsigned long long gen = 0;  // input generation (coefficients, records)
 };

@@ -815,15 +815,23 @@ void split_alloc_work(rt_ctx* c, int pair_chunk, int item_chunk) {
                             (size_t)ncmax * item_chunk, (size_t)P.m * item_chunk});
     sfree(S, S->a_sl);
     sfree(S, S->a_exp);
+    sfree(S, S->b_exp);
+    S->a_sl = nullptr;
+    S->a_exp = S->b_exp = nullptr;
+    S->a_cap = S->a_exp_cap = S->b_exp_cap = 0;
     S->a_sl = (__nv_bfloat16*)salloc(S, bytes);  // A and B slices share the arena in turn
     S->a_cap = bytes;
     S->a_exp = (int*)salloc(S, rows * sizeof(int));
     S->a_exp_cap = rows;
-    sfree(S, S->b_exp);
     S->b_exp = (int*)salloc(S, rows * sizeof(int));
     S->b_exp_cap = rows;
 }
 
+
+size_t split_work_bytes(rt_ctx* c) {
+    const SplitState* S = c->split;
+    return S ? S->a_cap + (S->a_exp_cap + S->b_exp_cap) * sizeof(int) : 0;
+}
 
 double split_flop_factor(rt_ctx* c) {
     const int s = c->cfg.slices;

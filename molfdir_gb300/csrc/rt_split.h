@@ -11,6 +11,8 @@ void split_prepare_constants(rt_ctx* c);
 double split_stageA_bytes_per_pair(rt_ctx* c);
 double split_stageB_bytes_per_item(rt_ctx* c);
 void split_alloc_work(rt_ctx* c, int pair_chunk, int item_chunk);
+// bytes the work arena of split_alloc_work holds now (0 before the first)
+size_t split_work_bytes(rt_ctx* c);
 // GEMM1 operand buffers the bucket expansion fills (slices, row exponents)
 __nv_bfloat16* split_a1_slices(rt_ctx* c);
 int* split_a1_exps(rt_ctx* c);

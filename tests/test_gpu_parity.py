@@ -40,7 +40,7 @@ def test_fp64_small(nl, ns, nkr, mfil, seed):
 
 
 def test_fp64_config1_n64_k32():
-    """BASELINE config 1: 24 L + 40 S functions, 32 Kramers pairs, seed 0."""
+    """The CPU-sized case: 24 L + 40 S functions, 32 Kramers pairs, seed 0."""
     p = synth.make_problem(24, 40, 32, seed=0)
     img, ref = ref_stream(p)
     got, st = run_gpu(p)
