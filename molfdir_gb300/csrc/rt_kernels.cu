@@ -413,6 +413,9 @@ __device__ __forceinline__ int find_record(long long x, const long long* __restr
     return lo;
 }
 
+// warp strips of 32 integrals each thread of the record scans takes at once
+constexpr int SCAN_U = 2;
+
 // Record of integral x for a warp handling 32 consecutive integrals: one
 // search by the first lane, shared when the whole warp lies in that record.
 __device__ __forceinline__ int warp_record(long long x, long long x0, long long nint,
@@ -425,14 +428,29 @@ __device__ __forceinline__ int warp_record(long long x, long long x0, long long 
     return x < nint ? find_record(x, rec_off, nrec) : r0;
 }
 
-__device__ __forceinline__ int decode_integral(long long x, int rec, const double* __restrict__ rint,
-                                               const int* __restrict__ l2, const int* __restrict__ l1,
-                                               const int2* __restrict__ rec_meta,
+// The record words of one integral, loaded ahead of its decoding.
+struct RecWords {
+    double v;
+    int L2, L1;
+};
+
+__device__ __forceinline__ RecWords load_words(long long x, long long nint, const double* __restrict__ rint,
+                                               const int* __restrict__ l2, const int* __restrict__ l1) {
+    RecWords w{0.0, 0, 0};
+    if (x < nint) {
+        w.v = rint[x];
+        w.L2 = l2[x];
+        w.L1 = l1[x];
+    }
+    return w;
+}
+
+__device__ __forceinline__ int decode_integral(const RecWords& w, int rec, const int2* __restrict__ rec_meta,
                                                const ScatterTabs& tb, unsigned int* status,
                                                int* pqs, int* rss, double& v) {
     const int2 meta = rec_meta[rec];
     if (meta.x < 1 || meta.x > tb.mfil) return 0;  // SORT1 reads files 1..MFIL only
-    const int L2 = l2[x], L1 = l1[x];
+    const int L2 = w.L2, L1 = w.L1;
     int a = (L2 >> 16) & 0xFFFF, b = L2 & 0xFFFF;
     int c = (L1 >> 16) & 0xFFFF, d = L1 & 0xFFFF;
     if (a < 1 || b < 1 || c < 1 || d < 1 || a > tb.n || b > tb.n || c > tb.n || d > tb.n || d > c) {
@@ -444,7 +462,7 @@ __device__ __forceinline__ int decode_integral(long long x, int rec, const doubl
     const int cdo = c * (c + 1) / 2 + d;
     if (!tb.pq_read[cdo]) return 0;  // INDPQ(pq) == 0: never transformed
     const int coinc = (pa == pb) + (c == d) + (pa == c && pb == d);
-    v = rint[x] * gettw_factor(meta.y) * (double)(1 << coinc);
+    v = w.v * gettw_factor(meta.y) * (double)(1 << coinc);
     const int abo = pa * (pa + 1) / 2 + pb;
     int ne = 0;
     for (int dir = 0; dir < 2; ++dir) {
@@ -474,14 +492,23 @@ __global__ void __launch_bounds__(256) k_bucket_count(const double* __restrict__
                                                       unsigned int* __restrict__ status) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long base0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
-    for (long long xb = base0; xb < nint; xb += stride) {
-        const long long x = xb + (threadIdx.x & 31);
-        int pqs[2], rss[2], ne = 0;
-        double v;
-        const int rec = warp_record(x, xb, nint, rec_off, nrec);
-        if (x < nint) ne = decode_integral(x, rec, rint, l2, l1, rec_meta, tb, status, pqs, rss, v);
-        warp_agg_add(count, ne > 0 ? pqs[0] : 0, ne > 0);
-        warp_agg_add(count, ne > 1 ? pqs[1] : 0, ne > 1);
+    // SCAN_U warp strips per iteration, their record words loaded together
+    for (long long xb = base0; xb < nint; xb += SCAN_U * stride) {
+        RecWords w[SCAN_U];
+#pragma unroll
+        for (int u = 0; u < SCAN_U; ++u) w[u] = load_words(xb + u * stride + (threadIdx.x & 31), nint, rint, l2, l1);
+#pragma unroll
+        for (int u = 0; u < SCAN_U; ++u) {
+            const long long xs = xb + u * stride;  // the same for the whole warp
+            if (xs >= nint) break;
+            const long long x = xs + (threadIdx.x & 31);
+            int pqs[2], rss[2], ne = 0;
+            double v;
+            const int rec = warp_record(x, xs, nint, rec_off, nrec);
+            if (x < nint) ne = decode_integral(w[u], rec, rec_meta, tb, status, pqs, rss, v);
+            warp_agg_add(count, ne > 0 ? pqs[0] : 0, ne > 0);
+            warp_agg_add(count, ne > 1 ? pqs[1] : 0, ne > 1);
+        }
     }
 }
 
@@ -494,19 +521,27 @@ __global__ void __launch_bounds__(256) k_bucket_place(const double* __restrict__
                                                       int* __restrict__ brs, unsigned int* __restrict__ status) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long base0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
-    for (long long xb = base0; xb < nint; xb += stride) {
-        const long long x = xb + (threadIdx.x & 31);
-        int pqs[2], rss[2], ne = 0;
-        double v = 0.0;
-        const int rec = warp_record(x, xb, nint, rec_off, nrec);
-        if (x < nint) ne = decode_integral(x, rec, rint, l2, l1, rec_meta, tb, status, pqs, rss, v);
+    for (long long xb = base0; xb < nint; xb += SCAN_U * stride) {
+        RecWords w[SCAN_U];
 #pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const long long p = warp_agg_add(fill, ne > e ? pqs[e] : 0, ne > e);
-            if (ne > e) {
-                const long long o = off[pqs[e]] + p;
-                bval[o] = v;
-                brs[o] = rss[e];
+        for (int u = 0; u < SCAN_U; ++u) w[u] = load_words(xb + u * stride + (threadIdx.x & 31), nint, rint, l2, l1);
+#pragma unroll
+        for (int u = 0; u < SCAN_U; ++u) {
+            const long long xs = xb + u * stride;  // the same for the whole warp
+            if (xs >= nint) break;
+            const long long x = xs + (threadIdx.x & 31);
+            int pqs[2], rss[2], ne = 0;
+            double v = 0.0;
+            const int rec = warp_record(x, xs, nint, rec_off, nrec);
+            if (x < nint) ne = decode_integral(w[u], rec, rec_meta, tb, status, pqs, rss, v);
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const long long p = warp_agg_add(fill, ne > e ? pqs[e] : 0, ne > e);
+                if (ne > e) {
+                    const long long o = off[pqs[e]] + p;
+                    bval[o] = v;
+                    brs[o] = rss[e];
+                }
             }
         }
     }
@@ -540,6 +575,8 @@ __global__ void __launch_bounds__(1024) k_scan_counts(const int* __restrict__ cn
 // [2 off[pq], 2 off[pq+1]); start and count of every (pq, job) bucket go to
 // jstart / jcount at pg_bbase[pg] + (pq - pg start) * njobs + job.
 constexpr int MAX_JOBS = 1024;
+// entries each thread loads ahead in the bucket loops (memory-level parallelism)
+constexpr int SPLIT_U = 4, EXPAND_U = 8;
 
 // expansion job of a row (block, position); -1 outside the pair group's jobs
 __device__ __forceinline__ int job_of(const int* jbb, const int* jbd, int nblk, int nj, int blk,
@@ -580,17 +617,28 @@ __global__ void __launch_bounds__(256) k_bucket_split(const long long* __restric
     }
     __syncthreads();
     const long long e0 = off[pq], e1 = off[pq + 1];
-    // the loops run in whole warps (the aggregated atomics use all lanes)
+    // the loops run in whole warps (the aggregated atomics use all lanes);
+    // each thread loads SPLIT_U entries before it files any of them
     const long long n = e1 - e0, nr = (n + 31) / 32 * 32;
-    for (long long t = threadIdx.x; t < nr; t += blockDim.x) {
-        const bool on = t < n;
-        const unsigned rs = on ? (unsigned)brs[e0 + t] : 0u;
-        const int br = (int)(rs >> 29), pr = (int)((rs >> 19) & 0x3FF);
-        const int bs = (int)((rs >> 16) & 0x7), ps = (int)((rs >> 6) & 0x3FF);
-        const int j1 = on ? job_of(jbb, jbd, tb.nblk, nj, br, pr) : -1;
-        smem_agg_add(cnt, j1 >= 0 ? j1 : 0, j1 >= 0);
-        const int j2 = on && !(rs & 1u) ? job_of(jbb, jbd, tb.nblk, nj, bs, ps) : -1;
-        smem_agg_add(cnt, j2 >= 0 ? j2 : 0, j2 >= 0);
+    const long long step = (long long)SPLIT_U * blockDim.x;
+    for (long long t0 = threadIdx.x; t0 < nr; t0 += step) {
+        unsigned rsu[SPLIT_U];
+#pragma unroll
+        for (int u = 0; u < SPLIT_U; ++u) {
+            const long long t = t0 + (long long)u * blockDim.x;
+            rsu[u] = t < n ? (unsigned)brs[e0 + t] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < SPLIT_U; ++u) {
+            const bool on = t0 + (long long)u * blockDim.x < n;
+            const unsigned rs = rsu[u];
+            const int br = (int)(rs >> 29), pr = (int)((rs >> 19) & 0x3FF);
+            const int bs = (int)((rs >> 16) & 0x7), ps = (int)((rs >> 6) & 0x3FF);
+            const int j1 = on ? job_of(jbb, jbd, tb.nblk, nj, br, pr) : -1;
+            smem_agg_add(cnt, j1 >= 0 ? j1 : 0, j1 >= 0);
+            const int j2 = on && !(rs & 1u) ? job_of(jbb, jbd, tb.nblk, nj, bs, ps) : -1;
+            smem_agg_add(cnt, j2 >= 0 ? j2 : 0, j2 >= 0);
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -603,23 +651,34 @@ __global__ void __launch_bounds__(256) k_bucket_split(const long long* __restric
         }
     }
     __syncthreads();
-    for (long long t = threadIdx.x; t < nr; t += blockDim.x) {
-        const bool on = t < n;
-        const unsigned rs = on ? (unsigned)brs[e0 + t] : 0u;
-        const double v = on ? bval[e0 + t] : 0.0;
-        const int br = (int)(rs >> 29), pr = (int)((rs >> 19) & 0x3FF);
-        const int bs = (int)((rs >> 16) & 0x7), ps = (int)((rs >> 6) & 0x3FF);
-        const int j1 = on ? job_of(jbb, jbd, tb.nblk, nj, br, pr) : -1;
-        const int s1 = smem_agg_add(cur, j1 >= 0 ? j1 : 0, j1 >= 0);
-        if (j1 >= 0) {
-            oval[2 * e0 + s1] = v;
-            ors[2 * e0 + s1] = (pr << 16) | ps;
+    for (long long t0 = threadIdx.x; t0 < nr; t0 += step) {
+        unsigned rsu[SPLIT_U];
+        double vu[SPLIT_U];
+#pragma unroll
+        for (int u = 0; u < SPLIT_U; ++u) {
+            const long long t = t0 + (long long)u * blockDim.x;
+            rsu[u] = t < n ? (unsigned)brs[e0 + t] : 0u;
+            vu[u] = t < n ? bval[e0 + t] : 0.0;
         }
-        const int j2 = on && !(rs & 1u) ? job_of(jbb, jbd, tb.nblk, nj, bs, ps) : -1;
-        const int s2 = smem_agg_add(cur, j2 >= 0 ? j2 : 0, j2 >= 0);
-        if (j2 >= 0) {
-            oval[2 * e0 + s2] = v;
-            ors[2 * e0 + s2] = (ps << 16) | pr;
+#pragma unroll
+        for (int u = 0; u < SPLIT_U; ++u) {
+            const bool on = t0 + (long long)u * blockDim.x < n;
+            const unsigned rs = rsu[u];
+            const double v = vu[u];
+            const int br = (int)(rs >> 29), pr = (int)((rs >> 19) & 0x3FF);
+            const int bs = (int)((rs >> 16) & 0x7), ps = (int)((rs >> 6) & 0x3FF);
+            const int j1 = on ? job_of(jbb, jbd, tb.nblk, nj, br, pr) : -1;
+            const int s1 = smem_agg_add(cur, j1 >= 0 ? j1 : 0, j1 >= 0);
+            if (j1 >= 0) {
+                oval[2 * e0 + s1] = v;
+                ors[2 * e0 + s1] = (pr << 16) | ps;
+            }
+            const int j2 = on && !(rs & 1u) ? job_of(jbb, jbd, tb.nblk, nj, bs, ps) : -1;
+            const int s2 = smem_agg_add(cur, j2 >= 0 ? j2 : 0, j2 >= 0);
+            if (j2 >= 0) {
+                oval[2 * e0 + s2] = v;
+                ors[2 * e0 + s2] = (ps << 16) | pr;
+            }
         }
     }
 }
@@ -646,11 +705,23 @@ __global__ void __launch_bounds__(256) k_expand_rows(const double* __restrict__ 
     for (int i = threadIdx.x; i < rows * nk; i += blockDim.x) tile[i] = 0.0;
     __syncthreads();
     const long long bk = bbase + (long long)pql * gridDim.x + blockIdx.x;
-    const long long e0 = jstart[bk], e1 = e0 + jcount[bk];
-    for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const int rs = brs[e];
-        const int pr = (rs >> 16) - J.r_lo, ps = rs & 0xFFFF;
-        if (pr >= 0 && pr < rows && ps < nk) atomicAdd(&tile[pr * nk + ps], bval[e]);
+    const long long e0 = jstart[bk], ne = jcount[bk];
+    // EXPAND_U entries per thread are loaded before any is added, so their
+    // global loads overlap instead of one latency per entry
+    for (long long b = threadIdx.x; b < ne; b += (long long)EXPAND_U * blockDim.x) {
+        int rs[EXPAND_U];
+        double v[EXPAND_U];
+#pragma unroll
+        for (int u = 0; u < EXPAND_U; ++u) {
+            const long long i = b + (long long)u * blockDim.x;
+            rs[u] = i < ne ? brs[e0 + i] : -1;
+            v[u] = i < ne ? bval[e0 + i] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < EXPAND_U; ++u) {
+            const int pr = (rs[u] >> 16) - J.r_lo, ps = rs[u] & 0xFFFF;
+            if (rs[u] >= 0 && pr >= 0 && pr < rows && ps < nk) atomicAdd(&tile[pr * nk + ps], v[u]);
+        }
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
