@@ -162,6 +162,57 @@ def run_gemm_case(args, rank):
                           "seconds_per_call_with_host_work": dt}))
 
 
+def run_files_case(args, rank):
+    """Integral input from files at n = 160 (64 L + 96 S AOs), 40 Kramers
+    pairs, 2.27e7 integrals: the serial SRTTW/SRTLB files (SORT1's input)
+    and the MPI version's pq-sorted SRTPQIL files of 4 ranks (GETPQ's
+    input), each read into a context (host parse + upload) and transformed
+    on the split path; the two MDCINT streams must agree."""
+    import tempfile
+    from molfdir_gb300 import fortio, rotran, synth
+    if rank != 0:
+        return
+    prob = synth.make_problem(64, 96, 40, seed=0)
+    nint = int(prob.flat_records()[3].size)
+    out = {"workload": "files_n160_k40", "integrals": nint, "steps": args.steps,
+           "warmup": args.warmup}
+    results = {}
+    with tempfile.TemporaryDirectory() as d:
+        fortio.write_srt_files(prob, d)
+        fortio.write_srtpq_files(prob, d, nranks=4)
+        names = sorted(os.listdir(d))
+        for fmt, files in (("srt", [f for f in names if f.startswith("SRTTW") or f.startswith("SRTLB")]),
+                           ("srtpq", [f for f in names if f.startswith("SRTPQ")])):
+            nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in files)
+            rd, tr = [], []
+            for step in range(args.warmup + args.steps):
+                rt = rotran.Rotran.for_problem(prob, precision=rotran.RT_PREC_SPLIT_BF16,
+                                               slices=args.slices)
+                rt.set_problem_coefficients(prob)
+                t0 = time.perf_counter()
+                if fmt == "srt":
+                    rt.read_srt_files(d)
+                else:
+                    rt.read_srtpq_files(d, nranks=4)
+                t1 = time.perf_counter()
+                rt.transform()
+                t2 = time.perf_counter()
+                if step >= args.warmup:
+                    rd.append(t1 - t0)
+                    tr.append(t2 - t1)
+                results[fmt] = rt.result()
+                rt.close()
+            r = statistics.median(rd)
+            out[fmt] = {"file_bytes": nbytes, "read_s": r, "read_GBps": nbytes / r / 1e9,
+                        "read_Mintegrals_per_s": nint / r / 1e6,
+                        "transform_s_incl_staged_upload": statistics.median(tr)}
+    a, b = results["srt"], results["srtpq"]
+    same = np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    out["same_records_and_elements"] = bool(same)
+    out["max_abs_diff"] = float(np.max(np.abs(a[2] - b[2]))) if same and a[2].size else None
+    print(json.dumps(out))
+
+
 def run_batched(args, rank, world, local, bf16_peak, peak_kind):
     """48 independent transforms of uneven size (n_AO ~ U[40,200], 60% small
     component, 16..80 Kramers pairs, seeds 0..47): split precision as one
@@ -277,7 +328,7 @@ def main():
     ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "c1", "profile", "large", "batched", "gemm"])
+                    choices=["precision", "c1", "profile", "large", "batched", "gemm", "files"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -287,6 +338,8 @@ def main():
         return run_batched(args, rank, world, local, bf16_peak, peak_kind)
     if args.workload == "gemm":
         return run_gemm_case(args, rank)
+    if args.workload == "files":
+        return run_files_case(args, rank)
     work = {"precision": WORKLOAD, "c1": SMALL, "profile": PROFILE, "large": LARGE}[args.workload]
 
     if args.impl == "reference":

@@ -124,6 +124,30 @@ int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* file_class, c
  * 1..MFIL, as SORT1 does (sort1.F:118-205). */
 int rt_read_srt_files(rt_ctx* ctx, const char* dir);
 
+/* Read the MPI version's pq-sorted integral files of ranks 0..nranks-1
+ * from directory dir (replaces GETPQ's input, getpq.F:57-125, and its set-up
+ * in rotran.par.F:430-506): SRTPQLN[.r], one sequential record LRECCO,
+ * IRECL, ILSTA, ILEND, ISSTA, ISEND; SRTPQIL[.r], LRECCO direct-access
+ * records of IRECL bytes, each IPQL, NT, INXT, RBUF(NT) real*8,
+ * LBUF(NT) I<<16|K (32-bit layout, mfdtwoe.par.F:344-352,919-926).  Rank
+ * 0's files have no suffix.  Every record is read once: the INXT links must
+ * chain each stream's records, newest first.  Records of an SL pq pair
+ * (Breit) are skipped; each other entry is the integral (I K | pq) of type
+ * INTTYP with the larger pair first (getpq.F:81-96), added as by
+ * rt_add_ao_records (file class from the L/S types of the two pairs). */
+int rt_read_srtpq_files(rt_ctx* ctx, const char* dir, int nranks);
+
+/* No counterpart in the reference: the same parse without a context or a
+ * device, for checks and tools.  nsc/nsc1 as in rt_config.  On return
+ * *nrec = records (one per file class and type, at most 42) and *nint =
+ * integrals; if *nint > cap, returns RT_ERR_DIM and copies nothing (call
+ * with cap = 0 to size the arrays).  Otherwise fills file_class, itype, nt
+ * (nrec entries) and rint, label2, label1 (nint entries).  Errors: message
+ * in rt_last_error(NULL). */
+int rt_srtpq_scan(const char* dir, int nranks, int nsc, int nsc1, long long cap, long long* nrec,
+                  long long* nint, int* file_class, int* itype, long long* nt, double* rint,
+                  int* label2, int* label1);
+
 /* Drop all records added so far (a new integral set, same sizes). */
 int rt_clear_ao_records(rt_ctx* ctx);
 

@@ -1869,6 +1869,9 @@ extern "C" void rt_destroy(rt_ctx* ctx) {
 
 int rt_internal_mfil(rt_ctx* c) { return c->cfg.mfil; }
 int rt_internal_nkr(rt_ctx* c) { return c->cfg.nkr; }
+int rt_internal_nsc(rt_ctx* c) { return c->cfg.nsc; }
+int rt_internal_nsc1(rt_ctx* c) { return c->cfg.nsc1; }
+void rt_internal_set_thread_error(const char* msg) { rt::set_thread_error(msg); }
 const int* rt_internal_imoras(rt_ctx* c) { return c->imoras.data(); }
 void rt_internal_set_error(rt_ctx* c, const char* msg) { c->err = msg; }
 

@@ -19,6 +19,7 @@ from . import build as _build
 
 RT_PREC_FP64 = 0
 RT_PREC_SPLIT_BF16 = 1
+RT_ERR_EOF, RT_ERR_USER, RT_ERR_DIM = 1, 2, 3
 
 ERROR_CLASSES = {
     1: "end of file / missing data",
@@ -83,7 +84,8 @@ EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_transform", "rt_result_sizes", "rt_copy_result", "rt_write_mdcint",
            "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm",
            "rt_split_dgemm_noalloc", "rt_adjoint", "rt_batch_create", "rt_batch_run",
-           "rt_batch_get_stats", "rt_batch_last_error", "rt_batch_destroy"]
+           "rt_batch_get_stats", "rt_batch_last_error", "rt_batch_destroy", "rt_srtpq_scan",
+           "rt_read_srtpq_files"]
 
 _lib = None
 
@@ -131,6 +133,10 @@ def load(build: bool = True):
     lib.rt_batch_last_error.restype = C.c_char_p
     lib.rt_batch_destroy.argtypes = [vp]
     lib.rt_batch_destroy.restype = None
+    lib.rt_srtpq_scan.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_longlong,
+                                  P(C.c_longlong), P(C.c_longlong), P(C.c_int), P(C.c_int),
+                                  P(C.c_longlong), P(C.c_double), P(C.c_int), P(C.c_int)]
+    lib.rt_read_srtpq_files.argtypes = [vp, C.c_char_p, C.c_int]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy", "rt_batch_last_error", "rt_batch_destroy"):
@@ -283,6 +289,10 @@ class Rotran:
     def read_srt_files(self, directory):
         self._check(self.lib.rt_read_srt_files(self.h, os.fsencode(directory)))
 
+    def read_srtpq_files(self, directory, nranks=1):
+        """The MPI version's pq-sorted files SRTPQIL[.r]/SRTPQLN[.r], r < nranks."""
+        self._check(self.lib.rt_read_srtpq_files(self.h, os.fsencode(directory), nranks))
+
     def clear_records(self):
         self._check(self.lib.rt_clear_ao_records(self.h))
 
@@ -332,6 +342,39 @@ class Rotran:
         s = RtStats()
         self._check(self.lib.rt_get_stats(self.h, C.byref(s)))
         return s
+
+
+def srtpq_scan(directory, nranks: int, nsc: int, nsc1: int):
+    """Parse SRTPQIL[.r]/SRTPQLN[.r] (r < nranks) without a context or GPU.
+
+    Returns ``(file_class, itype, nt, rint, label2, label1)``: one record
+    per (file class, integral type), the integrals as ``rt_add_ao_records``
+    takes them (label1 = the stream's pq pair, label2 = the entry's label).
+    """
+    lib = load()
+    nrec, nint = C.c_longlong(), C.c_longlong()
+    d = os.fsencode(directory)
+    rc = lib.rt_srtpq_scan(d, nranks, nsc, nsc1, 0, C.byref(nrec), C.byref(nint),
+                           None, None, None, None, None, None)
+    if rc == 0 and nint.value == 0:
+        z = np.zeros(0)
+        return (z.astype(np.int32), z.astype(np.int32), z.astype(np.int64), z,
+                z.astype(np.int32), z.astype(np.int32))
+    if rc not in (0, RT_ERR_DIM):
+        raise RotranError(rc, lib.rt_last_error(None).decode(errors="replace"))
+    nr, ni = nrec.value, nint.value
+    cls = np.empty(nr, np.int32)
+    its = np.empty(nr, np.int32)
+    nts = np.empty(nr, np.int64)
+    v = np.empty(ni, np.float64)
+    l2 = np.empty(ni, np.int32)
+    l1 = np.empty(ni, np.int32)
+    rc = lib.rt_srtpq_scan(d, nranks, nsc, nsc1, ni, C.byref(nrec), C.byref(nint),
+                           _p(cls, C.c_int), _p(its, C.c_int), _p(nts, C.c_longlong),
+                           _p(v, C.c_double), _p(l2, C.c_int), _p(l1, C.c_int))
+    if rc:
+        raise RotranError(rc, lib.rt_last_error(None).decode(errors="replace"))
+    return cls, its, nts, v, l2, l1
 
 
 def split_dgemm(a: np.ndarray, b: np.ndarray, slices: int = 5, mode: int = 0) -> np.ndarray:

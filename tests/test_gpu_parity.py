@@ -94,6 +94,27 @@ def test_per_record_calls_and_srt_files_match_bulk(tmp_path):
         assert np.max(np.abs(other[2] - bulk[2])) <= 1e-15
 
 
+@pytest.mark.parametrize("precision", [rotran.RT_PREC_FP64, rotran.RT_PREC_SPLIT_BF16],
+                         ids=["fp64", "split"])
+def test_srtpq_files_match_the_oracle(tmp_path, precision):
+    """The MPI version's pq-sorted files (three ranks, short records, repeated
+    entries, Breit streams to skip) give the serial files' result."""
+    p = synth.make_problem(7, 9, 4, seed=19)
+    img, ref = ref_stream(p)
+    fortio.write_srtpq_files(p, str(tmp_path), nranks=3, nbuf=24, split_every=4, breit_pairs=3)
+    with rotran.Rotran.for_problem(p, precision=precision) as rt:
+        rt.set_problem_coefficients(p)
+        rt.read_srtpq_files(str(tmp_path), nranks=3)
+        rt.transform()
+        got = rt.result()
+        st = rt.stats()
+    fp64 = precision == rotran.RT_PREC_FP64
+    tol = TOL_FP64 if fp64 else 1e-10
+    assert compare_streams(got, ref, tol) <= tol
+    if fp64:
+        assert list(st.nfinal) == [int(x) for x in img.nfinal]
+
+
 def test_mdcint_file(tmp_path):
     p = synth.make_problem(6, 8, 4, seed=16)
     with rotran.Rotran.for_problem(p) as rt:
