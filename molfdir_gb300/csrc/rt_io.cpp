@@ -4,12 +4,15 @@
 // written by INITTWOE/PPSYM/EXITTWOE (gfortran sequential unformatted
 // records with 4-byte length markers), and the KRAMERS pairing check.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/rotran_gb300.h"
@@ -56,21 +59,28 @@ int write_record(FILE* f, const std::vector<const void*>& parts, const std::vect
     return 0;
 }
 
-// INTTYP (inttyp.F:1-79): index-coincidence type 1..14 of (i j | k l) with
-// the larger pair first.
-int inttyp(int i, int j, int k, int l) {
-    if (k > j) {
-        if (j > l) return i != k ? 13 : 10;
-        if (j != l) return k != l ? 14 : 8;
-        return i != k ? 11 : 2;
+// INTTYP (inttyp.F:1-79), the index-coincidence type 1..14 of (i j | k l)
+// with the larger pair first, as a table over the seven comparisons its
+// decision tree reads: bit 0 k>j, 1 j>l, 2 i!=k, 3 j!=l, 4 k!=l, 5 i!=j, 6 j!=k.
+struct InttypTable {
+    unsigned char t[128];
+    InttypTable() {
+        for (int x = 0; x < 128; ++x) {
+            const bool kgj = x & 1, jgl = x & 2, ik = x & 4, jl = x & 8, kl = x & 16, ij = x & 32,
+                       jk = x & 64;
+            int r;
+            if (kgj) r = jgl ? (ik ? 13 : 10) : jl ? (kl ? 14 : 8) : (ik ? 11 : 2);
+            else if (kl) r = ij ? (jk ? 12 : 9) : (jk ? 5 : 4);
+            else r = jk ? (ij ? 7 : 3) : (ij ? 6 : 1);
+            t[x] = (unsigned char)r;
+        }
     }
-    if (k != l) {
-        if (i != j) return j != k ? 12 : 9;
-        return j != k ? 5 : 4;
+    int operator()(int i, int j, int k, int l) const {
+        return t[(k > j) | (j > l) << 1 | (i != k) << 2 | (j != l) << 3 | (k != l) << 4 |
+                 (i != j) << 5 | (j != k) << 6];
     }
-    if (j != k) return i != j ? 7 : 3;
-    return i != j ? 6 : 1;
-}
+};
+const InttypTable inttyp_table;
 
 // ---------------------------------------------------------------------------
 // parallel-format input: SRTPQIL[.r] / SRTPQLN[.r]
@@ -89,7 +99,28 @@ struct SrtpqGroup {
 
 struct SrtpqSet {
     SrtpqGroup g[3][14];  // [class 1..3][type 1..14]
-    long long streams = 0, records = 0, breit_records = 0;
+};
+
+// The entries of one block of records, grouped: group g = 14*(class-1) +
+// type-1 occupies [start[g], start[g+1]) of v / l2 / l1 -- the layout of
+// rt_add_ao_records_bulk with one record per non-empty group.
+struct SrtpqBlock {
+    // storage grows but is never value-initialised (every slot is written)
+    template <class T>
+    struct Buf {
+        std::unique_ptr<T[]> p;
+        size_t cap = 0;
+        void reserve(size_t n) {
+            if (n > cap) {
+                p.reset(new T[n]);
+                cap = n;
+            }
+        }
+        T* data() const { return p.get(); }
+    };
+    Buf<double> v;
+    Buf<int> l2, l1;
+    long long start[43] = {};
 };
 
 std::string rank_name(const char* dir, const char* base, int r) {
@@ -98,15 +129,69 @@ std::string rank_name(const char* dir, const char* base, int r) {
     return s;
 }
 
+// Header of one record after the chain checks: its pq pair, or skip.
+struct SrtpqRec {
+    int ip = 0, iq = 0, nt = 0;
+    bool skip = true;
+};
+
+// Decode the entries of records [r0, r1) of a block, calling
+// f(group, value, label2, label1) in file order; group = 14*(class-1)+type-1.
+// Returns an error text, or an empty string.
+template <class F>
+std::string srtpq_decode(const char* block, int irecl, const SrtpqRec* hd, long long r0, long long r1,
+                         int nsc, int nsc1, F&& f) {
+    for (long long k = r0; k < r1; ++k) {
+        const SrtpqRec& h = hd[k];
+        if (h.skip) continue;
+        const char* vals = block + k * (long long)irecl + 12;
+        const char* labs = vals + 8 * (size_t)h.nt;
+        const bool pq_s = h.ip > nsc1;  // an LL or SS pair
+        const int32_t l1 = (h.ip << 16) | h.iq;
+        for (int e = 0; e < h.nt; ++e) {
+            double v;
+            int32_t lab;
+            std::memcpy(&v, vals + 8 * (size_t)e, 8);
+            std::memcpy(&lab, labs + 4 * (size_t)e, 4);
+            const int a = (lab >> 16) & 0xFFFF, b = lab & 0xFFFF;
+            if (a < 1 || b < 1 || a > nsc || b > nsc) return "label outside 1..NSC";
+            const bool rs_s = a > nsc1;
+            if (rs_s != (b > nsc1)) return "mixed L/S label pair in a Coulomb stream";
+            // getpq.F:92-96: the type with the larger pair first
+            const bool first = a > h.ip || (a == h.ip && b >= h.iq);
+            const int it = first ? inttyp_table(a, b, h.ip, h.iq) : inttyp_table(h.ip, h.iq, a, b);
+            const int cls = (pq_s && rs_s) ? 3 : (pq_s || rs_s) ? 2 : 1;
+            f(14 * (cls - 1) + it - 1, v, lab, l1);
+        }
+    }
+    return std::string();
+}
+
+// Run fn(w, r0, r1) on t threads over [0, nb) (the calling thread takes the last part).
+template <class F>
+void srtpq_parallel(int t, long long nb, F&& fn) {
+    std::vector<std::thread> pool;
+    for (int w = 0; w + 1 < t; ++w) pool.emplace_back([&, w] { fn(w, nb * w / t, nb * (w + 1) / t); });
+    fn(t - 1, nb * (t - 1) / t, nb);
+    for (auto& th : pool) th.join();
+}
+
 // Read the files of ranks 0..nranks-1 (rotran.par.F:430-506, getpq.F:57-125).
-// Records are taken in file order; the chains GETPQ follows (INXT links,
-// newest first) are checked to partition the records into one chain per
-// pq stream, so every record is read exactly once, as GETPQ reads it.
-void srtpq_read(const char* dir, int nranks, int nsc, int nsc1, SrtpqSet& out) {
+// Records are taken in file order, in blocks: the headers and the chains
+// GETPQ follows (INXT links, newest first) are checked sequentially -- the
+// links must partition the records into one chain per pq stream, so every
+// record is read exactly once, as GETPQ reads it -- then the entries of a
+// block are decoded by several threads, each over a contiguous record range,
+// and appended in file order.
+template <class Sink>
+void srtpq_read(const char* dir, int nranks, int nsc, int nsc1, Sink&& sink) {
     if (!dir || nranks < 1 || nranks > 999 || nsc < 1 || nsc > 65535 || nsc1 < 0 || nsc1 > nsc)
         throw SrtpqError{RT_ERR_USER, "rt_srtpq: bad arguments"};
     const long long npair = (long long)nsc * (nsc + 1) / 2;
+    const int nthr = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     std::vector<char> rec;
+    SrtpqBlock out;
+    SrtpqBlock::Buf<char> block;  // file bytes of a block of records
     for (int r = 0; r < nranks; ++r) {
         const std::string pln = rank_name(dir, "SRTPQLN", r), pil = rank_name(dir, "SRTPQIL", r);
         File fl(fopen(pln.c_str(), "rb")), fi(fopen(pil.c_str(), "rb"));
@@ -129,60 +214,81 @@ void srtpq_read(const char* dir, int nranks, int nsc, int nsc1, SrtpqSet& out) {
         if (fseek(fi.f, 0, SEEK_SET) != 0) throw SrtpqError{RT_ERR_EOF, "cannot rewind " + pil};
         std::vector<int32_t> ipql(lrecco + 1, 0);
         std::vector<char> linked(lrecco + 1, 0);
-        std::vector<char> buf((size_t)irecl);
-        for (long long k = 1; k <= lrecco; ++k) {
-            const long long pos = (k - 1) * (long long)irecl;
-            const size_t want = (size_t)std::min<long long>(irecl, fsize - pos);
-            if (pos + 12 > fsize || fread(buf.data(), 1, want, fi.f) != want)
-                throw SrtpqError{RT_ERR_EOF, "READ ERROR ON FILE SRTPQIL.*: " + pil + " record " +
-                                                 std::to_string(k)};
-            int32_t h[3];
-            std::memcpy(h, buf.data(), 12);
-            const int32_t pq = h[0], nt = h[1], nxt = h[2];
-            if (pq < 1 || pq > npair || nt < 0 || nt > nbuf || 12 + 12 * (size_t)nt > want)
-                throw SrtpqError{RT_ERR_USER, "bad record header in " + pil + " record " + std::to_string(k)};
-            // a link goes to an earlier record of the same stream, and at most
-            // one record links to any record (one chain per stream)
-            if (nxt < 0 || nxt >= k || (nxt > 0 && (linked[nxt] || ipql[nxt] != pq)))
-                throw SrtpqError{RT_ERR_USER, "broken record chain in " + pil + " at record " +
-                                                  std::to_string(k)};
-            ipql[k] = pq;
-            if (nxt > 0) linked[nxt] = 1;
-            else ++out.streams;
-            ++out.records;
-            // the pq pair of the stream (getpq.F:66-67), p >= q
-            int ip = (int)(0.5 + 0.5 * std::sqrt(8.0 * pq - 7.0));
-            while ((long long)ip * (ip - 1) / 2 >= pq) --ip;
-            while ((long long)(ip + 1) * ip / 2 < pq) ++ip;
-            const int iq = (int)(pq - (long long)ip * (ip - 1) / 2);
-            // Breit records (an SL pq pair) are not Coulomb input (getpq.F:69-75)
-            if (ip >= issta && iq <= ilend && nsc > nsc1) {
-                ++out.breit_records;
-                continue;
-            }
-            const bool pq_s = ip > nsc1;  // an LL or SS pair from here on
-            const char* vals = buf.data() + 12;
-            const char* labs = vals + 8 * (size_t)nt;
-            for (int e = 0; e < nt; ++e) {
-                double v;
-                int32_t lab;
-                std::memcpy(&v, vals + 8 * (size_t)e, 8);
-                std::memcpy(&lab, labs + 4 * (size_t)e, 4);
-                const int a = (lab >> 16) & 0xFFFF, b = lab & 0xFFFF;
-                if (a < 1 || b < 1 || a > nsc || b > nsc)
-                    throw SrtpqError{RT_ERR_USER, "label outside 1..NSC in " + pil + " record " +
+        const long long per_block = std::max(1LL, (64LL << 20) / irecl);
+        std::vector<SrtpqRec> hd;
+        for (long long k0 = 1; k0 <= lrecco; k0 += per_block) {
+            const long long nb = std::min(per_block, lrecco - k0 + 1);
+            const long long pos = (k0 - 1) * (long long)irecl;
+            // the last record may end short of IRECL
+            const long long want = std::min<long long>(nb * (long long)irecl, fsize - pos);
+            block.reserve((size_t)nb * irecl);
+            if (want < (nb - 1) * (long long)irecl + 12 ||
+                fread(block.data(), 1, (size_t)want, fi.f) != (size_t)want)
+                throw SrtpqError{RT_ERR_EOF, "READ ERROR ON FILE SRTPQIL.*: " + pil + " records " +
+                                                 std::to_string(k0) + ".." + std::to_string(k0 + nb - 1)};
+            hd.assign((size_t)nb, SrtpqRec{});
+            for (long long i = 0; i < nb; ++i) {
+                const long long k = k0 + i;
+                int32_t h[3];
+                std::memcpy(h, block.data() + i * irecl, 12);
+                const int32_t pq = h[0], nt = h[1], nxt = h[2];
+                if (pq < 1 || pq > npair || nt < 0 || nt > nbuf ||
+                    i * (long long)irecl + 12 + 12LL * nt > want)
+                    throw SrtpqError{RT_ERR_USER, "bad record header in " + pil + " record " + std::to_string(k)};
+                // a link goes to an earlier record of the same stream, and at
+                // most one record links to any record (one chain per stream)
+                if (nxt < 0 || nxt >= k || (nxt > 0 && (linked[nxt] || ipql[nxt] != pq)))
+                    throw SrtpqError{RT_ERR_USER, "broken record chain in " + pil + " at record " +
                                                       std::to_string(k)};
-                const bool rs_s = a > nsc1;
-                if (rs_s != (b > nsc1))
-                    throw SrtpqError{RT_ERR_USER, "mixed L/S label pair in a Coulomb stream of " + pil};
-                // getpq.F:92-96: the type with the larger pair first
-                const int it = (a > ip || (a == ip && b >= iq)) ? inttyp(a, b, ip, iq) : inttyp(ip, iq, a, b);
-                const int cls = (pq_s && rs_s) ? 3 : (pq_s || rs_s) ? 2 : 1;
-                SrtpqGroup& g = out.g[cls - 1][it - 1];
-                g.v.push_back(v);
-                g.l2.push_back(lab);
-                g.l1.push_back((ip << 16) | iq);
+                ipql[k] = pq;
+                if (nxt > 0) linked[nxt] = 1;
+                // the pq pair of the stream (getpq.F:66-67), p >= q
+                int ip = (int)(0.5 + 0.5 * std::sqrt(8.0 * pq - 7.0));
+                while ((long long)ip * (ip - 1) / 2 >= pq) --ip;
+                while ((long long)(ip + 1) * ip / 2 < pq) ++ip;
+                const int iq = (int)(pq - (long long)ip * (ip - 1) / 2);
+                SrtpqRec& x = hd[(size_t)i];
+                x.ip = ip;
+                x.iq = iq;
+                x.nt = nt;
+                // Breit records (an SL pq pair) are not Coulomb input (getpq.F:69-75)
+                x.skip = ip >= issta && iq <= ilend && nsc > nsc1;
             }
+            // count per thread and group, grow the groups once, then write
+            // each thread's entries at its offsets (file order is kept)
+            const int t = (int)std::min<long long>(nthr, std::max(1LL, nb / 64));
+            std::vector<std::array<long long, 42>> cnt((size_t)t), off((size_t)t);
+            std::vector<std::string> errs((size_t)t);
+            srtpq_parallel(t, nb, [&](int w, long long a, long long b) {
+                cnt[w].fill(0);
+                errs[w] = srtpq_decode(block.data(), irecl, hd.data(), a, b, nsc, nsc1,
+                                       [&](int g, double, int32_t, int32_t) { ++cnt[w][g]; });
+            });
+            for (int w = 0; w < t; ++w)
+                if (!errs[w].empty()) throw SrtpqError{RT_ERR_USER, errs[w] + " in " + pil};
+            long long base = 0;
+            for (int g = 0; g < 42; ++g) {
+                out.start[g] = base;
+                for (int w = 0; w < t; ++w) {
+                    off[w][g] = base;
+                    base += cnt[w][g];
+                }
+            }
+            out.start[42] = base;
+            out.v.reserve((size_t)base);  // reused from block to block
+            out.l2.reserve((size_t)base);
+            out.l1.reserve((size_t)base);
+            srtpq_parallel(t, nb, [&](int w, long long a, long long b) {
+                std::array<long long, 42> o = off[w];
+                srtpq_decode(block.data(), irecl, hd.data(), a, b, nsc, nsc1,
+                             [&](int g, double v, int32_t l2, int32_t l1) {
+                                 const long long x = o[g]++;
+                                 out.v.data()[x] = v;
+                                 out.l2.data()[x] = l2;
+                                 out.l1.data()[x] = l1;
+                             });
+            });
+            if (base > 0) sink(out);
         }
     }
 }
@@ -196,7 +302,15 @@ extern "C" int rt_srtpq_scan(const char* dir, int nranks, int nsc, int nsc1, lon
     try {
         if (!nrec || !nint) throw SrtpqError{RT_ERR_USER, "rt_srtpq_scan: null count pointers"};
         SrtpqSet s;
-        srtpq_read(dir, nranks, nsc, nsc1, s);
+        srtpq_read(dir, nranks, nsc, nsc1, [&](const SrtpqBlock& b) {
+            for (int g = 0; g < 42; ++g) {
+                SrtpqGroup& G = s.g[g / 14][g % 14];
+                const long long a = b.start[g], e = b.start[g + 1];
+                G.v.insert(G.v.end(), b.v.data() + a, b.v.data() + e);
+                G.l2.insert(G.l2.end(), b.l2.data() + a, b.l2.data() + e);
+                G.l1.insert(G.l1.end(), b.l1.data() + a, b.l1.data() + e);
+            }
+        });
         long long nr = 0, ni = 0;
         for (auto& c : s.g)
             for (auto& g : c)
@@ -230,26 +344,27 @@ extern "C" int rt_srtpq_scan(const char* dir, int nranks, int nsc, int nsc1, lon
     }
 }
 
-// The MPI rotran's input (GETPQ) into a context: one record per (class, type).
+// The MPI rotran's input (GETPQ) into a context, streamed: each block of
+// records goes to the device as one record per (class, type) it holds.
 extern "C" int rt_read_srtpq_files(rt_ctx* ctx, const char* dir, int nranks) {
     if (!ctx) return RT_ERR_USER;
     try {
-        SrtpqSet s;
-        srtpq_read(dir, nranks, rt_internal_nsc(ctx), rt_internal_nsc1(ctx), s);
-        for (int c = 0; c < 3; ++c)
-            for (int t = 0; t < 14; ++t) {
-                SrtpqGroup& g = s.g[c][t];
-                if (g.v.empty()) continue;
-                const int cls = c + 1, it = t + 1;
-                const long long n = (long long)g.v.size();
-                const int rc = rt_add_ao_records_bulk(ctx, 1, &cls, &n, &it, g.v.data(), g.l2.data(),
-                                                      g.l1.data());
-                if (rc) return rc;
-                std::vector<double>().swap(g.v);
-                std::vector<int>().swap(g.l2);
-                std::vector<int>().swap(g.l1);
-            }
-        return RT_OK;
+        int rc = RT_OK;
+        srtpq_read(dir, nranks, rt_internal_nsc(ctx), rt_internal_nsc1(ctx), [&](const SrtpqBlock& b) {
+            if (rc) return;
+            int cls[42], it[42];
+            long long nt[42];
+            long long nr = 0;
+            for (int g = 0; g < 42; ++g)
+                if (b.start[g + 1] > b.start[g]) {
+                    cls[nr] = g / 14 + 1;
+                    it[nr] = g % 14 + 1;
+                    nt[nr] = b.start[g + 1] - b.start[g];
+                    ++nr;
+                }
+            rc = rt_add_ao_records_bulk(ctx, nr, cls, nt, it, b.v.data(), b.l2.data(), b.l1.data());
+        });
+        return rc;
     } catch (const SrtpqError& e) {
         rt_internal_set_error(ctx, e.msg.c_str());
         return e.code;
