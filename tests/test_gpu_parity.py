@@ -5,7 +5,7 @@ import pytest
 
 import pyoracle
 from molfdir_gb300 import fortio, rotran, synth
-from util import compare_streams, permute_spinors
+from util import check_rdtwo_reconstruction, compare_streams, dense_full, permute_spinors
 
 pytestmark = pytest.mark.gpu
 
@@ -113,6 +113,21 @@ def test_srtpq_files_match_the_oracle(tmp_path, precision):
     assert compare_streams(got, ref, tol) <= tol
     if fp64:
         assert list(st.nfinal) == [int(x) for x in img.nfinal]
+
+
+@pytest.mark.parametrize("precision", [rotran.RT_PREC_FP64, rotran.RT_PREC_SPLIT_BF16],
+                         ids=["fp64", "split"])
+def test_stream_reconstructs_the_tensor_as_a_reader_does(precision):
+    """The GPU's MDCINT stream, expanded as goscip's RDTWO expands it
+    (rdtwo.F:29-83), gives the whole dense (ij|kl): every quadruple reached,
+    every implied value consistent."""
+    p = permute_spinors(synth.make_problem(5, 7, 4, seed=20),
+                        np.random.default_rng(3).permutation(8))
+    (hdr, idx, val), _ = run_gpu(p, precision=precision)
+    dense = dense_full(p)
+    scale = max(1.0, float(np.abs(dense).max()))
+    tol = (TOL_FP64 if precision == rotran.RT_PREC_FP64 else 1e-10) * scale
+    check_rdtwo_reconstruction(hdr, idx, val, p.kra, p.krb, dense, tol=tol, throut=1e-16)
 
 
 def test_mdcint_file(tmp_path):

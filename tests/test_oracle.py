@@ -5,16 +5,7 @@ import pytest
 
 import pyoracle
 from molfdir_gb300 import synth
-from util import permute_spinors
-
-
-def dense_full(p):
-    """(ij|kl) over all spinors by the textbook four-index sum (small n)."""
-    n, m = p.n, p.m
-    g = synth.dense_ao_tensor(p.model, p.mfil).reshape(n * n, n * n)
-    d = (np.einsum("pa,qb->abpq", p.qa.conj(), p.qa)
-         + np.einsum("pa,qb->abpq", p.qb.conj(), p.qb)).reshape(m * m, n * n)
-    return ((d @ g) @ d.T).reshape(m, m, m, m)
+from util import dense_full, permute_spinors
 
 
 def spinor_of(p, k):
@@ -104,3 +95,42 @@ def test_oracle_golden_fixture():
     img = pyoracle.run(p)
     assert np.array_equal(img.hdr, g["hdr"]) and np.array_equal(img.idx, g["idx"])
     assert np.max(np.abs(img.val - g["dense_val"])) <= 1e-13
+
+
+@pytest.mark.parametrize("nl,ns,nkr,seed,shuffle", [(3, 4, 2, 0, False), (5, 7, 3, 3, False),
+                                                    (4, 6, 3, 5, True)])
+def test_oracle_stream_reconstructs_the_tensor_as_a_reader_does(nl, ns, nkr, seed, shuffle):
+    """Structural parity of the MDCINT stream with its reader (rdtwo.F:29-83):
+    expanding every element into its 16 related quadruples reproduces the
+    whole dense (ij|kl), consistently."""
+    from util import check_rdtwo_reconstruction
+    p = synth.make_problem(nl, ns, nkr, seed=seed)
+    if shuffle:
+        p = permute_spinors(p, np.random.default_rng(seed).permutation(p.m))
+    img = pyoracle.run(p)
+    dense = dense_full(p)
+    check_rdtwo_reconstruction(img.hdr, img.idx, img.val, p.kra, p.krb, dense,
+                               tol=1e-13 * max(1.0, np.abs(dense).max()), throut=1e-16)
+
+
+@pytest.mark.parametrize("mistake", ["conjugate_one", "drop_record", "flip_sign"])
+def test_reconstruction_check_catches_planted_mistakes(mistake):
+    from util import check_rdtwo_reconstruction
+    p = synth.make_problem(3, 4, 2, seed=0)
+    img = pyoracle.run(p)
+    dense = dense_full(p)
+    hdr, idx, val = img.hdr.copy(), img.idx.copy(), img.val.copy()
+    z = int(np.argmax(np.abs(val.imag)))  # an element with an imaginary part
+    if mistake == "conjugate_one":
+        val[z] = np.conj(val[z])
+    elif mistake == "flip_sign":
+        val[z] = -val[z]
+    else:  # drop the largest record's elements
+        r = int(np.argmax(hdr[:, 2]))
+        start = int(hdr[:r, 2].sum())
+        keep = np.r_[0:start, start + hdr[r, 2]:val.size]
+        idx, val = idx[keep], val[keep]
+        hdr[r, 2] = 0
+    with pytest.raises(AssertionError):
+        check_rdtwo_reconstruction(hdr, idx, val, p.kra, p.krb, dense,
+                                   tol=1e-13 * max(1.0, np.abs(dense).max()), throut=1e-16)

@@ -57,3 +57,71 @@ def compare_streams(got, ref, tol, presence_tol=None):
         kb = [k for k in ri[ro[r]:ro[r + 1]].tolist() if tuple(k) in a]
         assert ka == kb, f"record {r}: element order differs"
     return err
+
+
+def rdtwo_expand(hdr, idx, val, kra, krb, m):
+    """The spinor integral tensor a MDCINT reader reconstructs: goscip's RDTWO
+    (source/goscip/rdtwo.F:29-83) stores each element (ij|kl) under 16
+    quadruples -- itself, its complex conjugate (ji|lk)*, the particle
+    interchange (kl|ij) and (lk|ji)*, each with the time-reversed partners of
+    the pairs, signed by SignIJ = sign(IKR) sign(JKR) and SignKL.  Returns
+    (full, hits): the implied values (later assignments win, as in RDTWO)
+    and, per quadruple, the list of all implied values, for consistency
+    checks.  Kramers index k > 0 is spinor kra[k-1], k < 0 is krb[-k-1]."""
+    full = np.zeros((m, m, m, m), np.complex128)
+    hits = {}
+
+    def sp(k):
+        return (kra[k - 1] if k > 0 else krb[-k - 1]) - 1
+
+    off = 0
+    for ikr, jkr, nz in hdr:
+        i, itr, j, jtr = sp(ikr), sp(-ikr), sp(jkr), sp(-jkr)
+        sij = np.sign(ikr) * np.sign(jkr)
+        for z in range(nz):
+            kkr, lkr = idx[off + z]
+            v = val[off + z]
+            k, ktr, l, ltr = sp(kkr), sp(-kkr), sp(lkr), sp(-lkr)
+            skl = np.sign(kkr) * np.sign(lkr)
+            c = np.conj(v)
+            for q, x in (((i, j, k, l), v), ((jtr, itr, k, l), sij * v),
+                         ((i, j, ltr, ktr), skl * v), ((jtr, itr, ltr, ktr), sij * skl * v),
+                         ((j, i, l, k), c), ((itr, jtr, l, k), sij * c),
+                         ((j, i, ktr, ltr), skl * c), ((itr, jtr, ktr, ltr), sij * skl * c),
+                         ((k, l, i, j), v), ((ltr, ktr, i, j), skl * v),
+                         ((k, l, jtr, itr), sij * v), ((ltr, ktr, jtr, itr), sij * skl * v),
+                         ((l, k, j, i), c), ((ktr, ltr, j, i), skl * c),
+                         ((l, k, itr, jtr), sij * c), ((ktr, ltr, itr, jtr), sij * skl * c)):
+                full[q] = x
+                hits.setdefault(q, []).append(x)
+        off += nz
+    return full, hits
+
+
+def check_rdtwo_reconstruction(hdr, idx, val, kra, krb, dense, tol, throut=0.0):
+    """Every quadruple a reader reconstructs equals the dense tensor, every
+    implied value agrees, and every quadruple the stream leaves out is at
+    most THROUT (plus tol) in the dense tensor.  Returns the max error."""
+    m = dense.shape[0]
+    full, hits = rdtwo_expand(hdr, idx, val, kra, krb, m)
+    err = 0.0
+    for q, xs in hits.items():
+        for x in xs:
+            err = max(err, abs(x - dense[q]))
+    mask = np.zeros(dense.shape, bool)
+    if hits:
+        mask[tuple(np.array(list(hits)).T)] = True
+    missing = float(np.abs(dense[~mask]).max()) if (~mask).any() else 0.0
+    assert missing <= throut + tol, f"an integral of size {missing:.3e} is not reachable"
+    assert err <= tol, f"reconstructed value off by {err:.3e}"
+    return err
+
+
+def dense_full(p):
+    """(ij|kl) over all spinors by the textbook four-index sum (small n)."""
+    from molfdir_gb300 import synth
+    n, m = p.n, p.m
+    g = synth.dense_ao_tensor(p.model, p.mfil).reshape(n * n, n * n)
+    d = (np.einsum("pa,qb->abpq", p.qa.conj(), p.qa)
+         + np.einsum("pa,qb->abpq", p.qb.conj(), p.qb)).reshape(m * m, n * n)
+    return ((d @ g) @ d.T).reshape(m, m, m, m)
