@@ -331,6 +331,8 @@ def main():
                     choices=["precision", "c1", "profile", "large", "batched", "gemm", "files"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--per-class", action="store_true",
+                    help="also split vs FP64 per AO integral class (3 + 3 extra transforms)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     hbm_peak, bf16_peak, peak_kind = peaks()
@@ -482,6 +484,42 @@ def main():
                 "ms_per_step": ref["sec"] * 1e3, "steps": 1, "warmup": 0,
                 "split_speedup": ref["sec"] / main["sec"], "split_vs_fp64": acc}
 
+    # ---- split vs FP64 per AO integral class, each class transformed alone ----
+    per_class = None
+    if args.per_class and prec_name == "split" and rank == 0:
+        per_class = {}
+        ends = np.cumsum(nts)
+        starts = ends - nts
+        for c, name in ((1, "(LL|LL)"), (2, "(SS|LL)"), (3, "(SS|SS)")):
+            sel = np.nonzero(cls == c)[0]
+            if sel.size == 0:
+                continue
+            a, b = int(starts[sel[0]]), int(ends[sel[-1]])  # a class's records are contiguous
+            outs = []
+            for p_, s_ in ((prec, args.slices), (rotran.RT_PREC_FP64, 0)):
+                rt = make_ctx(p_, s_)
+                rt.add_records_bulk_ptr(cls[sel], nts[sel], its[sel], dv[a:].data_ptr(),
+                                        dl2[a:].data_ptr(), dl1[a:].data_ptr())
+                rt.transform()
+                outs.append(rt.result())
+                rt.close()
+            (h1, i1, v1), (h2, i2, v2) = outs
+            if np.array_equal(h1, h2) and np.array_equal(i1, i2):
+                mx = ss = mv = 0.0
+                for q in range(0, v1.size, 1 << 26):
+                    d = np.abs(v1[q:q + (1 << 26)] - v2[q:q + (1 << 26)])
+                    mx = max(mx, float(d.max()))
+                    ss += float(np.dot(d, d))
+                    mv = max(mv, float(np.abs(v2[q:q + (1 << 26)]).max()))
+                per_class[name] = {"integrals": int(b - a), "max_abs_err": mx,
+                                   "rms_err": float(np.sqrt(ss / max(1, v1.size))),
+                                   "max_abs_value": mv, "same_elements": True}
+            else:
+                per_class[name] = {"integrals": int(b - a), "same_elements": False}
+        if fp64 is not None:
+            fp64["split_vs_fp64_per_class"] = per_class
+            per_class = None  # reported inside the fp64 object
+
     # ---- CPU baseline (rank 0, N = 1) ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -526,6 +564,8 @@ def main():
             "gpu_launches": st.gpu_launches * args.steps, "clocks": main["clocks"],
             "stats": st.as_dict(), "mdcint": {"records": nrec, "elements": nz},
         }
+        if per_class is not None:
+            line["split_vs_fp64_per_class"] = per_class
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -57,3 +57,29 @@ def test_split_irrep_blocks():
     img = pyoracle.run(p)
     got, _ = run(p, rotran.RT_PREC_SPLIT_BF16)
     assert compare_streams(got, (img.hdr, img.idx, img.val), TOL_SPLIT) <= TOL_SPLIT
+
+
+def test_split_error_per_integral_class():
+    """Max and RMS error of the split path per AO integral class, (LL|LL),
+    (SS|LL) and (SS|SS), each transformed alone at the CPU-sized case."""
+    p = synth.make_problem(24, 40, 32, seed=0)
+    cls, its, nts, v, l2, l1 = p.flat_records()
+    ends = np.cumsum(nts)
+    starts = ends - nts
+    for c, name in ((1, "(LL|LL)"), (2, "(SS|LL)"), (3, "(SS|SS)")):
+        sel = np.nonzero(cls == c)[0]
+        pieces = [slice(int(starts[r]), int(ends[r])) for r in sel]
+        recs = (cls[sel], its[sel], nts[sel], np.concatenate([v[s] for s in pieces]),
+                np.concatenate([l2[s] for s in pieces]), np.concatenate([l1[s] for s in pieces]))
+        img = pyoracle.run(p, records=recs)
+        with rotran.Rotran.for_problem(p, precision=rotran.RT_PREC_SPLIT_BF16) as rt:
+            rt.set_problem_coefficients(p)
+            rt.add_records_bulk(recs[0], recs[2], recs[1], *recs[3:])
+            rt.transform()
+            got = rt.result()
+        err = compare_streams(got, (img.hdr, img.idx, img.val), TOL_SPLIT)
+        same = np.array_equal(got[0], img.hdr) and np.array_equal(got[1], img.idx)
+        rms = float(np.sqrt(np.mean(np.abs(got[2] - img.val) ** 2))) if same else float("nan")
+        print(f"{name}: max abs err {err:.3e}, rms {rms:.3e}, max |value| "
+              f"{float(np.abs(img.val).max()):.3e}")
+        assert err <= TOL_SPLIT
