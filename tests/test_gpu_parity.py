@@ -130,6 +130,38 @@ def test_stream_reconstructs_the_tensor_as_a_reader_does(precision):
     check_rdtwo_reconstruction(hdr, idx, val, p.kra, p.krb, dense, tol=tol, throut=1e-16)
 
 
+def test_no_integrals():
+    """No records at all: every MDCINT record is written, with no elements,
+    as the oracle writes it."""
+    p = synth.make_problem(4, 5, 3, seed=21)
+    empty = (np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0, np.int64),
+             np.zeros(0), np.zeros(0, np.int32), np.zeros(0, np.int32))
+    img = pyoracle.run(p, records=empty)
+    with rotran.Rotran.for_problem(p) as rt:
+        rt.set_problem_coefficients(p)
+        rt.transform()
+        hdr, idx, val = rt.result()
+    assert np.array_equal(hdr, img.hdr) and idx.shape[0] == 0 == img.idx.shape[0]
+    assert np.all(hdr[:, 2] == 0)
+
+
+def test_files_above_mfil_are_not_read():
+    """SORT1 reads files 1..MFIL only (sort1.F:118): (SS|SS) records added to
+    an MFIL = 2 transform change nothing."""
+    p2 = synth.make_problem(5, 6, 3, seed=22, mfil=2)
+    p3 = synth.make_problem(5, 6, 3, seed=22, mfil=3)
+    base, _ = run_gpu(p2)
+    with rotran.Rotran.for_problem(p2) as rt:
+        rt.set_problem_coefficients(p2)
+        rt.add_problem_records(p2)
+        for r in p3.files["SS"]:
+            rt.add_record(3, r.it, r.rint, r.label2, r.label1)
+        rt.transform()
+        more = rt.result()
+    assert all(np.array_equal(a, b) for a, b in zip(base[:2], more[:2]))
+    assert np.max(np.abs(base[2] - more[2])) <= 1e-15
+
+
 def test_mdcint_file(tmp_path):
     p = synth.make_problem(6, 8, 4, seed=16)
     with rotran.Rotran.for_problem(p) as rt:
