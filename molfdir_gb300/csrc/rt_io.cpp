@@ -137,9 +137,9 @@ struct SrtpqRec {
 
 // Decode the entries of records [r0, r1) of a block, calling
 // f(group, value, label2, label1) in file order; group = 14*(class-1)+type-1.
-// Returns an error text, or an empty string.
+// Returns an error text, or nullptr (no allocation: runs on worker threads).
 template <class F>
-std::string srtpq_decode(const char* block, int irecl, const SrtpqRec* hd, long long r0, long long r1,
+const char* srtpq_decode(const char* block, int irecl, const SrtpqRec* hd, long long r0, long long r1,
                          int nsc, int nsc1, F&& f) {
     for (long long k = r0; k < r1; ++k) {
         const SrtpqRec& h = hd[k];
@@ -164,15 +164,23 @@ std::string srtpq_decode(const char* block, int irecl, const SrtpqRec* hd, long 
             f(14 * (cls - 1) + it - 1, v, lab, l1);
         }
     }
-    return std::string();
+    return nullptr;
 }
 
-// Run fn(w, r0, r1) on t threads over [0, nb) (the calling thread takes the last part).
+// Run fn(w, r0, r1) on t threads over [0, nb); the calling thread takes the
+// last part, and the part of any thread that cannot be started.  fn must not
+// throw.
 template <class F>
 void srtpq_parallel(int t, long long nb, F&& fn) {
     std::vector<std::thread> pool;
-    for (int w = 0; w + 1 < t; ++w) pool.emplace_back([&, w] { fn(w, nb * w / t, nb * (w + 1) / t); });
-    fn(t - 1, nb * (t - 1) / t, nb);
+    pool.reserve((size_t)t);
+    int started = 0;
+    try {
+        for (; started + 1 < t; ++started)
+            pool.emplace_back([&, w = started] { fn(w, nb * w / t, nb * (w + 1) / t); });
+    } catch (...) {
+    }
+    for (int w = started; w < t; ++w) fn(w, nb * w / t, nb * (w + 1) / t);
     for (auto& th : pool) th.join();
 }
 
@@ -258,14 +266,14 @@ void srtpq_read(const char* dir, int nranks, int nsc, int nsc1, Sink&& sink) {
             // each thread's entries at its offsets (file order is kept)
             const int t = (int)std::min<long long>(nthr, std::max(1LL, nb / 64));
             std::vector<std::array<long long, 42>> cnt((size_t)t), off((size_t)t);
-            std::vector<std::string> errs((size_t)t);
+            std::vector<const char*> errs((size_t)t, nullptr);
             srtpq_parallel(t, nb, [&](int w, long long a, long long b) {
                 cnt[w].fill(0);
                 errs[w] = srtpq_decode(block.data(), irecl, hd.data(), a, b, nsc, nsc1,
                                        [&](int g, double, int32_t, int32_t) { ++cnt[w][g]; });
             });
             for (int w = 0; w < t; ++w)
-                if (!errs[w].empty()) throw SrtpqError{RT_ERR_USER, errs[w] + " in " + pil};
+                if (errs[w]) throw SrtpqError{RT_ERR_USER, std::string(errs[w]) + " in " + pil};
             long long base = 0;
             for (int g = 0; g < 42; ++g) {
                 out.start[g] = base;
@@ -341,6 +349,9 @@ extern "C" int rt_srtpq_scan(const char* dir, int nranks, int nsc, int nsc1, lon
     } catch (const std::bad_alloc&) {
         rt_internal_set_thread_error("rt_srtpq_scan: out of host memory");
         return RT_ERR_DIM;
+    } catch (...) {
+        rt_internal_set_thread_error("rt_srtpq_scan failed");
+        return RT_ERR_PROGRAM;
     }
 }
 
@@ -371,6 +382,9 @@ extern "C" int rt_read_srtpq_files(rt_ctx* ctx, const char* dir, int nranks) {
     } catch (const std::bad_alloc&) {
         rt_internal_set_error(ctx, "rt_read_srtpq_files: out of host memory");
         return RT_ERR_DIM;
+    } catch (...) {
+        rt_internal_set_error(ctx, "rt_read_srtpq_files failed");
+        return RT_ERR_PROGRAM;
     }
 }
 
