@@ -130,6 +130,18 @@ def barrier_max(value, world):
     return float(t.item())
 
 
+def dense_equivalent_flops(n, nkr):
+    """The dense count of the reference algorithm over all n(n+1)/2 AO pairs:
+    F1 = P (4 n^2 m + 8 n m^2) (MATMUL1 as a dense real x complex product,
+    then the m x m x n ZGEMM) and F2 = K(K+1) (8 n^2 m + 8 n m^2) (the
+    symmetric expansion as a dense complex product, then the ZGEMM), m = 2K.
+    It includes the SL pairs Coulomb rotran never transforms and the zero
+    L/S blocks of each pair, so it is about 2x the work done; the bench's
+    value uses the count of nonzero blocks instead (flops_algorithmic)."""
+    m, P = 2 * nkr, n * (n + 1) // 2
+    return P * (4.0 * n * n * m + 8.0 * n * m * m) + nkr * (nkr + 1) * (8.0 * n * n * m + 8.0 * n * m * m)
+
+
 def cpu_sample(work, steps=1, warmup=0, seconds=15.0):
     """CPU restatement of rotran on a bounded sample of the workload:
     TRANS1 over the first pq blocks and TRANS2 over the first items with
@@ -558,6 +570,9 @@ def main():
                        "n_irrep": work.get("n_irrep", 1),
                        "precision": prec_name, "slices": args.slices if prec_name == "split" else None,
                        "integrals": nint, "flops_algorithmic": flops,
+                       "flops_dense_equivalent": dense_equivalent_flops(prob.n, work["nkr"]),
+                       "tflops_dense_equivalent": dense_equivalent_flops(prob.n, work["nkr"]) * world
+                       / main["sec"] / 1e12,
                        "l2": "inputs larger than L2 (integral records 16 B each)",
                        "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64,
