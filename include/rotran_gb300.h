@@ -181,7 +181,9 @@ int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double* energy);
  * replay.  The results are then read per context with rt_result_sizes /
  * rt_copy_result / rt_write_mdcint.  All contexts: same device, precision
  * RT_PREC_SPLIT_BF16, coefficients and records set before rt_batch_create
- * and left unchanged while the batch lives (RT_ERR_MISMATCH otherwise). */
+ * and left unchanged while the batch lives (RT_ERR_MISMATCH otherwise).
+ * The batch keeps work arrays in its contexts: destroy it before any of
+ * them. */
 typedef struct rt_batch rt_batch;
 typedef struct rt_batch_stats {
     int instances;

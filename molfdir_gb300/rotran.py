@@ -409,7 +409,8 @@ def split_dgemm_noalloc(m: int, n: int, k: int, a_ptr: int, b_ptr: int, c_ptr: i
 class Batch:
     """Batched transforms of several split-precision contexts (``rt_batch_*``):
     one grouped GEMM launch per stage, captured as a CUDA graph on the first
-    ``run()`` (after tuning the tile width per stage) and replayed after."""
+    ``run()`` (after tuning the tile width per stage) and replayed after.
+    Close the batch before closing any of its contexts."""
 
     def __init__(self, rts):
         self.lib = load()
