@@ -68,3 +68,13 @@ def test_reference_arm_line_on_rank_zero():
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_dense_equivalent_flops_match_the_workload_table():
+    """The dense count bench.py reports beside its value: F1 = P(4n^2m +
+    8nm^2) over all n(n+1)/2 pairs plus F2 = K(K+1)(8n^2m + 8nm^2)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    for (n, k), f in (((64, 32), 1.10e10), ((400, 120), 3.42e13), ((256, 64), 2.63e12),
+                      ((480, 200), 1.68e14)):
+        assert abs(bench.dense_equivalent_flops(n, k) / f - 1) < 0.01, (n, k)
