@@ -128,3 +128,33 @@ def test_record_framing_subrecords(tmp_path):
     with open(path, "rb") as f:
         assert fortio.read_record(f) == b"abcdefg"
         assert fortio.read_record(f) is None
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """A C caller (the Fortran binding goes through the same ABI) compiles
+    against include/rotran_gb300.h as strict C99 and links the library; the
+    argument checks that need no device answer without one."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = rotran.load()
+    libdir = os.path.dirname(lib._name)
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "rotran_gb300.h"\n'
+        "int main(void) {\n"
+        "  rt_ctx* ctx = 0;\n"
+        "  if (rt_transform(0) != RT_ERR_USER) return 1;\n"
+        "  if (rt_create(0, 0) != RT_ERR_USER) return 2;\n"
+        "  if (rt_split_dgemm_noalloc(0, 8, 8, 0, 0, 0, 5, 0) != RT_ERR_USER) return 3;\n"
+        "  (void)ctx; puts(\"ok\"); return 0;\n}\n")
+    exe = tmp_path / "caller"
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                        "-I", os.path.join(ROOT, "include"), str(src), "-L", libdir,
+                        "-lrotran_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
