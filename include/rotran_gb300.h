@@ -59,7 +59,8 @@ typedef struct rt_config {
     int n_irrep;      /* 1, or 4: AO functions carry the labels in ao_irrep and
                          (pq|rs) vanishes unless irr(p)^irr(q) == irr(r)^irr(s) */
     const int* ao_irrep; /* NSC labels 0..n_irrep-1 (NULL when n_irrep == 1) */
-    long long mem_budget; /* device bytes the context may use (0: 85% of free) */
+    long long mem_budget; /* device bytes the context may use (0: 85% of the free
+                             memory plus the work arena the context already holds) */
 } rt_config;
 
 typedef struct rt_stats {
