@@ -97,14 +97,16 @@ def test_oracle_golden_fixture():
     assert np.max(np.abs(img.val - g["dense_val"])) <= 1e-13
 
 
-@pytest.mark.parametrize("nl,ns,nkr,seed,shuffle", [(3, 4, 2, 0, False), (5, 7, 3, 3, False),
-                                                    (4, 6, 3, 5, True)])
-def test_oracle_stream_reconstructs_the_tensor_as_a_reader_does(nl, ns, nkr, seed, shuffle):
+@pytest.mark.parametrize("nl,ns,nkr,seed,shuffle,mfil,nirr", [
+    (3, 4, 2, 0, False, 3, 1), (5, 7, 3, 3, False, 3, 1), (4, 6, 3, 5, True, 3, 1),
+    (5, 6, 3, 6, False, 2, 1), (6, 0, 3, 7, False, 1, 1), (6, 8, 3, 8, False, 3, 4)])
+def test_oracle_stream_reconstructs_the_tensor_as_a_reader_does(nl, ns, nkr, seed, shuffle, mfil,
+                                                                 nirr):
     """Structural parity of the MDCINT stream with its reader (rdtwo.F:29-83):
     expanding every element into its 16 related quadruples reproduces the
-    whole dense (ij|kl), consistently."""
+    whole dense (ij|kl), consistently (MFIL 1-3, 4-irrep blocks)."""
     from util import check_rdtwo_reconstruction
-    p = synth.make_problem(nl, ns, nkr, seed=seed)
+    p = synth.make_problem(nl, ns, nkr, seed=seed, mfil=mfil, n_irrep=nirr)
     if shuffle:
         p = permute_spinors(p, np.random.default_rng(seed).permutation(p.m))
     img = pyoracle.run(p)
