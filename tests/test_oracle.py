@@ -136,3 +136,31 @@ def test_reconstruction_check_catches_planted_mistakes(mistake):
     with pytest.raises(AssertionError):
         check_rdtwo_reconstruction(hdr, idx, val, p.kra, p.krb, dense,
                                    tol=1e-13 * max(1.0, np.abs(dense).max()), throut=1e-16)
+
+
+def test_reconstruction_property_over_random_small_problems():
+    """Property form of the reader check: any small problem (sizes, MFIL,
+    irreps, seed, spinor order) gives a stream that reconstructs the tensor."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    from util import check_rdtwo_reconstruction
+
+    @hyp.settings(max_examples=20, deadline=None, derandomize=True)
+    @hyp.given(nl=st.integers(1, 5), ns=st.integers(0, 6), nkr=st.integers(1, 3),
+               seed=st.integers(0, 10_000), mfil=st.integers(1, 3), nirr=st.sampled_from([1, 4]),
+               shuffle=st.booleans())
+    def prop(nl, ns, nkr, seed, mfil, nirr, shuffle):
+        if mfil == 1:
+            ns = 0
+        if ns == 0:
+            mfil = 1
+        hyp.assume(nkr <= nl + ns)
+        p = synth.make_problem(nl, ns, nkr, seed=seed, mfil=mfil, n_irrep=nirr)
+        if shuffle:
+            p = permute_spinors(p, np.random.default_rng(seed).permutation(p.m))
+        img = pyoracle.run(p)
+        dense = dense_full(p)
+        check_rdtwo_reconstruction(img.hdr, img.idx, img.val, p.kra, p.krb, dense,
+                                   tol=1e-13 * max(1.0, np.abs(dense).max()), throut=1e-16)
+
+    prop()
