@@ -153,3 +153,29 @@ def test_capacity_protocol(tmp_path):
     assert rc == rotran.RT_ERR_DIM
     assert nint.value == p.flat_records()[3].size
     assert 1 <= nrec.value <= 42
+
+
+def test_scan_property_over_random_layouts():
+    """Any rank count, record size, repeat pattern and number of Breit
+    streams: the parse returns exactly the serial integrals."""
+    import tempfile
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+
+    @hyp.settings(max_examples=25, deadline=None, derandomize=True)
+    @hyp.given(nl=st.integers(1, 5), ns=st.integers(1, 6), seed=st.integers(0, 1000),
+               nranks=st.integers(1, 5), nbuf=st.integers(1, 40), split=st.integers(0, 4),
+               breit=st.integers(0, 3))
+    def prop(nl, ns, seed, nranks, nbuf, split, breit):
+        p = synth.make_problem(nl, ns, 1, seed=seed)
+        with tempfile.TemporaryDirectory() as d:
+            fortio.write_srtpq_files(p, d, nranks=nranks, nbuf=nbuf, split_every=split,
+                                     breit_pairs=breit, seed=seed)
+            got = rotran.srtpq_scan(d, nranks, p.n, p.model.n_l)
+        want = summed(*p.flat_records())
+        have = summed(*got)
+        assert set(have) == set(want)
+        for k, x in want.items():
+            assert have[k] == x
+
+    prop()
