@@ -333,7 +333,7 @@ template <int BN, class Epi, class Tab>
 __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* error) {
     constexpr uint32_t TCOLS = 4 * BN;  // four accumulators of BN columns
     extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t full[NSTAGE], empty[NSTAGE], tfull, tempty;
+    __shared__ __align__(8) uint64_t full[NSTAGE], empty[NSTAGE], tfull, tempty, tdrain;
     __shared__ uint32_t tbase;
     __shared__ volatile int abort_flag;
     __shared__ int issued[NSTAGE];
@@ -351,6 +351,7 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
         }
         mbar_init(&tfull, 1);
         mbar_init(&tempty, EPI_WARPS);
+        mbar_init(&tdrain, 1);
         abort_flag = 0;
         mbar_fence_init();
     }
@@ -431,6 +432,11 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
                 if (abort_flag) break;
                 umma_commit(&tfull);
             }
+            // every MMA this thread issued completes before TMEM is freed
+            // (after an abort, the last ones were never waited for)
+            umma_commit(&tdrain);
+            volatile int never = 0;
+            mbar_wait_bounded(&tdrain, 0, &never, WAIT_NS);
         }
     } else {  // ---- epilogue: warps 2..9; lane group warp%4, column half (warp-2)/4 ----
         const int ew = warp - 2;
@@ -438,7 +444,10 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
         const int chalf = ew >> 2;
         const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
         int it = 0;
-        for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x, ++it) {
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+            // the whole warp leaves together (the TMEM loads and __syncwarp
+            // below need every lane)
+            if (__any_sync(0xffffffffu, abort_flag != 0)) break;
             const TileRef r = tile_ref(tab, tile);
             const SplitArgs& g = tab.args(r.p);
             const long long ks = r.ks, tm = r.tm, tn = r.tn;
@@ -452,8 +461,10 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
                 fcol[j] = e < -1000 ? 0.0f : pow2f_safe(e);
             }
             __syncwarp();
-            if (!mbar_wait_bounded(&tfull, (uint32_t)(it & 1), &abort_flag, WAIT_NS)) {
-                if (!abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_TMEM);
+            const bool ready = __all_sync(
+                0xffffffffu, mbar_wait_bounded(&tfull, (uint32_t)(it & 1), &abort_flag, WAIT_NS));
+            if (!ready) {
+                if (lane == 0 && !abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_TMEM);
                 abort_flag = 1;
                 break;
             }
