@@ -78,7 +78,7 @@ typedef struct rt_stats {
 } rt_stats;
 
 /* Sizes of a transformation, computed on the host without a device: the
- * pq blocks transformed (makind.F:223-277), device bytes of the main arrays,
+ * pq blocks transformed (makind.F:58-112), device bytes of the main arrays,
  * MDCINT records and an upper bound of their elements per class. */
 typedef struct rt_plan_info {
     long long npairs;          /* pq blocks transformed */
@@ -96,11 +96,11 @@ int rt_plan(const rt_config* cfg, rt_plan_info* out);
  * of rotran.F:74-231).  Fails with RT_ERR_PROGRAM if no sm_103a device. */
 int rt_create(rt_ctx** out, const rt_config* cfg);
 
-/* Spinor coefficients and Kramers tables (GETMOS, getmos.F:191-430;
+/* Spinor coefficients and Kramers tables (GETMOS, getmos.F:3-242;
  * KRAMERS, kramers.F:3-165).  qa: QA(ld_qa, NSP) COMPLEX*16, rows 1..NSC
  * used; itrmo/ikrmo: NSP entries; kra/krb: NKR spinor indices of the
  * unbarred/barred member of each pair; imoras_pairs: 2*NKR orbital numbers
- * written to the MDCINT header (inittwoe.F:139-141). */
+ * written to the MDCINT header (inittwoe.F:21-23). */
 int rt_set_coefficients(rt_ctx* ctx, const double* qa, int ld_qa, const int* itrmo,
                         const int* kra, const int* krb, const int* ikrmo,
                         const int* imoras_pairs);
@@ -108,7 +108,7 @@ int rt_set_coefficients(rt_ctx* ctx, const double* qa, int ld_qa, const int* itr
 /* One SRTTW/SRTLB record pair as GETTW reads it (gettw.F:15-29): nt unscaled
  * integrals of type itype from file file_class (1 = SRTTWLL, 2 = SRTTWSL
  * (SS|LL), 3 = SRTTWSS); label2 = I<<16|K of the first pair, label1 =
- * L<<16|N of the second (the pq bucket of sort1.F:136-142).  Records of
+ * L<<16|N of the second (the pq bucket of sort1.F:124-142).  Records of
  * files above MFIL are accepted and ignored, as SORT1 does not read them. */
 int rt_add_ao_records(rt_ctx* ctx, int file_class, int nt, int itype, const double* rint,
                       const int* label2, const int* label1);
@@ -122,7 +122,7 @@ int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* file_class, c
 
 /* Read SRTTWLL/SRTLBLL, SRTTWSL/SRTLBSL, SRTTWSS/SRTLBSS (gfortran
  * sequential unformatted, 4-byte markers) from directory dir, files
- * 1..MFIL, as SORT1 does (sort1.F:118-205). */
+ * 1..MFIL, as SORT1 does (sort1.F:60-147). */
 int rt_read_srt_files(rt_ctx* ctx, const char* dir);
 
 /* Read the MPI version's pq-sorted integral files of ranks 0..nranks-1
@@ -212,7 +212,7 @@ int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz);
  * (ppsym.F:89-91), idx[2*nz] = (INDK, INDL), val[2*nz] = (re, im). */
 int rt_copy_result(rt_ctx* ctx, int* hdr, int* idx, double* val);
 
-/* Write MDCINT (inittwoe.F:119-143, ppsym.F:89-91, exittwoe.F:144-153) as
+/* Write MDCINT (inittwoe.F:1-25, ppsym.F:89-91, exittwoe.F:1-10) as
  * a gfortran sequential unformatted file. */
 int rt_write_mdcint(rt_ctx* ctx, const char* path, const char* datex10, const char* timex8);
 

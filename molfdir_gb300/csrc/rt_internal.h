@@ -7,7 +7,7 @@
 //                 increasing reference index.  The L functions occupy sorted
 //                 positions [0, nL) and the S functions [nL, n).
 //   pair order    the pq blocks rotran transforms (LL pairs, and SS pairs
-//                 when S functions exist; makind.F:235-255) grouped by
+//                 when S functions exist; makind.F:70-90) grouped by
 //                 (class, pair irrep), inside a group in increasing
 //                 p(p-1)/2+q.  P = number of pairs.
 //   buckets       the integral records sorted by pq bucket (value + (r,s)),
@@ -127,7 +127,7 @@ struct Stage {
 struct Work {
     std::vector<int4> items4;     // (I, J, Ibar, Jbar) per item
     std::vector<float> isign;     // sign(ITRMO(I) ITRMO(J))
-    std::vector<double> pair_vmx; // VMX(p) VMX(q) per pair (trout.F:194)
+    std::vector<double> pair_vmx; // VMX(p) VMX(q) per pair (trout.F:30)
     std::vector<EmitRec> recs;    // MDCINT records in item order
     std::vector<int> item_rec0;   // first record of each item
     long long cap[4] = {0, 0, 0, 0};   // element capacity per class
@@ -225,6 +225,9 @@ struct rt_ctx {
     cudaStream_t cstream[4] = {};  // host <-> device copies in pieces
     cudaEvent_t ev[8] = {};
     bool have_coef = false;
+    // set when an aborted GEMM could not confirm that its tensor-core work
+    // and copies had finished: no further device work runs on the context
+    bool unusable = false;
     // host copies of the tables
     std::vector<double> qa;   // n x m complex, column-major, interleaved
     std::vector<int> itrmo, kra, krb, ikrmo, imoras;  // in the internal spinor order

@@ -123,7 +123,7 @@ struct F64El {
     static __device__ __forceinline__ T from(double v) { return v; }
     static __device__ __forceinline__ bool nonzero(T re, T im) { return re != 0.0 || im != 0.0; }
     static __device__ __forceinline__ bool above(T re, T im, double thr) { return hypot(re, im) > thr; }
-    // TROUT's screen (trout.F:194-207): kept unless VMX product or value too small
+    // TROUT's screen (trout.F:30-43): kept unless VMX product or value too small
     static __device__ __forceinline__ bool screen(T re, T im, double vv, float, double thrgen) {
         return !(vv < thrgen) && !(hypot(re, im) < thrgen / vv);
     }
@@ -148,11 +148,11 @@ struct FFEl {
 
 // ---------------------------------------------------------------------------
 // K2: Kramers-unique selection + time-reversal completion + transpose
-// (MTIMHER + TROUT + SR2FLSH + GETHTI + UNIQUE: mtimher.F:141-164,
-// trout.F:165-227, unique.F:1-50).  With the full symmetric G_pq the
+// (MTIMHER + TROUT + SR2FLSH + GETHTI + UNIQUE: mtimher.F:3-26,
+// trout.F:1-63, unique.F:1-50).  With the full symmetric G_pq the
 // half-transformed integral of the pair (I, J) is
 //   (pq| I J) = RI(I,J) + s_IJ RI(Jbar, Ibar),   s_IJ = sign(ITRMO(I) ITRMO(J)),
-// RI = QA^H G_pq QA.  The screening test of TROUT (trout.F:194-207) is
+// RI = QA^H G_pq QA.  The screening test of TROUT (trout.F:30-43) is
 // applied to these values.
 // ---------------------------------------------------------------------------
 // pair_thr: THRGEN / VMX(p) VMX(q) per pair (+inf where the product is below
@@ -189,7 +189,7 @@ __global__ void k_tr_select(const typename E::T* __restrict__ ri, int m, int npc
 
 // ---------------------------------------------------------------------------
 // Symmetric expansion of the half-transformed integrals of one component
-// block (the role of MATMUL3's two updates, matmul3.F:75-82):
+// block (the role of MATMUL3's two updates, matmul3.F:25-32):
 //   M3[p][ij][plane][q] = Hp[plane][ij][pair(p,q)]
 // ---------------------------------------------------------------------------
 // The row blocks of one item are adjacent in launch order (blockIdx.x), so
@@ -214,7 +214,7 @@ __global__ void k_expand(const double* __restrict__ hp, int P, int nitems, int i
 
 // ---------------------------------------------------------------------------
 // MDCINT element selection (MSUMTIM + OUTPP1/OUTPP2 + PPSYM:
-// msumtim.F:87-105, outpp1.F:43-116, outpp2.F:117-255, ppsym.F:67-91).
+// msumtim.F:3-21, outpp1.F:1-74, outpp2.F:1-139, ppsym.F:67-91).
 // One block per record; positions (KKR, LKR) in the order PPSYM writes them;
 // an element is written when it belongs to the record's canonical set and
 // |value| > THROUT.  The value is the complete integral
@@ -377,7 +377,7 @@ void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, in
 
 // ===========================================================================
 // pq buckets of the integral records (the role of SORT1 + INTSRT + GETSTI:
-// sort1.F:128-221, getsti.F:230-278) and their expansion into the GEMM1
+// sort1.F:70-163, getsti.F:1-49) and their expansion into the GEMM1
 // operand, one pair chunk at a time
 // ===========================================================================
 namespace rt {

@@ -15,7 +15,7 @@ enum : unsigned int {
 // Index tables of the record bucketing (device pointers).
 struct ScatterTabs {
     int n, mfil, nblk;
-    const unsigned char* pq_read;  // [n(n+1)/2] rotran transforms this pq bucket (makind.F:235-255)
+    const unsigned char* pq_read;  // [n(n+1)/2] rotran transforms this pq bucket (makind.F:70-90)
     const int* pair_of_orig;       // [n(n+1)/2] -> pair order or -1
     const int* pair_group;         // [P] pair group
     const int* pg_start;           // [npg]

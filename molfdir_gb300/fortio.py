@@ -8,10 +8,10 @@ records have a fixed length and no markers.  Layouts follow the reference:
 * SRTLB record (32-bit labels): ``NT, IT, FINISH, LABEL(NT), LABEL1(NT)``
   (``source/reltwel/wrbuf.F:44-45``)
 * MDCINT: header ``DATEX(c10), TIMEX(c8), NKR, (KR(i), KR(-i)) * NKR``
-  (``source/rotran/inittwoe.F:139-141``), records
+  (``source/rotran/inittwoe.F:21-23``), records
   ``IKR, JKR, NZ, (INDK, INDL) * NZ, (complex) * NZ``
   (``source/rotran/ppsym.F:89-91``), terminator ``0, 0, 0``
-  (``source/rotran/exittwoe.F:149``), read as in
+  (``source/rotran/exittwoe.F:6``), read as in
   ``source/goscip/rdtwo.F:17-28``.
 * SRTPQIL[.r] (direct access) and SRTPQLN[.r] (sequential) of the MPI
   integral program, read by the MPI rotran's GETPQ

@@ -97,7 +97,7 @@ def make_spinors(n: int, nkr: int, rng: np.random.Generator):
 
     Returns ``qa, qb`` (``n x 2*nkr`` complex, Fortran order semantics:
     column ``j`` is spinor ``j+1``) and the 1-based index tables of
-    ``source/rotran/getmos.F:354-387``: ``itrmo`` (partner, + for the
+    ``source/rotran/getmos.F:166-199``: ``itrmo`` (partner, + for the
     unbarred member), ``kra``/``krb`` (spinor of the unbarred / barred member
     of each pair) and ``ikrmo`` (+/- pair index).  Spinor ``2k-1`` is the
     unbarred and ``2k`` the barred member of pair ``k``.
@@ -297,7 +297,7 @@ class Problem:
         return 2 * self.nkr
 
     def all_records(self):
-        """(file_class, record) in the order SORT1 reads them (sort1.F:118)."""
+        """(file_class, record) in the order SORT1 reads them (sort1.F:60)."""
         order = [("LL", 1), ("SL", 2), ("SS", 3)][: self.mfil]
         for key, cls in order:
             for r in self.files.get(key, []):
@@ -319,7 +319,7 @@ class Problem:
                 cat(l2s, np.int32), cat(l1s, np.int32))
 
     def imoras_pairs(self):
-        """MDCINT header orbital pairs (inittwoe.F:139-141) for one C1 irrep."""
+        """MDCINT header orbital pairs (inittwoe.F:21-23) for one C1 irrep."""
         out = np.empty(2 * self.nkr, dtype=np.int32)
         out[0::2] = self.kra
         out[1::2] = self.krb
@@ -488,7 +488,7 @@ def bucket_records(model: AOModel, pq_pairs, mfil: int = 3):
 
     Bucket pq (label1) holds (rs|pq) with rs >= pq of the same class
     ((LL|LL) or (SS|SS)) and, for an LL pair, every (SS|LL) integral
-    (sort1.F:136-200).  Returns flat record arrays like
+    (sort1.F:78-142).  Returns flat record arrays like
     ``Problem.flat_records`` (one record per file and type).
     """
     nl = model.n_l

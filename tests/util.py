@@ -31,7 +31,7 @@ def compare_streams(got, ref, tol, presence_tol=None):
     both its values are at most ``presence_tol`` (default ``tol``): a value
     within rounding of THROUT, or, for a large THROUT, an integral whose
     canonical and particle-interchanged halves the reference filters
-    separately (outpp1.F:76, outpp2.F:156) while the GPU filters the sum.
+    separately (outpp1.F:34, outpp2.F:40) while the GPU filters the sum.
     """
     presence_tol = tol if presence_tol is None else presence_tol
     gh, gi, gv = got
