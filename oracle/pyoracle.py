@@ -131,9 +131,15 @@ def time_sample(problem, seconds=15.0, nthreads=0, steps=1, warmup=0):
     TRANS1 runs over pq blocks spread evenly over the transformed blocks
     (their integral buckets generated on the host), TRANS2 over the first
     items with half-transformed lists of the full length (one entry per
-    transformed pq block).  The sample is sized to take about ``seconds``.
-    Returns the algorithmic TFLOP/s of the sample (same per-block and
-    per-item FLOP counts as the GPU library) and a description.
+    transformed pq block).  The two halves are timed separately and each is
+    scaled by its own share of the full transform,
+
+        T = t1 * P / n_pq + t2 * K(K+1) / n_items,
+
+    so the estimate does not depend on how the sample mixes the two.  The
+    sample is sized to take about ``seconds``.  Returns the algorithmic
+    TFLOP/s of the full transform (same per-block and per-item FLOP counts as
+    the GPU library) over T, and a description.
     """
     from molfdir_gb300 import synth
     model = problem.model
@@ -141,33 +147,43 @@ def time_sample(problem, seconds=15.0, nthreads=0, steps=1, warmup=0):
     pairs = [(p, q) for p in range(1, n + 1) for q in range(1, p + 1)
              if (p <= nl) == (q <= nl) and (p <= nl or problem.mfil >= 3)]
     P = len(pairs)
+    items = k * (k + 1)
     blk = nl * nl + ns * ns
     f_pq = 4.0 * blk * m + 8.0 * n * m * m
     f_it = 8.0 * blk * m + 8.0 * n * m * m
-    # calibration run
-    npq, nit = 8, 4
-    for attempt in range(3):
+    flops_full = P * f_pq + items * f_it
+
+    def sample_run(npq, nit):
         idx = np.linspace(0, P - 1, npq).round().astype(int)
         sel_pairs = [pairs[i] for i in idx]
         recs = synth.bucket_records(model, sel_pairs, problem.mfil)
         sel = [p * (p - 1) // 2 + q for p, q in sel_pairs]
+        return recs, sel
+
+    # calibration: grow each half to about a third of the budget
+    npq, nit = 8, 4
+    for attempt in range(3):
+        recs, sel = sample_run(npq, nit)
         img = run(problem, nthreads=nthreads, records=recs, pq_select=sel, limit_ij=nit,
                   fake_list_len=P)
         t1, t2 = img.times[0], img.times[1]
-        if attempt == 2 or t1 + t2 > 0.5 * seconds:
+        if attempt == 2 or (t1 > 0.25 * seconds and t2 > 0.25 * seconds):
             break
-        npq = max(npq, int(npq * 0.5 * seconds / max(t1, 1e-3)))
-        nit = max(nit, int(nit * 0.5 * seconds / max(t2, 1e-3)))
-        npq, nit = min(npq, P), min(nit, k * (k + 1))
-    times = []
-    for s in range(warmup + steps):
+        npq = min(P, max(npq, int(npq * seconds / 3 / max(t1, 1e-3))))
+        nit = min(items, max(nit, int(nit * seconds / 3 / max(t2, 1e-3))))
+    t1s, t2s = [], []
+    for s_ in range(warmup + steps):
         img = run(problem, nthreads=nthreads, records=recs, pq_select=sel, limit_ij=nit,
                   fake_list_len=P)
-        if s >= warmup:
-            times.append(img.times[0] + img.times[1])
-    t = float(np.mean(times))
-    flops = img.npq_done * f_pq + img.nij_done * f_it
-    return {"tflops": flops / t / 1e12, "ms_per_step": t * 1e3,
-            "sample": (f"TRANS1 over {img.npq_done} of {P} pq blocks (evenly spaced) + TRANS2 over "
-                       f"{img.nij_done} of {k * (k + 1)} Kramers pairs with full-length "
-                       f"half-transformed lists; algorithmic FLOPs {flops:.3e}")}
+        if s_ >= warmup:
+            t1s.append(img.times[0])
+            t2s.append(img.times[1])
+    t1, t2 = float(np.mean(t1s)), float(np.mean(t2s))
+    T = t1 * P / img.npq_done + t2 * items / img.nij_done
+    return {"tflops": flops_full / T / 1e12, "ms_per_step": T * 1e3,
+            "seconds_first_half": t1 * P / img.npq_done,
+            "seconds_second_half": t2 * items / img.nij_done,
+            "sample": (f"TRANS1 over {img.npq_done} of {P} pq blocks (evenly spaced) in {t1:.2f} s "
+                       f"and TRANS2 over {img.nij_done} of {items} Kramers pairs with full-length "
+                       f"half-transformed lists in {t2:.2f} s, each half scaled by its own "
+                       f"fraction; full-transform algorithmic FLOPs {flops_full:.3e}")}

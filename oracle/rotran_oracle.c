@@ -30,8 +30,8 @@
  *      a Kramers pair pass and TRANS2 (trans2.F:230-311) would write two
  *      records under every barred label.  Here records are written only for
  *      barred I (IKRMO(I) < 0), the set the record labels describe.
- *  (3) source/rotran/outpp2.F:220-251 (ITYP 4) lacks the IKR.EQ.JKR return
- *      that ITYP 1 has at outpp2.F:186, so a diagonal source record would
+ *  (3) source/rotran/outpp2.F:104-135 (ITYP 4) lacks the IKR.EQ.JKR return
+ *      that ITYP 1 has at outpp2.F:70, so a diagonal source record would
  *      add its (a,a) element twice to class-4 records.  The guard is applied
  *      here; with it every MDCINT element equals the complete integral.
  *  (4) With a one-slot PPSYM buffer (NC2 = 1, e.g. NKR = 1) the end-of-file
@@ -123,7 +123,7 @@ static void ref_buffer_sizes(int nsc, int nkr, int nsp, int npqbuf_used, int* ni
     long nsctr = (long)nsc * (nsc + 1) / 2, nsptr = (long)nkr * (nkr + 1), nspsq = (long)nsp * nsp;
     long ng = nsctr, nijbuf = nsptr;
     long npqbuf = nsctr < 16384 ? nsctr : 16384;
-    if (npqbuf_used < npqbuf) npqbuf = npqbuf_used; /* MAKIND (makind.F:277) */
+    if (npqbuf_used < npqbuf) npqbuf = npqbuf_used; /* MAKIND (makind.F:112) */
     long lbrcij = 1;
     long indpq = lbrcij + ((nsptr + 1) + 1) / NITR;
     long indpqu = indpq + (nsctr + 1) / NITR;
@@ -175,7 +175,7 @@ static void ref_buffer_sizes(int nsc, int nkr, int nsp, int npqbuf_used, int* ni
 }
 
 /* CSR list whose per-row order is the newest-first chunk order in which a
- * linked-record bucket file is read back (e.g. getsti.F:252-269). */
+ * linked-record bucket file is read back (e.g. getsti.F:23-40). */
 static void chunk_reverse_order(long n, int chunk, long* perm) {
     /* entries 0..n-1 appended in order; chunks of `chunk`; newest first */
     if (n == 0) return;
@@ -244,7 +244,7 @@ static void sk_add(skfile* f, int kl, cplx v) {
     f->r[f->nr - 1].nz++;
 }
 
-/* OUTPP1 (source/rotran/outpp1.F:43-116); rl is NSP x NSP column-major. */
+/* OUTPP1 (source/rotran/outpp1.F:1-74); rl is NSP x NSP column-major. */
 static void outpp1(int nkr, int nsp, int ityp, skfile* f, double thres, const int* krk,
                    const int* krl, int ikr, int jkr, const cplx* rl, long* nskel) {
     sk_begin(f, ikr, jkr);
@@ -275,7 +275,7 @@ static void outpp1(int nkr, int nsp, int ityp, skfile* f, double thres, const in
     *nskel += f->r[f->nr - 1].nz;
 }
 
-/* OUTPP2 (source/rotran/outpp2.F:117-255): pp-interchanged integrals,
+/* OUTPP2 (source/rotran/outpp2.F:1-139): pp-interchanged integrals,
  * bucketed on KKR. */
 static void outpp2(int nkr, int nsp, int ityp, pplist* bk, double thres, const int* krk,
                    const int* krl, int ikr, int jkr, const cplx* rl) {
@@ -369,7 +369,7 @@ static long ppsym(const skfile* f, const pplist* bk, int nsksiz, int nc2, int nk
         if (ir < f->nr) {
             ikr = f->r[ir].ikr; jkr = f->r[ir].jkr; nz = f->r[ir].nz; off = f->r[ir].off;
         } else {
-            ikr = 0; jkr = 0; nz = 0; off = 0; /* OUTPP3 terminator (outpp3.F:266) */
+            ikr = 0; jkr = 0; nz = 0; off = 0; /* OUTPP3 terminator (outpp3.F:11) */
         }
         if (ic2 == 1) ikrc = ikr;
         for (int z = 0; z < nz; z++) cb2[(long)ic2 * kk + f->kl[off + z] - 1] = f->v[off + z];
@@ -437,7 +437,7 @@ static long ppsym(const skfile* f, const pplist* bk, int nsksiz, int nc2, int nk
     return nfinal;
 }
 
-/* MAKIND's Coulomb selection of pq blocks (makind.F:235-255) for C1. */
+/* MAKIND's Coulomb selection of pq blocks (makind.F:70-90) for C1. */
 static int pq_included(int p, int q, int nsc1, int mfil) {
     if (p > nsc1 && q <= nsc1) return 0;
     if (p > nsc1 && mfil < 3) return 0;
@@ -460,7 +460,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     const long nsctr = (long)n * (n + 1) / 2;
     const int nji = nkr * (nkr + 1);
 
-    /* VMX (getmos.F:417-423) */
+    /* VMX (getmos.F:229-235) */
     double* vmx = (double*)calloc(n, sizeof(double));
     for (int p = 0; p < n; p++) {
         double a = 0.0;
@@ -471,7 +471,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
         vmx[p] = a;
     }
 
-    /* ---------------- SORT1 (sort1.F:118-221) ---------------- */
+    /* ---------------- SORT1 (sort1.F:60-163) ---------------- */
     long* cnt = (long*)calloc(nsctr + 1, sizeof(long));
     long nincl = 0;
     for (int p = 1; p <= n; p++)
@@ -506,7 +506,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
             long pq = (long)ip * (ip - 1) / 2 + iq;
             long slot = bstart[pq] + cnt[pq]++;
             gval[slot] = rint[x] * fac;
-            gr[slot] = ir > is ? ir : is; /* sort1.F:167-170 */
+            gr[slot] = ir > is ? ir : is; /* sort1.F:109-112 */
             gs[slot] = ir > is ? is : ir;
         }
         off += rec_nt[r];
@@ -517,9 +517,16 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     ref_buffer_sizes(n, nkr, m, (int)(nincl < 16384 ? nincl : 16384), &nijsiz, nsksiz, &nc2);
 
     /* ---------------- TRANS1 (trans1.F:48-103) ---------------- */
+    /* The half-transformed integrals are held per transformed pq block
+     * (slot), slots in ascending pq order: the INTTWO bucket of one JI then
+     * lists its kept values in the order TROUT appended them. */
     long pq_limit = prm->limit_pq > 0 ? prm->limit_pq : nsctr;
-    cplx* hstore = (cplx*)calloc((size_t)nsctr * nji, sizeof(cplx));
-    unsigned char* hkeep = (unsigned char*)calloc((size_t)nsctr * nji, 1);
+    long* slot_of = (long*)malloc(sizeof(long) * (nsctr + 1));
+    for (long pq = 0; pq <= nsctr; pq++) slot_of[pq] = -1;
+    long nslot = 0;
+    long* slot_pq = NULL;
+    cplx* hstore = NULL;
+    unsigned char* hkeep = NULL;
     long npq_done = 0;
     {
         long* pqlist = (long*)malloc(sizeof(long) * (nsctr + 1));
@@ -527,13 +534,27 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
         if (prm->pq_select) {
             for (long t = 0; t < prm->n_pq_select; t++) {
                 long pq = prm->pq_select[t];
-                if (pq >= 1 && pq <= nsctr && bstart[pq + 1] > bstart[pq]) pqlist[npql++] = pq;
+                if (pq >= 1 && pq <= nsctr && bstart[pq + 1] > bstart[pq] && slot_of[pq] < 0) {
+                    slot_of[pq] = 0;
+                    pqlist[npql++] = pq;
+                }
             }
         } else {
             for (long pq = 1; pq <= nsctr && npql < pq_limit; pq++)
-                if (bstart[pq + 1] > bstart[pq]) pqlist[npql++] = pq;
+                if (bstart[pq + 1] > bstart[pq]) {
+                    slot_of[pq] = 0;
+                    pqlist[npql++] = pq;
+                }
         }
         npq_done = npql;
+        slot_pq = (long*)malloc(sizeof(long) * (npql ? npql : 1));
+        for (long pq = 1; pq <= nsctr; pq++)
+            if (slot_of[pq] == 0) {
+                slot_of[pq] = nslot;
+                slot_pq[nslot++] = pq;
+            }
+        hstore = (cplx*)calloc((size_t)(nslot ? nslot : 1) * nji, sizeof(cplx));
+        hkeep = (unsigned char*)calloc((size_t)(nslot ? nslot : 1) * nji, 1);
 #pragma omp parallel
         {
             cplx* ha = (cplx*)malloc(sizeof(cplx) * (size_t)n * m);
@@ -551,7 +572,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                 long nb = bstart[pq + 1] - bstart[pq];
                 if (nb > permcap) { permcap = nb; perm = (long*)realloc(perm, sizeof(long) * permcap); }
                 chunk_reverse_order(nb, 512, perm); /* GETSTI read order, NPQSIZ=512 */
-                /* MATMUL1 (matmul1.F:108-138) */
+                /* MATMUL1 (matmul1.F:3-33) */
                 memset(ha, 0, sizeof(cplx) * (size_t)n * m);
                 for (long x = 0; x < nb; x++) {
                     long e = bstart[pq] + perm[x];
@@ -571,7 +592,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                         for (int l = 0; l < n; l++) tmp = cadd(tmp, cmul(cconj(QA(l, i)), ha[l + (long)j * n]));
                         ri[i + (long)j * m] = tmp;
                     }
-                /* MTIMHER(RIA,RI,+1) (mtimher.F:141-164) */
+                /* MTIMHER(RIA,RI,+1) (mtimher.F:3-26) */
                 for (int i = 1; i <= m; i++)
                     for (int j = 1; j <= m; j++) {
                         int itr = abs(itrmo[i - 1]), jtr = abs(itrmo[j - 1]);
@@ -583,7 +604,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                         cplx h = cadd(cadd(cadd(a, cscal(sg, b)), c), cscal(sg, d));
                         ria[(j - 1) + (long)(i - 1) * m] = h;
                     }
-                /* TROUT (trout.F:165-227) */
+                /* TROUT (trout.F:1-63) */
                 double thrsh = vmx[ip - 1] * vmx[iq - 1];
                 if (thrsh < prm->thrgen) continue;
                 thrsh = prm->thrgen / thrsh;
@@ -596,8 +617,8 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                             ji++;
                             cplx h = ria[(j - 1) + (long)(i - 1) * m];
                             if (cabs_(h) < thrsh) continue;
-                            hstore[(pq - 1) * nji + (ji - 1)] = h;
-                            hkeep[(pq - 1) * nji + (ji - 1)] = 1;
+                            hstore[slot_of[pq] * nji + (ji - 1)] = h;
+                            hkeep[slot_of[pq] * nji + (ji - 1)] = 1;
                         }
                     }
             }
@@ -605,35 +626,35 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
         }
         free(pqlist);
     }
-    /* bucket lists per JI in pq order (INTTWO chains) */
+    /* the AO buckets are not read again */
+    free(gval); free(gr); free(gs);
+    gval = NULL; gr = NULL; gs = NULL;
+    /* bucket list lengths per JI (INTTWO chains) */
     long* jcnt = (long*)calloc(nji + 2, sizeof(long));
-    for (long pq = 1; pq <= nsctr; pq++)
-        for (int ji = 0; ji < nji; ji++) jcnt[ji + 2] += hkeep[(pq - 1) * nji + ji];
+    for (long sl = 0; sl < nslot; sl++)
+        for (int ji = 0; ji < nji; ji++) jcnt[ji + 2] += hkeep[sl * nji + ji];
     for (int ji = 0; ji <= nji; ji++) jcnt[ji + 1] += jcnt[ji];
     long nhalft = jcnt[nji + 1];
-    cplx* hval = (cplx*)malloc(sizeof(cplx) * (nhalft ? nhalft : 1));
-    int* hp = (int*)malloc(sizeof(int) * (nhalft ? nhalft : 1));
-    int* hq = (int*)malloc(sizeof(int) * (nhalft ? nhalft : 1));
-    {
-        long* fill = (long*)calloc(nji + 1, sizeof(long));
-        for (long pq = 1; pq <= nsctr; pq++) {
-            int ip = (int)(0.5 + 0.5 * sqrt((double)(8 * pq - 7)));
-            while ((long)ip * (ip - 1) / 2 >= pq) ip--;
-            while ((long)(ip + 1) * ip / 2 < pq) ip++;
-            int iq = (int)(pq - (long)ip * (ip - 1) / 2);
-            for (int ji = 0; ji < nji; ji++) {
-                if (!hkeep[(pq - 1) * nji + ji]) continue;
-                long s = jcnt[ji + 1] + fill[ji]++;
-                hval[s] = hstore[(pq - 1) * nji + ji];
-                hp[s] = ip;
-                hq[s] = iq;
-            }
-        }
-        free(fill);
+    /* p, q of every slot */
+    int* slot_p = (int*)malloc(sizeof(int) * (nslot ? nslot : 1));
+    int* slot_q = (int*)malloc(sizeof(int) * (nslot ? nslot : 1));
+    for (long sl = 0; sl < nslot; sl++) {
+        long pq = slot_pq[sl];
+        int ip = (int)(0.5 + 0.5 * sqrt((double)(8 * pq - 7)));
+        while ((long)ip * (ip - 1) / 2 >= pq) ip--;
+        while ((long)(ip + 1) * ip / 2 < pq) ip++;
+        slot_p[sl] = ip;
+        slot_q[sl] = (int)(pq - (long)ip * (ip - 1) / 2);
     }
-    free(hstore);
-    free(hkeep);
+    /* timing samples: contiguous lists of a given length instead */
+    cplx* hval = NULL;
+    int* hp = NULL;
+    int* hq = NULL;
     if (prm->fake_list_len > 0) {
+        free(hstore);
+        free(hkeep);
+        hstore = NULL;
+        hkeep = NULL;
         /* timing sample: every JI list has fake_list_len entries */
         long L = prm->fake_list_len;
         free(hval); free(hp); free(hq);
@@ -682,6 +703,9 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
 #pragma omp parallel
         {
             cplx* rj = (cplx*)malloc(sizeof(cplx) * maxmrj);
+            cplx* lv = (cplx*)malloc(sizeof(cplx) * maxmrj); /* the JI list in bucket order */
+            int* lp = (int*)malloc(sizeof(int) * maxmrj);
+            int* lq = (int*)malloc(sizeof(int) * maxmrj);
             cplx* rk = (cplx*)malloc(sizeof(cplx) * (size_t)n * m);
             cplx* rlr = (cplx*)malloc(sizeof(cplx) * (size_t)m * m);
             long* perm = (long*)malloc(sizeof(long) * 16);
@@ -698,18 +722,34 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                     continue;
                 }
                 if (mrj > permcap) { permcap = mrj; perm = (long*)realloc(perm, sizeof(long) * permcap); }
+                if (hstore) { /* gather the JI bucket: kept values in pq order */
+                    long x = 0;
+                    for (long sl = 0; sl < nslot; sl++) {
+                        size_t h = (size_t)sl * nji + (ji - 1);
+                        if (!hkeep[h]) continue;
+                        lv[x] = hstore[h];
+                        lp[x] = slot_p[sl];
+                        lq[x] = slot_q[sl];
+                        x++;
+                    }
+                } else {
+                    for (long x = 0; x < mrj; x++) {
+                        lv[x] = hval[s0 + x];
+                        lp[x] = hp[s0 + x];
+                        lq[x] = hq[s0 + x];
+                    }
+                }
                 chunk_reverse_order(mrj, nijsiz, perm); /* GETHTI read order */
                 for (long x = 0; x < mrj; x++) {
-                    cplx v = hval[s0 + perm[x]];
+                    cplx v = lv[perm[x]];
                     if (conjug) v = cconj(v);
                     if (is < 0) v = cscal(-1.0, v);
                     rj[x] = v;
                 }
-                /* MATMUL3 (matmul3.F:53-84) */
+                /* MATMUL3 (matmul3.F:3-34) */
                 memset(rk, 0, sizeof(cplx) * (size_t)n * m);
                 for (long x = 0; x < mrj; x++) {
-                    long e = s0 + perm[x];
-                    int p = hp[e] - 1, q = hq[e] - 1;
+                    int p = lp[perm[x]] - 1, q = lq[perm[x]] - 1;
                     cplx a = rj[x];
                     for (int k = 0; k < m; k++) {
                         rk[p + (long)k * n] = cadd(rk[p + (long)k * n], cmul(a, QA(q, k)));
@@ -723,7 +763,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                         for (int l = 0; l < n; l++) tmp = cadd(tmp, cmul(cconj(QA(l, i)), rk[l + (long)j * n]));
                         rlr[i + (long)j * m] = tmp;
                     }
-                /* MSUMTIM(RL,RLR,+1) (msumtim.F:87-105) */
+                /* MSUMTIM(RL,RLR,+1) (msumtim.F:3-21) */
                 for (int i = 1; i <= m; i++)
                     for (int j = 1; j <= m; j++) {
                         int itr = abs(itrmo[i - 1]), jtr = abs(itrmo[j - 1]);
@@ -734,7 +774,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                 /* the reduced-matrix-element gather/scatter (trans2.F:199-265)
                  * is the identity for a single one-dimensional irrep */
             }
-            free(rj); free(rk); free(rlr); free(perm);
+            free(rj); free(lv); free(lp); free(lq); free(rk); free(rlr); free(perm);
         }
         /* OUTPP1 / OUTPP2 in TRANS2's loop order (trans2.F:272-310) */
         for (long t = b0; t < b1; t++) {
@@ -782,7 +822,8 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
         free(bk[c]);
     }
     free(items); free(hval); free(hp); free(hq); free(jcnt);
-    free(gval); free(gr); free(gs); free(bstart); free(vmx);
+    free(hstore); free(hkeep); free(slot_of); free(slot_pq); free(slot_p); free(slot_q);
+    free(bstart); free(vmx);
 
     out->nrec = md.nrec;
     out->hdr = md.hdr;
