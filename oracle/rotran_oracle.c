@@ -646,6 +646,9 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
         slot_p[sl] = ip;
         slot_q[sl] = (int)(pq - (long)ip * (ip - 1) / 2);
     }
+    /* TRANS1 ends here; a timing sample's synthetic lists below are not
+     * part of either half's time */
+    double t1 = now_s();
     /* timing samples: contiguous lists of a given length instead */
     cplx* hval = NULL;
     int* hp = NULL;
@@ -671,7 +674,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
         }
         nhalft = L * nji;
     }
-    double t1 = now_s();
+    double t1b = now_s();
 
     /* ---------------- TRANS2 (trans2.F:68-326), one quaternionic irrep ---------------- */
     typedef struct { int i, j; } item;
@@ -836,7 +839,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     out->nij_done = ij_limit;
     out->nij_total = nitems;
     out->t_first = t1 - t0;
-    out->t_second = t2 - t1;
+    out->t_second = t2 - t1b;
     out->t_pp = t3 - t2;
     out->nijsiz = nijsiz;
     out->nc2 = nc2;
