@@ -40,10 +40,12 @@ PROFILE = dict(name="profile_n128_k32", n_l=48, n_s=80, nkr=32, seed=0)
 # the large single transform: 192 L + 288 S AOs, 200 Kramers pairs, AOs in 4
 # irreps with the integrals zero outside the symmetry-allowed blocks
 LARGE = dict(name="large_c2v_n480_k200", n_l=192, n_s=288, nkr=200, seed=0, n_irrep=4)
-# DRAM bytes per k_split_gemm launch measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum, averaged over the launches of one transform); the
-# captures are summarised under profiles/.
+# DRAM bytes per k_split_gemm launch from an ncu launch-list capture of the
+# same transform (dram__bytes_read.sum + dram__bytes_write.sum averaged over
+# its GEMM launches; summary in profiles/launches_split_n400_k120.md).  It is
+# not measured by the run that prints it: the line labels it so.
 TRAFFIC = {"precision_study_n400_k120": 34310516753}
+TRAFFIC_SOURCE = "ncu launch list of this workload (profiles/launches_split_n400_k120.md), not this run"
 
 
 def peaks():
@@ -140,6 +142,61 @@ def dense_equivalent_flops(n, nkr):
     value uses the count of nonzero blocks instead (flops_algorithmic)."""
     m, P = 2 * nkr, n * (n + 1) // 2
     return P * (4.0 * n * n * m + 8.0 * n * m * m) + nkr * (nkr + 1) * (8.0 * n * n * m + 8.0 * n * m * m)
+
+
+def workload_counts(prob):
+    """Integral count and algorithmic FLOPs of a workload, from the generator
+    alone (no device): the dense-block count of the reference algorithm
+    over the transformed pq blocks, GEMM1 over the symmetry-allowed AO
+    blocks (the library's rt_stats.flops_algorithmic)."""
+    mdl = prob.model
+    nl, ns = mdl.n_l, mdl.n_s
+    n, m, k = nl + ns, prob.m, prob.nkr
+    irr, ng = mdl.irrep, mdl.n_irrep
+    comp = [np.arange(nl), np.arange(nl, n)]
+    nb = [[int(np.sum(irr[c] == g)) for g in range(ng)] for c in comp]
+    npair = np.zeros((2, ng), np.int64)
+    for ci, c in enumerate(comp):
+        ir = irr[c]
+        x = ir[:, None] ^ ir[None, :]
+        tri = np.tril(np.ones((c.size, c.size), bool))
+        npair[ci] = np.bincount(x[tri], minlength=ng)[:ng]
+    P = int(npair.sum()) if prob.mfil >= 3 else int(npair[0].sum())
+    f1 = 8.0 * n * m * m * P
+    for ci in range(2 if prob.mfil >= 3 else 1):
+        for gam in range(ng):
+            f1 += npair[ci, gam] * sum(4.0 * nb[cr][g] * nb[cr][g ^ gam] * m
+                                       for cr in range(2) for g in range(ng))
+    f2 = k * (k + 1) * (8.0 * nl * nl * m + 8.0 * ns * ns * m + 8.0 * n * m * m)
+    L, S = npair[0], npair[1]
+    nint = int(sum(L[g] * (L[g] + 1) // 2 + S[g] * L[g] + S[g] * (S[g] + 1) // 2 for g in range(ng)))
+    return nint, float(f1 + f2)
+
+
+def workload_config(work, prob, world):
+    """The `config` object of both arms: the workload only."""
+    nint, flops = workload_counts(prob)
+    return {"workload": work["name"], "n": prob.n, "n_large": work["n_l"], "n_small": work["n_s"],
+            "nkr": work["nkr"], "seed": work["seed"], "n_irrep": work.get("n_irrep", 1),
+            "integrals": nint, "flops_algorithmic": flops,
+            "flops_dense_equivalent": dense_equivalent_flops(prob.n, work["nkr"]),
+            "l2": "inputs larger than L2 (integral records 16 B each)",
+            "parallelism": f"replicas x{world}"}
+
+
+def oracle_check(result, tol):
+    """The MDCINT stream against the oracle's digest of the full
+    precision-study transform (tests/golden), or None without the fixture."""
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import digest_check
+    dg = digest_check.load(digest_check.PRECISION)
+    if dg is None:
+        return None
+    hdr, idx, val = result
+    res = digest_check.check_stream(dg, hdr, idx, val, tol)
+    res["nhalft_oracle"] = int(dg["counts"][0])
+    res["nfinal_oracle"] = [int(x) for x in dg["counts"][2:6]]
+    return res
 
 
 def cpu_sample(work, steps=1, warmup=0, seconds=15.0):
@@ -359,16 +416,22 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        from molfdir_gb300 import synth
+        rprob = synth.make_spinor_problem(work["n_l"], work["n_s"], work["nkr"], seed=work["seed"],
+                                          n_irrep=work.get("n_irrep", 1))
+        config = workload_config(work, rprob, args.gpus)
+        del rprob
         res, cores = cpu_sample(work, steps=args.steps, warmup=args.warmup)
         line = {"metric": "4-index transform TFLOP/s", "impl": "reference",
                 "value": res["tflops"], "unit": "TFLOP/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": res["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": work["name"], "n": work["n_l"] + work["n_s"],
-                           "nkr": work["nkr"], "seed": work["seed"]},
+                "config": config,
                 "cpu_baseline": {"value": res["tflops"], "unit": "TFLOP/s", "cores": cores,
-                                 "kind": "port", "sample": res["sample"]},
+                                 "kind": "port", "sample": res["sample"],
+                                 "seconds_first_half": res["seconds_first_half"],
+                                 "seconds_second_half": res["seconds_second_half"]},
                 "e2e": {"value": res["tflops"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -387,9 +450,11 @@ def main():
 
     prob = synth.make_spinor_problem(work["n_l"], work["n_s"], work["nkr"], seed=work["seed"],
                                      n_irrep=work.get("n_irrep", 1))
+    config = workload_config(work, prob, world)
     cls, its, nts, dv, dl2, dl1 = synth.device_records(prob, 3, device="cuda")
     torch.cuda.synchronize()
     nint = int(nts.sum())
+    assert nint == config["integrals"], "generator and workload count disagree"
 
     def make_ctx(p, slices):
         rt = rotran.Rotran.for_problem(prob, precision=p, slices=slices)
@@ -470,14 +535,18 @@ def main():
                "h2d_bytes_per_step": nint * 16, "d2h_bytes_per_step": nz * 24 + nrec * 12,
                "ms_per_step": esec * 1e3,
                "ms_records_in": phase[0] * 1e3 / ne, "ms_transform": phase[1] * 1e3 / ne,
-               "ms_results_out": phase[2] * 1e3 / ne}
+               "ms_results_out": phase[2] * 1e3 / ne,
+               "h2d_GBps": nint * 16 / (phase[0] / ne) / 1e9,
+               "d2h_GBps": (nz * 24 + nrec * 12) / (phase[2] / ne) / 1e9}
         rt.close()
         del hv, h2, h1, eidx, evalt
 
     # ---- plain FP64 GPU transform: the comparison leg and accuracy reference ----
     fp64 = None
+    ref_result = None
     if prec_name == "split" and not args.no_fp64:
         ref = run_leg(rotran.RT_PREC_FP64, 0, 0, 1)
+        ref_result = ref["result"]
         rh, ri, rv = ref["result"]
         acc = {}
         if np.array_equal(rh, hdr) and np.array_equal(ri, idx):
@@ -539,6 +608,18 @@ def main():
         cpu = {"value": res["tflops"], "unit": "TFLOP/s", "cores": cores, "kind": "port",
                "sample": res["sample"]}
 
+    # ---- the streams against the oracle's digest of this workload ----
+    ocheck = None
+    if rank == 0 and work["name"] == WORKLOAD["name"]:
+        tol = 1e-10 if prec_name == "split" else 1e-12
+        ocheck = {prec_name: oracle_check(main["result"], tol)}
+        if ref_result is not None:
+            ocheck["fp64"] = oracle_check(ref_result, 1e-12)
+        if ocheck[prec_name] is None:
+            ocheck = {"unavailable": "tests/golden/oracle_digest_n400_k120.npz missing"}
+        else:
+            ocheck[prec_name]["nhalft"] = int(st.nhalft)
+
     if rank == 0:
         gsec = main["gemm_ms"] / 1e3
         if prec_name == "split":
@@ -550,6 +631,7 @@ def main():
             roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak / prods,
                     "unit": "TFLOP/s", "frac": achieved / (bf16_peak / prods),
                     "traffic": TRAFFIC.get(work["name"]),
+                    "traffic_source": TRAFFIC_SOURCE if work["name"] in TRAFFIC else None,
                     "kernel": "k_split_gemm (tcgen05 BF16 digit products)",
                     "peak_source": f"bf16_tflops of {peak_kind} / {prods} digit products",
                     "executed_tflops": executed, "executed_frac": executed / bf16_peak,
@@ -565,16 +647,10 @@ def main():
             "ms_per_step": main["sec"] * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16-slices/f32-acc (split)" if prec_name == "split" else "f64",
             "data": "synthetic",
-            "config": {"workload": work["name"], "n": prob.n, "n_large": work["n_l"],
-                       "n_small": work["n_s"], "nkr": work["nkr"], "seed": work["seed"],
-                       "n_irrep": work.get("n_irrep", 1),
-                       "precision": prec_name, "slices": args.slices if prec_name == "split" else None,
-                       "integrals": nint, "flops_algorithmic": flops,
-                       "flops_dense_equivalent": dense_equivalent_flops(prob.n, work["nkr"]),
-                       "tflops_dense_equivalent": dense_equivalent_flops(prob.n, work["nkr"]) * world
-                       / main["sec"] / 1e12,
-                       "l2": "inputs larger than L2 (integral records 16 B each)",
-                       "parallelism": f"replicas x{world}"},
+            "config": config,
+            "precision": {"path": prec_name, "slices": args.slices if prec_name == "split" else None},
+            "tflops_dense_equivalent": config["flops_dense_equivalent"] * world / main["sec"] / 1e12,
+            "oracle_check": ocheck,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64,
             "gpu_launches": st.gpu_launches * args.steps, "clocks": main["clocks"],
             "stats": st.as_dict(), "mdcint": {"records": nrec, "elements": nz},

@@ -124,7 +124,7 @@ void check_config(const rt_config* cfg) {
 }
 
 // AO blocks, pair groups and GEMM1 groups (the pq-block list of
-// makind.F:223-277 and the block structure of the integral files).
+// makind.F:58-112 and the block structure of the integral files).
 void plan_ao(rt_ctx* c) {
     Plan& P = c->plan;
     const rt_config& cfg = c->cfg;
@@ -170,7 +170,7 @@ void plan_ao(rt_ctx* c) {
     for (int p = 0; p < P.n; ++p)
         for (int q = 0; q <= p; ++q) {
             bool pl = p < P.nL, ql = q < P.nL;
-            if (pl != ql) continue;  // no SL blocks for Coulomb (makind.F:240)
+            if (pl != ql) continue;  // no SL blocks for Coulomb (makind.F:75)
             pk.push_back({pl ? 0 : 1, irr(p) ^ irr(q), (long long)p * (p + 1) / 2 + q, p, q});
         }
     std::stable_sort(pk.begin(), pk.end(), [](const PK& a, const PK& b) {
@@ -397,7 +397,7 @@ static void plan_items(rt_ctx* c) {
         }
     }
     w.item_rec0[P.items.size()] = (int)w.recs.size();
-    // VMX (getmos.F:417-423) and the pair screening products
+    // VMX (getmos.F:229-235) and the pair screening products
     std::vector<double> vmx(P.n, 0.0);
     for (int p = 0; p < P.n; ++p)
         for (int i = 0; i < m; ++i) {
@@ -429,6 +429,8 @@ static void plan_items(rt_ctx* c) {
     return RT_OK;
 
 static thread_local std::string g_create_err;
+static const char* const UNUSABLE_MSG =
+    "context unusable: an aborted GEMM could not confirm that its tensor-core work and copies had finished";
 
 void rt::set_thread_error(const std::string& msg) { g_create_err = msg; }
 
@@ -482,7 +484,7 @@ extern "C" int rt_set_coefficients(rt_ctx* ctx, const double* qa, int ld_qa, con
     const int n = ctx->plan.n, m = ctx->plan.m, K = ctx->plan.K;
     if (!qa || !itrmo || !kra || !krb || !ikrmo) throw Error(RT_ERR_USER, "null coefficient table");
     if (ld_qa < n) throw Error(RT_ERR_USER, "ld_qa < NSC");
-    // consistency of the Kramers tables (getmos.F:354-387, kramers.F:114-115)
+    // consistency of the Kramers tables (getmos.F:166-199, kramers.F:114-115)
     for (int i = 0; i < m; ++i) {
         int j = std::abs(itrmo[i]);
         if (j < 1 || j > m || j == i + 1 || itrmo[j - 1] != -(itrmo[i] > 0 ? 1 : -1) * (i + 1))
@@ -772,7 +774,7 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
     for (int p = 0; p < P.n; ++p)
         for (int q = 0; q <= p; ++q) {
             bool pl = p < P.nL, ql = q < P.nL;
-            bool inc = !(!pl && ql) && !(!pl && c->cfg.mfil < 3);  // makind.F:240-242
+            bool inc = !(!pl && ql) && !(!pl && c->cfg.mfil < 3);  // makind.F:75-77
             pqr[(long long)p * (p + 1) / 2 + q] = inc ? 1 : 0;
         }
     std::vector<int> pgroup(P.P), pgs, pgz, aopos(P.n), g1of(P.pgroups.size() * P.nblk, -1), g1k;
@@ -1007,6 +1009,7 @@ double algorithmic_flops(const Plan& P) {
 extern "C" int rt_transform(rt_ctx* ctx) {
     if (!ctx) return RT_ERR_USER;
     API_TRY
+    if (ctx->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
     if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
     Plan& P = ctx->plan;
     Work& w = W(ctx);
@@ -1176,6 +1179,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     if (!ctx) return RT_ERR_USER;
     API_TRY
     if (!gamma || !dedc) throw Error(RT_ERR_USER, "rt_adjoint: null gamma or dEdC");
+    if (ctx->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
     if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
     Plan& P = ctx->plan;
     cudaStream_t st = ctx->stream;
@@ -1235,10 +1239,10 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     double per_item = 32.0 * n * m + 16.0 * ncmax * ncmax + 64.0 * m * m;
     double fixed = 8.0 * nacc + 8192.0;
     if (split) {
-        per_item += 4.0 * m / 1024.0 * 8.0 * nacc;                                  // partials
+        per_item += 4.0 * m / (double)SPLIT_LONG_BLOCK * 8.0 * nacc;                                  // partials
         per_item += std::max(2.0 * s * n * 4.0 * m, 2.0 * s * 2.0 * ncmax * kpc);    // A slices
         per_item += 2.0 * s * 2.0 * m * 4.0 * m + 8.0 * ncmax;                       // B slices, exps
-        per_item += 4.0 * m / 1024.0 * 4.0 * (n + 2.0 * m);                          // split exps
+        per_item += 4.0 * m / (double)SPLIT_LONG_BLOCK * 4.0 * (n + 2.0 * m);                          // split exps
         fixed += 2.0 * s * (n + 2.0 * m) * 64.0 + 8.0 * (n + 2 * m) + 8.0 * nacc + 2048.0;
     } else {
         per_item += 8.0 * nacc / G;
@@ -1285,7 +1289,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
             ++ps.launches;
             __nv_bfloat16* a_sl = (__nv_bfloat16*)carve(2.0 * s * n * Kp);
             __nv_bfloat16* b_sl = (__nv_bfloat16*)carve(2.0 * s * 2.0 * m * Kp);
-            const double nsplit = (double)((Kp + 1023) / 1024);
+            const double nsplit = (double)((Kp + SPLIT_LONG_BLOCK - 1) / SPLIT_LONG_BLOCK);
             int* a_ex = (int*)carve(4.0 * n * nsplit);
             int* b_ex = (int*)carve(8.0 * m * nsplit);
             double* part = (double*)carve(8.0 * nacc * ((Kp / 32 + 31) / 32));
@@ -1684,9 +1688,11 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
 extern "C" int rt_batch_run(rt_batch* b) {
     if (!b) return RT_ERR_USER;
     try {
-        for (BatchInst& I : b->inst)
+        for (BatchInst& I : b->inst) {
+            if (I.c->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
             if (I.c->gen != I.gen)
                 throw Error(RT_ERR_MISMATCH, "a context of the batch changed after rt_batch_create");
+        }
         if (!b->tuned) {
             // tile width per grouped stage: time every stage at 128 and at 64
             const double t0 = 0.0;
@@ -1746,8 +1752,12 @@ extern "C" int rt_batch_run(rt_batch* b) {
         int e = 0;
         RT_CUDA(cudaMemcpy(&e, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
         if (e) {
+            bool unconfirmed = false;
+            const std::string msg = split_status_text(e, &unconfirmed);
+            if (unconfirmed)
+                for (BatchInst& I : b->inst) I.c->unusable = true;
             RT_CUDA(cudaMemset(b->d_err, 0, sizeof(int)));
-            throw Error(RT_ERR_PROGRAM, "grouped split GEMM gave up waiting (status " + std::to_string(e) + ")");
+            throw Error(RT_ERR_PROGRAM, "grouped " + msg);
         }
         int grouped = 0;
         for (SplitGroup* g : b->all) grouped += split_group_size(g) > 0 ? 1 : 0;

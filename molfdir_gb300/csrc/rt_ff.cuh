@@ -3,12 +3,22 @@
 // float-float values into pre-scaled 7-bit BF16 digits.
 //
 // Slicing: every value x of a row (or column) with |x| < 2^S is written as
-//   x ~= 2^S * sum_{t=1..s} d_t 2^(-7t),  d_1 in [-128,128], d_t in [-64,63],
+//   x ~= 2^S * sum_{t=1..s} d_t 2^(-7t),  d_1 in [-128,128], d_t in [-64,64],
 // computed with integer arithmetic on the bit patterns (round to nearest of
 // x * 2^(7s-S), then balanced base-128 digits).  Digit t is stored as the
 // BF16 number d_t * 2^(-7(t-2)) (exact: at most 8 significant bits), so
 // that the product of digits t and u carries the weight 2^(-7(t+u-4)) of the
 // products it is summed with.
+//
+// Exactness of the FP32 sums of the three leading product diagonals (1, 2
+// and 3 digit products per k) over a GEMM depth K: with d_1 in [-128,128] a
+// diagonal reaches 16384, 16384 and 20480 units per k, below 2^24 units for
+// K <= 819 ("narrow" slicing).  Deeper operands are sliced "wide": S one
+// larger (|x| < 2^(S-1)), so every digit lies in [-64,64], at most 4096
+// units per product, exact for K <= 1365, at the cost of one bit.
+constexpr int KMAX_NARROW = 819;
+constexpr int KMAX_EXACT = 1365;
+__host__ __device__ __forceinline__ int slicing_wide(long long K) { return K > KMAX_NARROW ? 1 : 0; }
 #pragma once
 
 #include <cuda_bf16.h>
@@ -45,19 +55,19 @@ __host__ __device__ __forceinline__ double ff_to_double(float2 a) {
     return (double)a.x + (double)a.y;
 }
 
-// exponent S with |x| < 2^S for a double (S = -2000 for zero/denormal)
-__host__ __device__ __forceinline__ int scale_exp_f64(double x) {
+// slicing exponent S of a double: |x| < 2^(S-wide) (S = -2000 for zero/denormal)
+__host__ __device__ __forceinline__ int scale_exp_f64(double x, int wide) {
     union { double d; uint64_t u; } v;
     v.d = x;
     int e = (int)((v.u >> 52) & 0x7FF);
-    return e == 0 ? -2000 : e - 1022;
+    return e == 0 ? -2000 : e - 1022 + wide;
 }
 
-__host__ __device__ __forceinline__ int scale_exp_f32(float x) {
+__host__ __device__ __forceinline__ int scale_exp_f32(float x, int wide) {
     union { float f; uint32_t u; } v;
     v.f = x;
     int e = (int)((v.u >> 23) & 0xFF);
-    return e == 0 ? -2000 : e - 126;
+    return e == 0 ? -2000 : e - 126 + wide;
 }
 
 // round(|m| * 2^shift) for a non-negative integer mantissa m (< 2^53)
@@ -135,8 +145,9 @@ __device__ __forceinline__ float2 ff_from_double(double x) {
 }
 
 // Digits of a float-float value y = yh + yl with |y| < 1 (already scaled by
-// 2^-S): d_1 = rint(128 yh) in [-128,128], then d_t in [-64,64]; each step
-// is exact (products by 128, rint, Sterbenz subtraction, TwoSum).
+// 2^-S): d_1 = rint(128 yh) in [-128,128] ([-64,64] when |y| < 1/2, wide
+// slicing), then d_t in [-64,64]; each step is exact (products by 128, rint,
+// Sterbenz subtraction, TwoSum).
 // Writes the pre-scaled BF16 digits d_t * 2^(-7(t-2)) to out[t].
 template <int S>
 __device__ __forceinline__ void ff_digits(float yh, float yl, __nv_bfloat16* out) {

@@ -15,6 +15,8 @@
 #include <thread>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "../../include/rotran_gb300.h"
 #include "rt_access.h"
 
@@ -28,8 +30,18 @@ struct File {
     }
 };
 
+// Bytes left between the read position of f and the end of its file.
+long long file_left(FILE* f) {
+    struct stat st;
+    const long long pos = ftell(f);
+    if (pos < 0 || fstat(fileno(f), &st) != 0) return -1;
+    return (long long)st.st_size - pos;
+}
+
 // Read one sequential unformatted record (with gfortran subrecords).
-// Returns 1 on success, 0 at end of file, -1 on a malformed record.
+// Returns 1 on success, 0 at end of file, -1 on a malformed record (also a
+// length marker that claims more bytes than the file has left, which is
+// rejected before any buffer is sized from it).
 int read_record(FILE* f, std::vector<char>& buf) {
     buf.clear();
     for (;;) {
@@ -38,6 +50,7 @@ int read_record(FILE* f, std::vector<char>& buf) {
         if (got != 1) return buf.empty() ? 0 : -1;
         bool more = head < 0;
         long long len = more ? -(long long)head : head;
+        if (len + 4 > file_left(f)) return -1;
         size_t old = buf.size();
         buf.resize(old + len);
         if (len && fread(buf.data() + old, 1, len, f) != (size_t)len) return -1;
@@ -105,12 +118,13 @@ struct SrtpqSet {
 // type-1 occupies [start[g], start[g+1]) of v / l2 / l1 -- the layout of
 // rt_add_ao_records_bulk with one record per non-empty group.
 struct SrtpqBlock {
-    // storage grows but is never value-initialised (every slot is written)
+    // an array of at least n elements (new T[n]: allocated, not
+    // value-initialised; every slot is written before it is read)
     template <class T>
     struct Buf {
         std::unique_ptr<T[]> p;
         size_t cap = 0;
-        void reserve(size_t n) {
+        void grow_to(size_t n) {
             if (n > cap) {
                 p.reset(new T[n]);
                 cap = n;
@@ -229,7 +243,7 @@ void srtpq_read(const char* dir, int nranks, int nsc, int nsc1, Sink&& sink) {
             const long long pos = (k0 - 1) * (long long)irecl;
             // the last record may end short of IRECL
             const long long want = std::min<long long>(nb * (long long)irecl, fsize - pos);
-            block.reserve((size_t)nb * irecl);
+            block.grow_to((size_t)nb * irecl);
             if (want < (nb - 1) * (long long)irecl + 12 ||
                 fread(block.data(), 1, (size_t)want, fi.f) != (size_t)want)
                 throw SrtpqError{RT_ERR_EOF, "READ ERROR ON FILE SRTPQIL.*: " + pil + " records " +
@@ -283,9 +297,9 @@ void srtpq_read(const char* dir, int nranks, int nsc, int nsc1, Sink&& sink) {
                 }
             }
             out.start[42] = base;
-            out.v.reserve((size_t)base);  // reused from block to block
-            out.l2.reserve((size_t)base);
-            out.l1.reserve((size_t)base);
+            out.v.grow_to((size_t)base);  // reused from block to block
+            out.l2.grow_to((size_t)base);
+            out.l1.grow_to((size_t)base);
             srtpq_parallel(t, nb, [&](int w, long long a, long long b) {
                 std::array<long long, 42> o = off[w];
                 srtpq_decode(block.data(), irecl, hd.data(), a, b, nsc, nsc1,
@@ -388,7 +402,7 @@ extern "C" int rt_read_srtpq_files(rt_ctx* ctx, const char* dir, int nranks) {
     }
 }
 
-// SORT1's file loop (sort1.F:118-205) with GETTW's record reads (gettw.F:15-29).
+// SORT1's file loop (sort1.F:60-147) with GETTW's record reads (gettw.F:15-29).
 extern "C" int rt_read_srt_files(rt_ctx* ctx, const char* dir) {
     if (!ctx || !dir) return RT_ERR_USER;
     static const char* tw[3] = {"SRTTWLL", "SRTTWSL", "SRTTWSS"};
@@ -400,7 +414,7 @@ extern "C" int rt_read_srt_files(rt_ctx* ctx, const char* dir) {
         File fa(fopen(pa.c_str(), "rb")), fb(fopen(pb.c_str(), "rb"));
         if (!fa.f || !fb.f) {
             rt_internal_set_error(ctx, ("UNABLE TO OPEN SRT FILE " + (fa.f ? pb : pa)).c_str());
-            return RT_ERR_EOF;  // sort1.F:227, Q2JOB(1,...)
+            return RT_ERR_EOF;  // sort1.F:169, Q2JOB(1,...)
         }
         for (;;) {
             int ra = read_record(fa.f, a), rb = read_record(fb.f, b);
@@ -443,8 +457,8 @@ extern "C" int rt_read_srt_files(rt_ctx* ctx, const char* dir) {
     return RT_OK;
 }
 
-// INITTWOE header (inittwoe.F:139-141), PPSYM records (ppsym.F:89-91) and
-// EXITTWOE terminator (exittwoe.F:149).
+// INITTWOE header (inittwoe.F:21-23), PPSYM records (ppsym.F:89-91) and
+// EXITTWOE terminator (exittwoe.F:6).
 extern "C" int rt_write_mdcint(rt_ctx* ctx, const char* path, const char* datex10,
                                const char* timex8) {
     if (!ctx || !path) return RT_ERR_USER;

@@ -737,7 +737,8 @@ __global__ void __launch_bounds__(256) k_expand_rows(const double* __restrict__ 
         for (int i = warp; i < rows; i += nw) {
             const double* p = tile + i * nk;
             int S = -2000;
-            for (int k = lane; k < nk; k += 32) S = max(S, scale_exp_f64(p[k]));
+            const int wide = slicing_wide(nk);
+            for (int k = lane; k < nk; k += 32) S = max(S, scale_exp_f64(p[k], wide));
             for (int q = 16; q; q >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, q));
             const long long row = (long long)(J.r_lo + i) * npc + pql;
             if (lane == 0) out_exp[J.exp_pp * npc + row] = S;

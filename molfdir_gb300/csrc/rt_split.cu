@@ -4,10 +4,14 @@
 // computed from s BF16 digit slices per operand (row scales for A, column
 // scales for B; see rt_ff.cuh) on the tcgen05 tensor cores:
 //
-//   acc0 = sum_k a_1 b_1                       exact in FP32 (K <= 1024)
-//   acc1 = sum_k a_1 b_2 + a_2 b_1             exact in FP32 (K <= 1024)
-//   acc2 = sum_k a_1 b_3 + a_2 b_2 + a_3 b_1   exact in FP32 (K <= 1024)
+//   acc0 = sum_k a_1 b_1                       exact in FP32
+//   acc1 = sum_k a_1 b_2 + a_2 b_1             exact in FP32
+//   acc2 = sum_k a_1 b_3 + a_2 b_2 + a_3 b_1   exact in FP32
 //   acc3 = sum_k sum_{t+u>=5} a_t b_u          FP32 (relative weight 2^-21)
+//
+// (exact for K <= 819 with narrow slicing and K <= 1365 with wide slicing,
+// rt_ff.cuh; every operand is sliced for its GEMM's depth, split-K splits
+// for theirs, and deeper GEMMs are refused)
 //
 // (the tensor cores' FP32 accumulation of rounded sums behaves like about
 // 20 significant bits, so every product diagonal whose error would show
@@ -45,7 +49,17 @@ namespace rt {
 constexpr int SBM = 128, SBN = 128, SBK = 32, NSTAGE = 2, MAX_SLICES = 6;
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
-enum : int { ERR_TIMEOUT_EMPTY = 1, ERR_TIMEOUT_FULL = 2, ERR_TIMEOUT_TMEM = 3 };
+// Status word of a GEMM launch: the first wait that ran out (low byte), and
+// two bits for an abort that could not confirm its own clean-up -- MMAs
+// still writing TMEM when it was freed, or TMA copies still landing in shared
+// memory when the CTA left.  Those leave the device state in doubt.
+enum : int {
+    ERR_TIMEOUT_EMPTY = 1,
+    ERR_TIMEOUT_FULL = 2,
+    ERR_TIMEOUT_TMEM = 3,
+    ERR_DRAIN_UNCONFIRMED = 1 << 8,
+    ERR_COPIES_UNCONFIRMED = 1 << 9
+};
 
 // ---------------------------------------------------------------------------
 // slicing kernels
@@ -72,8 +86,8 @@ struct RowsFF {  // contiguous float-float rows of length K (stride ld)
 // exponent S with |value| < 2^S.
 __device__ __forceinline__ float2 ff_load(const double* p) { return ff_from_double(*p); }
 __device__ __forceinline__ float2 ff_load(const float2* p) { return *p; }
-__device__ __forceinline__ int exp_load(const double* p) { return scale_exp_f64(*p); }
-__device__ __forceinline__ int exp_load(const float2* p) { return scale_exp_f32(p->x); }
+__device__ __forceinline__ int exp_load(const double* p, int wide) { return scale_exp_f64(*p, wide); }
+__device__ __forceinline__ int exp_load(const float2* p, int wide) { return scale_exp_f32(p->x, wide); }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
     return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
@@ -90,8 +104,9 @@ __global__ void __launch_bounds__(256) k_slice_rows(Src src, long long M, int K,
     for (long long i = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < M;
          i += warps) {
         const auto* p = src.row(i);
+        const int wide = slicing_wide(K);
         int S = -2000;
-        for (int k = lane; k < K; k += 32) S = max(S, exp_load(p + k));
+        for (int k = lane; k < K; k += 32) S = max(S, exp_load(p + k, wide));
         for (int o = 16; o; o >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, o));
         if (lane == 0) exps[i] = S;
         const float sc = pow2f_safe(-S);
@@ -126,8 +141,9 @@ __global__ void __launch_bounds__(256) k_slice_cols(const float2* __restrict__ s
     const long long n0 = (long long)blockIdx.x * 32;
     const long long n = n0 + tx;
     int S = -2000;
+    const int wide = slicing_wide(K);
     if (n < N)
-        for (int k = ty; k < K; k += 8) S = max(S, scale_exp_f32(src[(long long)k * ld + n].x));
+        for (int k = ty; k < K; k += 8) S = max(S, scale_exp_f32(src[(long long)k * ld + n].x, wide));
     part[ty][tx] = S;
     __syncthreads();
     S = part[0][tx];
@@ -205,7 +221,7 @@ static void host_slice_rows(const std::vector<double>& a, int M, int K, int Kp, 
     exps.assign(M, -2000);
     for (int i = 0; i < M; ++i) {
         int S = -2000;
-        for (int k = 0; k < K; ++k) S = std::max(S, scale_exp_f64(a[(size_t)i * K + k]));
+        for (int k = 0; k < K; ++k) S = std::max(S, scale_exp_f64(a[(size_t)i * K + k], slicing_wide(K)));
         exps[i] = S;
         if (S < -1000) continue;
         for (int k = 0; k < K; ++k) {
@@ -224,7 +240,7 @@ static void host_slice_cols(const double* b, int K, int N, long long ld, int Kp,
     exps.assign(N, -2000);
     for (int j = 0; j < N; ++j) {
         int S = -2000;
-        for (int k = 0; k < K; ++k) S = std::max(S, scale_exp_f64(b[(size_t)k * ld + j]));
+        for (int k = 0; k < K; ++k) S = std::max(S, scale_exp_f64(b[(size_t)k * ld + j], slicing_wide(K)));
         exps[j] = S;
         if (S < -1000) continue;
         for (int k = 0; k < K; ++k) {
@@ -330,7 +346,9 @@ __device__ __forceinline__ TileRef tile_ref(const Tab& tab, long long t) {
 
 // The GEMM body: BN = output tile width (128 or 64), s slices.
 template <int BN, class Epi, class Tab>
-__device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* error) {
+__device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* error,
+                                                unsigned long long wait_ns = WAIT_NS,
+                                                bool no_copies = false) {
     constexpr uint32_t TCOLS = 4 * BN;  // four accumulators of BN columns
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[NSTAGE], empty[NSTAGE], tfull, tempty, tdrain;
@@ -372,13 +390,14 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
                 for (int kb = r.kb0; kb < r.kb1; ++kb, ++gk) {
                     const int st = (int)(gk % NSTAGE);
                     const uint32_t ph = (uint32_t)((gk / NSTAGE) & 1);
-                    if (!mbar_wait_bounded(&empty[st], ph ^ 1u, &abort_flag, WAIT_NS)) {
+                    if (!mbar_wait_bounded(&empty[st], ph ^ 1u, &abort_flag, wait_ns)) {
                         if (!abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_EMPTY);
                         abort_flag = 1;
                         break;
                     }
                     unsigned char* base = smem + (size_t)st * stage_bytes;
                     mbar_expect_tx(&full[st], stage_bytes);
+                    if (no_copies) continue;  // test hook: the MMA waits then run out
                     // all s slices of each operand tile in one 3D box
                     tma_load_3d(base, ma, &full[st], kb * SBK, (int)(r.tm * SBM), 0);
                     tma_load_3d(base + (size_t)s * slice_a, mb, &full[st], kb * SBK,
@@ -394,7 +413,7 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
             long long gk = 0;
             int it = 0;
             for (long long tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x, ++it) {
-                if (it > 0 && !mbar_wait_bounded(&tempty, (uint32_t)((it - 1) & 1), &abort_flag, WAIT_NS)) {
+                if (it > 0 && !mbar_wait_bounded(&tempty, (uint32_t)((it - 1) & 1), &abort_flag, wait_ns)) {
                     if (!abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_TMEM);
                     abort_flag = 1;
                     break;
@@ -405,7 +424,7 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
                 for (int kb = r.kb0; kb < r.kb1; ++kb, ++gk) {
                     const int st = (int)(gk % NSTAGE);
                     const uint32_t ph = (uint32_t)((gk / NSTAGE) & 1);
-                    if (!mbar_wait_bounded(&full[st], ph, &abort_flag, WAIT_NS)) {
+                    if (!mbar_wait_bounded(&full[st], ph, &abort_flag, wait_ns)) {
                         if (!abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_FULL);
                         abort_flag = 1;
                         break;
@@ -436,7 +455,7 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
             // (after an abort, the last ones were never waited for)
             umma_commit(&tdrain);
             volatile int never = 0;
-            mbar_wait_bounded(&tdrain, 0, &never, WAIT_NS);
+            if (!mbar_wait_bounded(&tdrain, 0, &never, WAIT_NS)) atomicOr(error, ERR_DRAIN_UNCONFIRMED);
         }
     } else {  // ---- epilogue: warps 2..9; lane group warp%4, column half (warp-2)/4 ----
         const int ew = warp - 2;
@@ -462,7 +481,7 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
             }
             __syncwarp();
             const bool ready = __all_sync(
-                0xffffffffu, mbar_wait_bounded(&tfull, (uint32_t)(it & 1), &abort_flag, WAIT_NS));
+                0xffffffffu, mbar_wait_bounded(&tfull, (uint32_t)(it & 1), &abort_flag, wait_ns));
             if (!ready) {
                 if (lane == 0 && !abort_flag) atomicCAS(error, 0, ERR_TIMEOUT_TMEM);
                 abort_flag = 1;
@@ -513,19 +532,254 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
         // let the outstanding tensor copies of this CTA land before exit
         volatile int never = 0;
         for (int st = 0; st < NSTAGE; ++st)
-            if (issued[st]) mbar_wait_bounded(&full[st], (uint32_t)(issued[st] - 1), &never, WAIT_NS);
+            if (issued[st] && !mbar_wait_bounded(&full[st], (uint32_t)(issued[st] - 1), &never, WAIT_NS))
+                atomicOr(error, ERR_COPIES_UNCONFIRMED);
     }
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, TCOLS);
+}
+
+// ---------------------------------------------------------------------------
+// The CTA-pair GEMM: clusters of two CTAs, one 2-SM MMA (tcgen05.mma
+// cta_group::2, M = 256, N = 128) issued by the even CTA.  Each CTA stages its
+// 128 rows of A and half (64 columns) of B -- 12 KB per slice and K block
+// instead of 16 KB -- so three pipeline stages fit, and the shared-memory
+// fill per output element is 3/4 of the single-CTA kernel's.  Both CTAs'
+// tensor copies count on the even CTA's full barriers; MMA completion is
+// multicast to both CTAs' empty and accumulator barriers; each CTA drains its
+// own TMEM lanes (its 128 rows) and signals the even CTA.
+// ---------------------------------------------------------------------------
+constexpr int PSTAGE = 3, PBM = 256, PBN = 128;
+
+// The j-th tile of pair `pair` (npairs pairs).  One problem: the tiles of
+// the shorter dimension are taken together (a strip), so the tile of the
+// longer operand is read from DRAM once and then from L2 by the same pair.
+template <class Epi>
+__device__ __forceinline__ bool pair_next(const OneProblem<Epi>& tab, long long pair, long long j,
+                                          long long npairs, TileRef& r) {
+    const SplitArgs& g = tab.g;
+    const bool mshort = g.tiles_m <= g.tiles_n;
+    const long long U = mshort ? g.tiles_m : g.tiles_n, L = mshort ? g.tiles_n : g.tiles_m;
+    const long long strip = pair + (j / U) * npairs;
+    if (strip >= L) return false;
+    const long long inner = j - (j / U) * U;
+    r.p = 0;
+    r.ks = 0;
+    r.kb0 = 0;
+    r.kb1 = g.Kp / SBK;
+    r.tm = mshort ? inner : strip;
+    r.tn = mshort ? strip : inner;
+    return true;
+}
+
+template <class Epi, class Tab>
+__device__ __forceinline__ void split_gemm_pair_body(const Tab& tab, int s, int* error,
+                                                     unsigned long long wait_ns, bool no_copies) {
+    constexpr uint32_t TCOLS = 4 * PBN;  // four accumulators of 128 columns
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[PSTAGE], empty[PSTAGE], tfull, tempty, tdrain;
+    __shared__ uint32_t tbase;
+    __shared__ volatile int abort_flag;
+    __shared__ float fcol_w[EPI_WARPS][PBN / 2];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t slice_a = (PBM / 2) * SBK * 2, slice_b = (PBN / 2) * SBK * 2;
+    const uint32_t stage_bytes = (uint32_t)s * (slice_a + slice_b);  // per CTA
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_ctarank();
+    const long long pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < PSTAGE; ++i) {
+            mbar_init(&full[i], 1);   // the even CTA's producer (expects both CTAs' bytes)
+            mbar_init(&empty[i], 1);  // one multicast MMA commit per use of the stage
+        }
+        mbar_init(&tfull, 1);
+        mbar_init(&tempty, 2 * EPI_WARPS);  // the epilogue warps of both CTAs
+        mbar_init(&tdrain, 1);
+        abort_flag = 0;
+        mbar_fence_init();
+    }
+    if (warp == 0) tmem_alloc_pair(&tbase, TCOLS);
+    tc_fence_before();
+    cluster_sync();  // barriers of both CTAs initialised, TMEM allocated
+    tc_fence_after();
+    const uint32_t tmem = tbase;
+    const uint32_t abort_peer = mapa_shared(smem_u32((const void*)&abort_flag), rank ^ 1u);
+    // give up: record the first cause, stop both CTAs' roles
+    auto give_up = [&](int code) {
+        if (!abort_flag) atomicCAS(error, 0, code);
+        abort_flag = 1;
+        st_cluster_u32(abort_peer, 1u);
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {  // ---- TMA producer (both CTAs) ----
+            uint32_t fullc[PSTAGE];
+            for (int i = 0; i < PSTAGE; ++i) fullc[i] = mapa_shared(smem_u32(&full[i]), 0);
+            long long gk = 0;
+            TileRef r;
+            for (long long j = 0; !abort_flag && pair_next(tab, pair, j, npairs, r); ++j) {
+                const CUtensorMap* ma = tab.mapA(r.p);
+                const CUtensorMap* mb = tab.mapB(r.p);
+                for (int kb = r.kb0; kb < r.kb1; ++kb, ++gk) {
+                    const int st = (int)(gk % PSTAGE);
+                    const uint32_t ph = (uint32_t)((gk / PSTAGE) & 1);
+                    if (!mbar_wait_bounded(&empty[st], ph ^ 1u, &abort_flag, wait_ns)) {
+                        if (!abort_flag) give_up(ERR_TIMEOUT_EMPTY);
+                        break;
+                    }
+                    if (rank == 0) mbar_expect_tx(&full[st], 2 * stage_bytes);
+                    if (no_copies) continue;  // test hook: the MMA waits then run out
+                    unsigned char* base = smem + (size_t)st * stage_bytes;
+                    tma_load_3d_pair(base, ma, fullc[st], kb * SBK, (int)(r.tm * PBM + rank * (PBM / 2)), 0);
+                    tma_load_3d_pair(base + (size_t)s * slice_a, mb, fullc[st], kb * SBK,
+                                     (int)(r.tn * PBN + rank * (PBN / 2)), 0);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 0) {  // ---- MMA issuer (even CTA) ----
+            const uint32_t idesc = umma_idesc_bf16(PBM, PBN);
+            long long gk = 0;
+            int it = 0;
+            TileRef r;
+            for (long long j = 0; !abort_flag && pair_next(tab, pair, j, npairs, r); ++j, ++it) {
+                if (it > 0 && !mbar_wait_bounded(&tempty, (uint32_t)((it - 1) & 1), &abort_flag, wait_ns)) {
+                    if (!abort_flag) give_up(ERR_TIMEOUT_TMEM);
+                    break;
+                }
+                tc_fence_after();
+                bool started[4] = {false, false, false, false};
+                for (int kb = r.kb0; kb < r.kb1; ++kb, ++gk) {
+                    const int st = (int)(gk % PSTAGE);
+                    const uint32_t ph = (uint32_t)((gk / PSTAGE) & 1);
+                    if (!mbar_wait_bounded(&full[st], ph, &abort_flag, wait_ns)) {
+                        if (!abort_flag) give_up(ERR_TIMEOUT_FULL);
+                        break;
+                    }
+                    tc_fence_after();
+                    unsigned char* base = smem + (size_t)st * stage_bytes;
+                    for (int t = 0; t < s; ++t)
+                        for (int u = 0; u + t < s; ++u) {
+                            const int acc = t + u < 3 ? t + u : 3;
+                            const uint32_t dt = tmem + (uint32_t)(acc * PBN);
+                            const uint64_t da = umma_sdesc(base + t * slice_a, 512, UMMA_SWIZZLE_64B);
+                            const uint64_t db = umma_sdesc(base + (size_t)s * slice_a + u * slice_b, 512,
+                                                           UMMA_SWIZZLE_64B);
+#pragma unroll
+                            for (int kk = 0; kk < SBK / 16; ++kk) {
+                                umma_bf16_pair(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc,
+                                               started[acc] ? 1u : 0u);
+                                started[acc] = true;
+                            }
+                        }
+                    umma_commit_pair(&empty[st], (uint16_t)3);
+                }
+                if (abort_flag) break;
+                umma_commit_pair(&tfull, (uint16_t)3);
+            }
+            // every MMA issued completes before TMEM is freed
+            umma_commit_pair(&tdrain, (uint16_t)1);
+            volatile int never = 0;
+            if (!mbar_wait_bounded(&tdrain, 0, &never, WAIT_NS)) atomicOr(error, ERR_DRAIN_UNCONFIRMED);
+        }
+    } else {  // ---- epilogue: warps 2..9 of both CTAs; lane group warp%4, column half (warp-2)/4 ----
+        const int ew = warp - 2;
+        const int lg = warp & 3;
+        const int chalf = ew >> 2;
+        const uint32_t lane_base = (uint32_t)(lg * 32) << 16;
+        const uint32_t tempty0 = mapa_shared(smem_u32(&tempty), 0);
+        int it = 0;
+        TileRef r;
+        for (long long j = 0; pair_next(tab, pair, j, npairs, r); ++j, ++it) {
+            if (__any_sync(0xffffffffu, abort_flag != 0)) break;
+            const SplitArgs& g = tab.args(r.p);
+            const long long ks = r.ks, tm = r.tm, tn = r.tn;
+            float* fcol = fcol_w[ew];
+            __syncwarp();
+            for (int jj = lane; jj < PBN / 2; jj += 32) {
+                const long long col = tn * PBN + chalf * (PBN / 2) + jj;
+                const int e = col < g.N ? g.col_exp[ks * g.N + col] : -2000;
+                fcol[jj] = e < -1000 ? 0.0f : pow2f_safe(e);
+            }
+            __syncwarp();
+            const bool ready = __all_sync(
+                0xffffffffu, mbar_wait_bounded(&tfull, (uint32_t)(it & 1), &abort_flag, wait_ns));
+            if (!ready) {
+                if (lane == 0) give_up(ERR_TIMEOUT_TMEM);
+                break;
+            }
+            tc_fence_after();
+            const long long row = tm * PBM + rank * (PBM / 2) + lg * 32 + lane;
+            const int erow = row < g.M ? g.row_exp[ks * g.M + row] : -2000;
+            const float frow = erow < -1000 ? 0.0f : pow2f_safe(erow - 28);
+            const auto& epi = tab.epi(r.p);
+            const typename Epi::Row er = epi.row(ks * g.M + (row < g.M ? row : 0));
+            for (int c0 = chalf * (PBN / 2); c0 < (chalf + 1) * (PBN / 2); c0 += EC) {
+                uint32_t r0[EC], r1[EC], r2[EC], r3[EC];
+                tmem_ld16(tmem + lane_base + (uint32_t)c0, r0);
+                if (s >= 2) tmem_ld16(tmem + lane_base + (uint32_t)(PBN + c0), r1);
+                if (s >= 3) tmem_ld16(tmem + lane_base + (uint32_t)(2 * PBN + c0), r2);
+                if (s >= 4) tmem_ld16(tmem + lane_base + (uint32_t)(3 * PBN + c0), r3);
+                tmem_ld_wait();
+                if (c0 + EC == (chalf + 1) * (PBN / 2)) {  // this warp's accumulators drained
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive_cluster(tempty0);
+                }
+                if (row >= g.M) continue;
+#pragma unroll
+                for (int jj = 0; jj < EC; ++jj) {
+                    const float a0 = __uint_as_float(r0[jj]);
+                    const float a1 = s >= 2 ? __uint_as_float(r1[jj]) : 0.f;
+                    const float a2 = s >= 3 ? __uint_as_float(r2[jj]) : 0.f;
+                    const float a3 = s >= 4 ? __uint_as_float(r3[jj]) : 0.f;
+                    float s1, e1, s2, e2, s3, e3, hi, lo;
+                    two_sum(a0, a1, s1, e1);
+                    two_sum(s1, a2, s2, e2);
+                    two_sum(s2, a3, s3, e3);
+                    fast_two_sum(s3, (e1 + e2) + e3, hi, lo);
+                    const float f = fcol[c0 - chalf * (PBN / 2) + jj] * frow;  // 2^(erow+ecol-28)
+                    r0[jj] = __float_as_uint(hi * f);
+                    r1[jj] = __float_as_uint(lo * f);
+                }
+                epi.store(er, tn * PBN + c0, g.N, r0, r1);
+            }
+        }
+    }
+    // Both CTAs meet before either frees TMEM or leaves: no CTA exits while
+    // the other can still write its shared memory or barriers.  After an
+    // abort (every wait above is bounded, so both get here), tensor copies
+    // either CTA issued may still be landing; their completion counts on the
+    // even CTA's barriers, which an aborted pipeline may never complete, so
+    // the CTA waits a fixed 1 ms -- far longer than a copy takes.
+    tc_fence_before();
+    cluster_sync();
+    if (abort_flag && threadIdx.x == 0) {
+        const unsigned long long t0 = global_ns();
+        while (global_ns() - t0 < 1000000ull) {
+        }
+    }
+    cluster_sync();
+    tc_fence_after();
+    __syncwarp();
+    if (warp == 0) tmem_dealloc_pair(tmem, TCOLS);
+}
+
+template <class Epi>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GEMM_THREADS, 1)
+    k_split_gemm_pair(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                      SplitArgs g, Epi epi, unsigned long long wait_ns, int no_copies) {
+    const OneProblem<Epi> tab{&mapA, &mapB, g, epi};
+    split_gemm_pair_body<Epi>(tab, g.s, g.error, wait_ns, no_copies != 0);
 }
 
 // One problem: operands through kernel-parameter tensor maps.
 template <int BN, class Epi>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                 SplitArgs g, Epi epi) {
+                 SplitArgs g, Epi epi, unsigned long long wait_ns, int no_copies) {
     const OneProblem<Epi> tab{&mapA, &mapB, g, epi};
-    split_gemm_body<BN, Epi>(tab, g.s, g.error);
+    split_gemm_body<BN, Epi>(tab, g.s, g.error, wait_ns, no_copies != 0);
 }
 
 // A group of problems (one persistent launch over all their tiles).
@@ -632,6 +886,7 @@ struct SplitState {
     int s = 6;
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     int num_sms = 152;
+    int max_pairs = 0;  // CTA pairs of the pair kernel resident at once
     // constant operands
     ConstSlices qah;                 // A of GEMM2/4: rows 2m, K = 2n
     ConstSlices qahB;                // the barred rows of qah (both planes): rows m
@@ -650,6 +905,43 @@ struct SplitState {
 };
 
 static int kpad(int K) { return (K + SBK - 1) / SBK * SBK; }
+
+// dynamic shared memory of the pair kernel: PSTAGE stages of s slices of a
+// 128-row A tile and a 64-column B tile, plus the 1024-byte alignment slack
+static size_t pair_smem_bytes(int s) {
+    return (size_t)PSTAGE * s * (PBM / 2 + PBN / 2) * SBK * 2 + 1024;
+}
+
+// Clusters of two CTAs of a pair kernel that can be resident together (a
+// persistent grid larger than that would run a second wave).
+static int pair_capacity(const void* kernel, size_t smem, int num_sms) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(num_sms & ~1), 1, 1);
+    cfg.blockDim = dim3(GEMM_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kernel, &cfg) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        throw Error(RT_ERR_PROGRAM, "no CTA pair of the split GEMM fits on this device");
+    }
+    return std::min(n, num_sms / 2);
+}
+
+// Test hook for the GEMM's abort path: with RT_TEST_GEMM_NO_COPIES=1 in the
+// environment a launch issues no tensor copies and gives its waits 50 ms, so
+// the waits run out, the kernel stops all its roles and reports status 2
+// (class 6 on the host) without faulting; the context stays usable.
+static bool test_no_copies() {
+    const char* e = getenv("RT_TEST_GEMM_NO_COPIES");
+    return e && e[0] == '1';
+}
 
 static void* salloc(SplitState* S, size_t bytes) {
     void* p = nullptr;
@@ -699,6 +991,11 @@ static SplitState* state(rt_ctx* c) {
         set_smem_limit(k_split_gemm<128, EpiFF_HA>, need, prop);
         set_smem_limit(k_split_gemm<128, EpiFF_RowMajor>, need, prop);
         set_smem_limit(k_split_gemm<128, EpiFF_RK>, need, prop);
+        const size_t need2 = pair_smem_bytes(S->s);
+        set_smem_limit(k_split_gemm_pair<EpiFF_HA>, need2, prop);
+        set_smem_limit(k_split_gemm_pair<EpiFF_RowMajor>, need2, prop);
+        set_smem_limit(k_split_gemm_pair<EpiFF_RK>, need2, prop);
+        S->max_pairs = pair_capacity((const void*)k_split_gemm_pair<EpiFF_RowMajor>, need2, S->num_sms);
         c->split = S;
     }
     return c->split;
@@ -721,8 +1018,9 @@ void split_prepare_constants(rt_ctx* c) {
     SplitState* S = state(c);
     const Plan& P = c->plan;
     const int n = P.n, m = P.m, s = S->s;
-    if (2 * n > 1024)
-        throw Error(RT_ERR_DIM, "split path: 2*NSC > 1024 exceeds the exact FP32 accumulation range");
+    if (2 * n > KMAX_EXACT)
+        throw Error(RT_ERR_DIM, "split path: 2*NSC > " + std::to_string(KMAX_EXACT) +
+                                    " exceeds the exact FP32 accumulation range");
     // planar QA in sorted AO order
     std::vector<double> qr((size_t)n * m), qi((size_t)n * m);
     for (int p = 0; p < n; ++p)
@@ -885,24 +1183,54 @@ static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M,
     g.tiles_n = (int)((N + SBN - 1) / SBN);
     g.ksplit = ksplit;
     g.kcb = ksplit > 1 ? kcb : Kp / SBK;
-    if (ksplit > 1) {  // every split non-empty, at most 1024 deep, all of K covered
+    if (ksplit > 1) {  // every split non-empty, exact in depth (narrow), all of K covered
         const long long nkb = Kp / SBK;
-        if (kcb < 1 || kcb * SBK > 1024 || (long long)(ksplit - 1) * kcb >= nkb ||
+        if (kcb < 1 || kcb * SBK > KMAX_NARROW || (long long)(ksplit - 1) * kcb >= nkb ||
             (long long)ksplit * kcb < nkb)
             throw Error(RT_ERR_INTERNAL, "inconsistent split-K layout");
     }
     g.row_exp = a_exp;
     g.col_exp = b_exp;
     g.error = S->d_err;
+    const bool nocp = test_no_copies();
+    const unsigned long long wait_ns = nocp ? 50000000ull : WAIT_NS;
+    // CTA pairs (256 rows per pair tile) unless one 128-row tile covers M
+    if (ksplit == 1 && M > SBM && S->max_pairs >= 1) {
+        CUtensorMap ma2 = make_map(S, a_sl, M, Kp, s, PBM / 2);
+        CUtensorMap mb2 = make_map(S, b_sl, N, Kp, s, PBN / 2, b_slice_rows);
+        g.tiles_m = (int)((M + PBM - 1) / PBM);
+        g.tiles_n = (int)((N + PBN - 1) / PBN);
+        const long long strips = std::max<long long>(g.tiles_m, g.tiles_n);
+        const int npairs = (int)std::min<long long>(strips, S->max_pairs);
+        c->ktimer.begin();
+        k_split_gemm_pair<Epi><<<2 * npairs, GEMM_THREADS, pair_smem_bytes(s), c->stream>>>(
+            ma2, mb2, g, epi, wait_ns, nocp ? 1 : 0);
+        c->ktimer.end(2.0 * (g.tiles_m * (double)PBM) * N * Kp * (s * (s + 1) / 2), 2.0 * M * (double)N * K);
+        ++*launches;
+        RT_CUDA(cudaGetLastError());
+        return;
+    }
     const long long ntiles = (long long)g.tiles_m * g.tiles_n * g.ksplit;
     const int grid = (int)std::min<long long>(ntiles, S->num_sms);
     const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
     c->ktimer.begin();
-    k_split_gemm<128, Epi><<<grid, GEMM_THREADS, smem, c->stream>>>(ma, mb, g, epi);
+    k_split_gemm<128, Epi><<<grid, GEMM_THREADS, smem, c->stream>>>(ma, mb, g, epi, wait_ns, nocp ? 1 : 0);
     // executed tensor FLOPs: s(s+1)/2 digit products over the padded K
     c->ktimer.end(2.0 * M * (double)N * Kp * (s * (s + 1) / 2), 2.0 * M * (double)N * K);
     ++*launches;
     RT_CUDA(cudaGetLastError());
+}
+
+std::string split_status_text(int e, bool* unconfirmed) {
+    static const char* what[] = {"", "waiting for a free pipeline stage", "waiting for operand tiles",
+                                 "waiting for the TMEM accumulators"};
+    const int first = e & 0xff;
+    std::string t = "split GEMM gave up " + std::string(first >= 1 && first <= 3 ? what[first] : "waiting") +
+                    " (status " + std::to_string(e) + ")";
+    *unconfirmed = (e & (ERR_DRAIN_UNCONFIRMED | ERR_COPIES_UNCONFIRMED)) != 0;
+    if (*unconfirmed)
+        t += "; its clean-up could not confirm that all tensor-core work and copies had finished";
+    return t;
 }
 
 static void check_error(rt_ctx* c) {
@@ -911,8 +1239,11 @@ static void check_error(rt_ctx* c) {
     RT_CUDA(cudaMemcpyAsync(&e, S->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     RT_CUDA(cudaStreamSynchronize(c->stream));
     if (e) {
+        bool unconfirmed = false;
+        const std::string msg = split_status_text(e, &unconfirmed);
+        if (unconfirmed) c->unusable = true;
         RT_CUDA(cudaMemset(S->d_err, 0, sizeof(int)));
-        throw Error(RT_ERR_PROGRAM, "split GEMM gave up waiting (status " + std::to_string(e) + ")");
+        throw Error(RT_ERR_PROGRAM, msg);
     }
 }
 
@@ -1184,7 +1515,7 @@ void split_group_free(SplitGroup* G) {
 // long rows (operands of the adjoint contraction, K up to ~10^8): exponents
 // by a block-parallel maximum, then the digits elementwise
 // ---------------------------------------------------------------------------
-constexpr int LONG_BLOCK = 1024;  // K per split of the contraction = per exponent
+constexpr int LONG_BLOCK = SPLIT_LONG_BLOCK;  // K per split of the contraction = per exponent
 
 // exps[kb * rows + row] = exponent of row's K block kb (LONG_BLOCK deep)
 __global__ void __launch_bounds__(256) k_rowexp_long(const float2* __restrict__ src, long long ld,
@@ -1195,7 +1526,7 @@ __global__ void __launch_bounds__(256) k_rowexp_long(const float2* __restrict__ 
     const long long k1 = min(K, k0 + LONG_BLOCK);
     int S = -2000;
     for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x)
-        S = max(S, scale_exp_f32(src[(long long)row * ld + k].x));
+        S = max(S, scale_exp_f32(src[(long long)row * ld + k].x, slicing_wide(LONG_BLOCK)));
     for (int o = 16; o; o >>= 1) S = max(S, __shfl_xor_sync(0xffffffffu, S, o));
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = S;
     __syncthreads();
@@ -1205,7 +1536,7 @@ __global__ void __launch_bounds__(256) k_rowexp_long(const float2* __restrict__ 
     }
 }
 
-// digits of row's K block blockIdx.x (256 threads x 4 consecutive k)
+// digits of row's K block blockIdx.x (LONG_BLOCK / 4 threads x 4 consecutive k)
 template <int NS>
 __global__ void __launch_bounds__(256) k_slice_rows_long(const float2* __restrict__ src, long long ld,
                                                          int rows, long long K, long long Kp,
@@ -1236,12 +1567,14 @@ static void slice_long_rows(int s, const float2* src, long long ld, int rows, lo
     if (rows > 65535) throw Error(RT_ERR_DIM, "long-row slicing: more than 65535 rows");
     dim3 g((unsigned)((Kp + LONG_BLOCK - 1) / LONG_BLOCK), (unsigned)rows);
     k_rowexp_long<<<g, 256, 0, st>>>(src, ld, rows, K, exps);
+    constexpr int T = LONG_BLOCK / 4;  // one thread per 4 k of the block
+    static_assert(LONG_BLOCK % 128 == 0 && T <= 256, "long-row block of whole warps");
     switch (s) {
-        case 2: k_slice_rows_long<2><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
-        case 3: k_slice_rows_long<3><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
-        case 4: k_slice_rows_long<4><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
-        case 5: k_slice_rows_long<5><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
-        default: k_slice_rows_long<6><<<g, 256, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        case 2: k_slice_rows_long<2><<<g, T, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        case 3: k_slice_rows_long<3><<<g, T, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        case 4: k_slice_rows_long<4><<<g, T, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        case 5: k_slice_rows_long<5><<<g, T, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
+        default: k_slice_rows_long<6><<<g, T, 0, st>>>(src, ld, rows, K, Kp, exps, out); break;
     }
 }
 
@@ -1262,7 +1595,7 @@ void split_adj_x(rt_ctx* c, int comp, const double* m3, int nc, int nij, double*
 long long split_adj_kpad(long long K) { return (K + SBK - 1) / SBK * SBK; }
 
 // Adjoint contraction part[ks][a][col] = sum over split ks of X(a,k) Ghat(k,col)
-// with Ghat given transposed (rows col, length Kx); every 1024-deep split
+// with Ghat given transposed (rows col, length Kx); every LONG_BLOCK-deep split
 // has its own row and column scales (a_ex: [ks][rows], b_ex: [ks][2m]).
 // Returns the split count.
 int split_adj_contract(rt_ctx* c, const double* x, int rows, long long Kx, const double* ghat_t,
@@ -1276,7 +1609,7 @@ int split_adj_contract(rt_ctx* c, const double* x, int rows, long long Kx, const
     slice_long_rows(S->s, (const float2*)ghat_t, Kx, m2, Kx, Kp, b_ex, b_sl, c->stream);
     *launches += 4;
     RT_CUDA(cudaGetLastError());
-    // one split per exponent block; K <= 1024 per split keeps the FP32 sums exact
+    // one split per exponent block; LONG_BLOCK <= 819 keeps the narrow FP32 sums exact
     const int kcb = LONG_BLOCK / SBK;
     const int nkb = (int)(Kp / SBK);
     const int ksplit = (nkb + kcb - 1) / kcb;
@@ -1297,7 +1630,8 @@ void split_release(rt_ctx* c) {
 extern "C" int rt_split_dgemm(int M, int N, int K, const double* A, const double* B, double* C,
                               int slices, int mode) {
     using namespace rt;
-    if (M < 1 || N < 1 || K < 1 || K > 1024 || !A || !B || !C || slices < 2 ||
+    if (K > 1024) return RT_ERR_DIM;  // the engine's tested depth; exact up to 1365
+    if (M < 1 || N < 1 || K < 1 || !A || !B || !C || slices < 2 ||
         slices > MAX_SLICES || mode < 0 || mode > 2)
         return RT_ERR_USER;
     rt_ctx ctx;
@@ -1396,6 +1730,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 struct NoallocDevice {
     unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
     int num_sms = 0;
+    bool unusable = false;  // an aborted GEMM could not confirm its clean-up
 };
 static NoallocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
 static PFN_cuTensorMapEncodeTiled_v12000 g_noalloc_encode = nullptr;
@@ -1419,6 +1754,37 @@ __global__ void k_ff_round(const double* __restrict__ x, long long n, float2* __
         const float h = __double2float_rn(v);
         out[i] = make_float2(h, __double2float_rn(v - (double)h));
     }
+}
+
+// Is [p, p + bytes) memory the current device `dev` can read and write?
+// Device memory of dev (the whole range inside one allocation), managed
+// memory, or page-locked host memory mapped at the same address; not
+// pageable host memory, and not memory of another device.
+static bool device_range_ok(const void* p, size_t bytes, int dev) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeManaged) return true;
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer == p;
+    if (a.type != cudaMemoryTypeDevice || a.device != dev) return false;
+    static PFN_cuMemGetAddressRange_v3020 range = nullptr;
+    if (!range) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &fn, 3020, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            !fn || q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return true;  // the type check above stands alone
+        }
+        range = (PFN_cuMemGetAddressRange_v3020)fn;
+    }
+    CUdeviceptr base = 0;
+    size_t size = 0;
+    if (range(&base, &size, (CUdeviceptr)(uintptr_t)p) != CUDA_SUCCESS) return false;
+    return (uintptr_t)p + bytes <= (uintptr_t)base + size;
 }
 
 // Per-device set-up, with that device current: the device address of the
@@ -1459,7 +1825,7 @@ extern "C" int rt_split_dgemm_noalloc(int M, int N, int K, const double* A, cons
         return RT_ERR_USER;
     }
     if (K > 1024) {
-        set_thread_error("rt_split_dgemm_noalloc: K > 1024 (the exact FP32 accumulation needs K <= 1024)");
+        set_thread_error("rt_split_dgemm_noalloc: K > 1024 (the depth the engine is tested to)");
         return RT_ERR_DIM;
     }
     const size_t need = noalloc_bytes(M, N, K, slices);
@@ -1474,6 +1840,12 @@ extern "C" int rt_split_dgemm_noalloc(int M, int N, int K, const double* A, cons
         RT_CUDA(cudaGetDevice(&dev));
         if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) throw Error(RT_ERR_DIM, "device ordinal above 63");
         const NoallocDevice& D = noalloc_setup(dev);
+        if (D.unusable)
+            throw Error(RT_ERR_PROGRAM, "an earlier call on this device was aborted without a confirmed clean-up");
+        if (!device_range_ok(A, 8 * (size_t)M * K, dev) || !device_range_ok(B, 8 * (size_t)K * N, dev) ||
+            !device_range_ok(C, 8 * (size_t)M * N, dev))
+            throw Error(RT_ERR_USER, "A, B and C must be device memory of the current device (or managed, "
+                                     "or mapped page-locked host memory) covering M*K, K*N and M*N doubles");
         cudaStream_t st = (cudaStream_t)stream;
         const int s = slices, Kp = kpad(K);
         unsigned char* w = D.scratch;
@@ -1514,12 +1886,18 @@ extern "C" int rt_split_dgemm_noalloc(int M, int N, int K, const double* A, cons
         g.error = err;
         const int grid = std::min(g.tiles_m * g.tiles_n, D.num_sms);
         const size_t smem = (size_t)NSTAGE * s * (SBM + SBN) * SBK * 2 + 1024;
-        k_split_gemm<128, EpiF64_RowMajor><<<grid, GEMM_THREADS, smem, st>>>(ma, mb, g, EpiF64_RowMajor{C, N});
+        k_split_gemm<128, EpiF64_RowMajor><<<grid, GEMM_THREADS, smem, st>>>(ma, mb, g, EpiF64_RowMajor{C, N},
+                                                                           WAIT_NS, 0);
         RT_CUDA(cudaGetLastError());
         int e = 0;
         RT_CUDA(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, st));
         RT_CUDA(cudaStreamSynchronize(st));
-        if (e) throw Error(RT_ERR_PROGRAM, "split GEMM gave up waiting (status " + std::to_string(e) + ")");
+        if (e) {
+            bool unconfirmed = false;
+            const std::string msg = split_status_text(e, &unconfirmed);
+            if (unconfirmed) g_noalloc_dev[dev].unusable = true;
+            throw Error(RT_ERR_PROGRAM, msg);
+        }
     } catch (const Error& e) {
         set_thread_error("rt_split_dgemm_noalloc: " + e.msg);
         return e.code;

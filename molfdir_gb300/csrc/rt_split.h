@@ -7,7 +7,12 @@
 
 namespace rt {
 
+// K per split of the adjoint's long contraction (one exponent per block)
+constexpr int SPLIT_LONG_BLOCK = 768;
 void split_prepare_constants(rt_ctx* c);
+// Message for a GEMM status word; *unconfirmed is set when the aborted
+// launch could not confirm that its MMAs and copies had finished.
+std::string split_status_text(int e, bool* unconfirmed);
 double split_stageA_bytes_per_pair(rt_ctx* c);
 double split_stageB_bytes_per_item(rt_ctx* c);
 void split_alloc_work(rt_ctx* c, int pair_chunk, int item_chunk);

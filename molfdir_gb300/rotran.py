@@ -20,6 +20,7 @@ from . import build as _build
 RT_PREC_FP64 = 0
 RT_PREC_SPLIT_BF16 = 1
 RT_ERR_EOF, RT_ERR_USER, RT_ERR_DIM = 1, 2, 3
+RT_ERR_PROGRAM = 6
 
 ERROR_CLASSES = {
     1: "end of file / missing data",

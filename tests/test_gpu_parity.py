@@ -69,12 +69,17 @@ def test_fp64_thresholds(thrgen, throut):
     p = synth.make_problem(6, 8, 4, seed=14)
     _, ref = ref_stream(p, thrgen=thrgen, throut=throut)
     got, _ = run_gpu(p, thrgen=thrgen, throut=throut)
-    # THRGEN screens different intermediates in the two codes (the GPU
-    # screens the complete half-transformed integrals), so only the
-    # default-threshold runs are compared element for element
+    # TROUT's test |H| < THRGEN / (VMX(p) VMX(q)) (trout.F:30-43) is applied
+    # to different intermediates: rotran's TRANS1 transforms bucket pq, which
+    # holds only the integrals (rs|pq) sorted under pq (rs >= pq), and adds
+    # the pair-interchanged part later (OUTPP2/PPSYM); the GPU's bucket holds
+    # every (pq|rs), so its half-transformed value is the complete sum over
+    # rs.  With the default THRGEN = 1e-16 (readin.F:93) both screens drop
+    # only values below rounding and the streams agree to 1e-12; a coarse
+    # THRGEN drops different values, hence the looser tolerance here.
     tol = TOL_FP64 if thrgen <= 1e-16 else 1e-4
     # with a large THROUT the reference drops canonical or pp-interchanged
-    # halves below THROUT before summing them (outpp1.F:76, outpp2.F:156)
+    # halves below THROUT before summing them (outpp1.F:34, outpp2.F:40)
     tol = max(tol, throut)
     assert compare_streams(got, ref, tol, presence_tol=max(tol, 2 * throut)) <= tol
 
@@ -146,7 +151,7 @@ def test_no_integrals():
 
 
 def test_files_above_mfil_are_not_read():
-    """SORT1 reads files 1..MFIL only (sort1.F:118): (SS|SS) records added to
+    """SORT1 reads files 1..MFIL only (sort1.F:60): (SS|SS) records added to
     an MFIL = 2 transform change nothing."""
     p2 = synth.make_problem(5, 6, 3, seed=22, mfil=2)
     p3 = synth.make_problem(5, 6, 3, seed=22, mfil=3)
