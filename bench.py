@@ -282,16 +282,13 @@ def run_files_case(args, rank):
     print(json.dumps(out))
 
 
-def run_batched(args, rank, world, local, bf16_peak, peak_kind):
+def batched_leg(args, world, local, steps, warmup, with_fp64=True, oracle=True):
     """48 independent transforms of uneven size (n_AO ~ U[40,200], 60% small
     component, 16..80 Kramers pairs, seeds 0..47): split precision as one
     batch (grouped GEMM launches in a captured CUDA graph, tile widths tuned),
-    against the same 48 transforms run one after another in FP64."""
+    against the same 48 transforms run one after another in FP64, and the
+    batch's streams against the oracle's digest of the 48 instances."""
     import torch
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
     from molfdir_gb300 import rotran, synth
     sizes = synth.batched_instances()
     probs, recs = [], []
@@ -313,31 +310,42 @@ def run_batched(args, rank, world, local, bf16_peak, peak_kind):
     t0 = time.perf_counter()
     batch.run()  # tuning + capture + first replay
     t_first = time.perf_counter() - t0
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.run()
     dev_ms = []
     sampler = ClockSampler(local)
     sampler.__enter__()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         batch.run()
         dev_ms.append(batch.stats().ms_last)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     sampler.__exit__(None, None, None)
     bst = batch.stats()
-    sec = barrier_max(max((t1 - t0) / args.steps, statistics.mean(dev_ms) / 1e3), world)
+    sec = barrier_max(max((t1 - t0) / steps, statistics.mean(dev_ms) / 1e3), world)
     flops = bst.flops_algorithmic
-    value = flops * world / sec / 1e12
     results = [rt.result() for rt in rts]
     batch.close()
     for rt in rts:
         rt.close()
-
-    # the same 48 transforms one after another in FP64 (and the accuracy reference)
+    ocheck = None
+    if oracle:
+        sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+        import digest_check
+        dg = digest_check.load(digest_check.BATCHED)
+        if dg is not None:
+            bad, worst = [], 0.0
+            for i, (h, ix, v) in enumerate(results):
+                res = digest_check.check_batched_instance(digest_check.batched_instance(dg, i), h, ix, v, 1e-10)
+                worst = max(worst, res.get("sample_max_abs_err", 0.0))
+                if not res["ok"]:
+                    bad.append(i)
+            ocheck = {"instances": len(results), "failed": bad, "tol": 1e-10,
+                      "sample_max_abs_err": worst, "ok": not bad}
     fp64 = None
-    if not args.no_fp64:
+    if with_fp64:
         t_fp = 0.0
         mx = ss = 0.0
         nel = 0
@@ -362,25 +370,41 @@ def run_batched(args, rank, world, local, bf16_peak, peak_kind):
                 "mode": "48 sequential FP64 transforms", "split_speedup": t_fp / sec,
                 "split_vs_fp64": {"max_abs_err": mx, "rms_err": float(np.sqrt(ss / max(1, nel))),
                                   "same_elements": same, "elements": nel}}
+    del recs
+    torch.cuda.empty_cache()
+    return {"value": flops * world / sec / 1e12, "unit": "TFLOP/s", "sec": sec, "flops": flops,
+            "sizes": sizes, "bst": bst, "fp64": fp64, "oracle_check": ocheck, "clocks": sampler.summary(),
+            "first_run_s": t_first}
+
+
+def run_batched(args, rank, world, local, bf16_peak, peak_kind):
+    """The batched workload on its own line (``--workload batched``)."""
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    b = batched_leg(args, world, local, args.steps, args.warmup, with_fp64=not args.no_fp64)
+    bst, sec, sizes = b["bst"], b["sec"], b["sizes"]
     if rank == 0:
         achieved = bst.flops_gemm_executed / sec / 1e12
         line = {
-            "metric": "4-index transform TFLOP/s", "value": value, "unit": "TFLOP/s",
+            "metric": "4-index transform TFLOP/s", "value": b["value"], "unit": "TFLOP/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16-slices/f32-acc (split)", "data": "synthetic",
             "config": {"workload": "batched_48", "instances": len(sizes),
                        "sizes": [[nl + ns, nkr] for nl, ns, nkr, _ in sizes],
-                       "slices": args.slices, "flops_algorithmic": flops,
+                       "slices": args.slices, "flops_algorithmic": b["flops"],
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak,
                          "unit": "TFLOP/s", "frac": achieved / bf16_peak, "traffic": None,
                          "kernel": "whole batch: grouped tcgen05 GEMM tensor FLOPs per batch time",
                          "peak_source": f"bf16_tflops of {peak_kind}"},
-            "cpu_baseline": None, "e2e": None, "fp64": fp64,
+            "cpu_baseline": None, "e2e": None, "fp64": b["fp64"], "oracle_check": b["oracle_check"],
             "gpu_launches": bst.kernel_launches * args.steps,
-            "clocks": sampler.summary(), "batch": bst.as_dict(),
-            "first_run_s": t_first,
+            "clocks": b["clocks"], "batch": bst.as_dict(),
+            "first_run_s": b["first_run_s"],
         }
         print(json.dumps(line))
     if world > 1:
@@ -400,6 +424,8 @@ def main():
                     choices=["precision", "c1", "profile", "large", "batched", "gemm", "files"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="leave out the 48-instance batched leg of the default line")
     ap.add_argument("--per-class", action="store_true",
                     help="also split vs FP64 per AO integral class (3 + 3 extra transforms)")
     args = ap.parse_args()
@@ -608,6 +634,18 @@ def main():
         cpu = {"value": res["tflops"], "unit": "TFLOP/s", "cores": cores, "kind": "port",
                "sample": res["sample"]}
 
+    # ---- the batched workload (48 instances, one CUDA graph) beside it ----
+    batched = None
+    if work["name"] == WORKLOAD["name"] and not args.no_batched and prec_name == "split":
+        b = batched_leg(args, world, local, steps=3, warmup=2, with_fp64=not args.no_fp64,
+                        oracle=rank == 0)
+        batched = {"workload": "batched_48 (48 instances, n_AO 40..200, 16..80 Kramers pairs, seeds 0..47)",
+                   "value": b["value"], "unit": "TFLOP/s", "ms_per_step": b["sec"] * 1e3, "steps": 3,
+                   "warmup": 2, "flops_algorithmic": b["flops"], "fp64": b["fp64"],
+                   "oracle_check": b["oracle_check"], "clocks": b["clocks"],
+                   "graph": {k: v for k, v in b["bst"].as_dict().items()
+                             if k in ("grouped_launches", "kernel_launches", "graph_nodes", "tile128", "tile64")}}
+
     # ---- the streams against the oracle's digest of this workload ----
     ocheck = None
     if rank == 0 and work["name"] == WORKLOAD["name"]:
@@ -651,6 +689,7 @@ def main():
             "precision": {"path": prec_name, "slices": args.slices if prec_name == "split" else None},
             "tflops_dense_equivalent": config["flops_dense_equivalent"] * world / main["sec"] / 1e12,
             "oracle_check": ocheck,
+            "batched": batched,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64,
             "gpu_launches": st.gpu_launches * args.steps, "clocks": main["clocks"],
             "stats": st.as_dict(), "mdcint": {"records": nrec, "elements": nz},

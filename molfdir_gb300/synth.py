@@ -193,11 +193,32 @@ def make_ao_model(n_l: int, n_s: int, rng: np.random.Generator,
                    pl, ql, ps, qs, bl, bs)
 
 
+def breit_pairs(model: AOModel):
+    """The SL pairs (p small, q large component; 1-based, p > q) of the Gaunt
+    integrals and their B rows: (pq|rs) = sum_Q B[pq,Q] B[rs,Q] with the
+    same Gaussian-envelope model as the Coulomb classes, each SL pair scaled
+    by 1/(2c).  The rows come from their own seeded generator (the AO
+    model's centres fix it), so adding the Gaunt file leaves the Coulomb
+    integrals and spinors of a problem unchanged."""
+    if getattr(model, "_breit", None) is None:
+        n_l, n = model.n_l, model.n
+        p = np.repeat(np.arange(n_l + 1, n + 1, dtype=np.int32), n_l)
+        q = np.tile(np.arange(1, n_l + 1, dtype=np.int32), model.n_s)
+        seed = int(np.abs(model.centres).sum() * 1e6) % (2 ** 31)
+        rng = np.random.default_rng(seed)
+        nq = 3 * n
+        d2 = np.sum((model.centres[p - 1] - model.centres[q - 1]) ** 2, axis=1)
+        env = np.exp(-d2 / (2.0 * 2.0 * 2.0))
+        b = env[:, None] * rng.standard_normal((p.size, nq)) / math.sqrt(nq) / (2.0 * C_LIGHT)
+        model._breit = (p, q, b)
+    return model._breit
+
+
 def _file_integrals(model: AOModel, which: str, chunk: int = 2048):
     """Unique canonical integrals of one SRT file as flat arrays.
 
-    ``which`` is ``"LL"`` ((LL|LL)), ``"SL"`` ((SS|LL), first pair SS) or
-    ``"SS"``.  Returns ``(value, label2, label1, it)``: ``label2`` packs
+    ``which`` is ``"LL"`` ((LL|LL)), ``"SL"`` ((SS|LL), first pair SS),
+    ``"SS"``, or ``"BR"`` (the Gaunt (SL|SL) integrals of the Breit file).  Returns ``(value, label2, label1, it)``: ``label2`` packs
     the first (larger) pair ``I<<16|K``, ``label1`` the second ``L<<16|N``.
     """
     if which == "LL":
@@ -206,6 +227,9 @@ def _file_integrals(model: AOModel, which: str, chunk: int = 2048):
         pa, qa_, ba, pc, qc, bc, tri = model.ps, model.qs, model.bs, model.pl, model.ql, model.bl, False
     elif which == "SS":
         pa, qa_, ba, pc, qc, bc, tri = model.ps, model.qs, model.bs, model.ps, model.qs, model.bs, True
+    elif which == "BR":
+        pb, qb_, bb = breit_pairs(model)
+        pa, qa_, ba, pc, qc, bc, tri = pb, qb_, bb, pb, qb_, bb, True
     else:
         raise ValueError(which)
     irr = model.irrep
@@ -297,8 +321,9 @@ class Problem:
         return 2 * self.nkr
 
     def all_records(self):
-        """(file_class, record) in the order SORT1 reads them (sort1.F:60)."""
-        order = [("LL", 1), ("SL", 2), ("SS", 3)][: self.mfil]
+        """(file_class, record) in the order SORT1 reads them (sort1.F:60);
+        the Gaunt file (class 4, SRTBREI) follows when the problem has one."""
+        order = [("LL", 1), ("SL", 2), ("SS", 3)][: self.mfil] + [("BR", 4)]
         for key, cls in order:
             for r in self.files.get(key, []):
                 yield cls, r
@@ -327,8 +352,9 @@ class Problem:
 
 
 def make_problem(n_l: int, n_s: int, nkr: int, seed: int = 0,
-                 n_irrep: int = 1, mfil: int = 3) -> Problem:
-    """Build one seeded transform instance (AO records + spinors)."""
+                 n_irrep: int = 1, mfil: int = 3, breit: bool = False) -> Problem:
+    """Build one seeded transform instance (AO records + spinors); with
+    ``breit`` also the Gaunt (SL|SL) file (class 4)."""
     rng = np.random.default_rng(seed)
     model = make_ao_model(n_l, n_s, rng, n_irrep=n_irrep)
     qa, qb, itrmo, kra, krb, ikrmo = make_spinors(model.n, nkr, rng)
@@ -337,6 +363,8 @@ def make_problem(n_l: int, n_s: int, nkr: int, seed: int = 0,
         files["SL"] = file_records(model, "SL")
     if mfil >= 3 and n_s > 0:
         files["SS"] = file_records(model, "SS")
+    if breit and n_s > 0 and n_l > 0:
+        files["BR"] = file_records(model, "BR")
     return Problem(model, nkr, qa, qb, itrmo, kra, krb, ikrmo, mfil, files)
 
 

@@ -32,7 +32,7 @@ class _Params(C.Structure):
                 ("mfil", C.c_int), ("quater", C.c_int), ("thrgen", C.c_double),
                 ("throut", C.c_double), ("nthreads", C.c_int), ("limit_pq", C.c_long),
                 ("limit_ij", C.c_long), ("pq_select", C.POINTER(C.c_long)),
-                ("n_pq_select", C.c_long), ("fake_list_len", C.c_long)]
+                ("n_pq_select", C.c_long), ("fake_list_len", C.c_long), ("breit", C.c_int)]
 
 
 class _Result(C.Structure):
@@ -78,7 +78,8 @@ def _ptr(a, t):
 
 
 def run(problem, thrgen=1e-16, throut=1e-16, nthreads=0, limit_pq=0, limit_ij=0,
-        quater=True, records=None, pq_select=None, fake_list_len=0) -> MdcintImage:
+        quater=True, records=None, pq_select=None, fake_list_len=0, breit=False) -> MdcintImage:
+    """The oracle's MDCINT (or, with breit, MDBINT) stream of a problem."""
     lib = _load()
     cls, its, nts, v, l2, l1 = problem.flat_records() if records is None else records
     qa = np.asfortranarray(problem.qa).astype(np.complex128)
@@ -87,7 +88,7 @@ def run(problem, thrgen=1e-16, throut=1e-16, nthreads=0, limit_pq=0, limit_ij=0,
     prm = _Params(problem.n, problem.nsc1, problem.m, problem.nkr, problem.mfil,
                   1 if quater else 0, thrgen, throut, nthreads, limit_pq, limit_ij,
                   None if sel is None else _ptr(sel, C.c_long),
-                  0 if sel is None else sel.size, fake_list_len)
+                  0 if sel is None else sel.size, fake_list_len, 1 if breit else 0)
     res = _Result()
     itrmo = np.ascontiguousarray(problem.itrmo, np.int32)
     kra = np.ascontiguousarray(problem.kra, np.int32)

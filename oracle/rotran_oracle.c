@@ -10,9 +10,11 @@
  * cross-checked instead against an independent dense formulation of the
  * same integrals (tests/test_oracle.py).
  *
- * Scope: Coulomb integrals (BREIT = .FALSE.), spinors without point-group
- * symmetry (one fermion irrep, quaternionic: classes 1-4 are written), the
- * 32-bit LINUX label layout.  Each routine cites the reference lines it
+ * Scope: Coulomb integrals (BREIT = .FALSE.) and the Gaunt (Breit) branch
+ * (BREIT = .TRUE. with MFIL = 0: file 4, SL pq blocks, three half-transformed
+ * streams, MDBINT), spinors without point-group symmetry (one fermion
+ * irrep, quaternionic: classes 1-4 are written), the 32-bit LINUX label
+ * layout.  Each routine cites the reference lines it
  * follows (paths relative to the MOLFDIR source tree).  Arithmetic order is
  * kept where the reference fixes it (netlib ZGEMM summation order, the
  * newest-first read order of the bucket chains) so that the restatement is
@@ -95,7 +97,7 @@ int orc_inttyp(int imm, int jmm, int kmm, int lmm) {
 }
 
 /* Record index of the Kramers-unique pair (source/rotran/unique.F:1-50). */
-static void unique_(int nkr, const int* ikrmo, int i, int j, int* ij, int* conjug, int* is) {
+static void unique_(int nkr, const int* ikrmo, int breit, int i, int j, int* ij, int* conjug, int* is) {
     int ikr = ikrmo[i - 1], jkr = ikrmo[j - 1];
     int iikr, jjkr;
     if (abs(ikr) >= abs(jkr)) {
@@ -106,6 +108,7 @@ static void unique_(int nkr, const int* ikrmo, int i, int j, int* ij, int* conju
     *is = 1;
     if (iikr > 0) {
         *is = (iikr * jjkr >= 0) ? 1 : -1; /* ISIGN(1, IIKR*JJKR) */
+        if (breit) *is = -*is;             /* unique.F:34 */
         iikr = -iikr; jjkr = -jjkr; *conjug = !*conjug;
     }
     int ijbaroff = nkr * (nkr + 1) / 2;
@@ -117,7 +120,7 @@ static void unique_(int nkr, const int* ikrmo, int i, int j, int* ij, int* conju
 
 /* The buffer sizes rotran derives from its fixed work array (rotran.F:77-225);
  * they fix the order in which bucket chains are read back. */
-static void ref_buffer_sizes(int nsc, int nkr, int nsp, int npqbuf_used, int* nijsiz,
+static void ref_buffer_sizes(int nsc, int nkr, int nsp, int npqbuf_used, int breit, int* nijsiz,
                              int* nsksiz, int* nc2) {
     const long NWORK = 16000000L, NITR = 2, NRTC = 2, MAXPASS = 10;
     long nsctr = (long)nsc * (nsc + 1) / 2, nsptr = (long)nkr * (nkr + 1), nspsq = (long)nsp * nsp;
@@ -136,9 +139,11 @@ static void ref_buffer_sizes(int nsc, int nkr, int nsp, int npqbuf_used, int* ni
     long label1 = top + ((npqbuf + 1) + 1) / NITR;
     for (;;) {
         long nbck = label1;
-        long lbck = nbck + (nijbuf + 1) / NITR;
+        /* the Gaunt buckets hold two counters and six reals per entry
+         * (rotran.F:128-137) */
+        long lbck = nbck + (breit ? 2 * (nijbuf + 1) / NITR : (nijbuf + 1) / NITR);
         long cbck = lbck + (nijbuf * nij + 1) / NITR;
-        long indg = cbck + nijbuf * nij * NRTC;
+        long indg = cbck + (breit ? 6 * nijbuf * nij : nijbuf * nij * NRTC);
         long g = indg + ng * 2;
         long ha = g + ng;
         long ri = ha + (long)nsc * nsp * NRTC;
@@ -184,6 +189,31 @@ static void chunk_reverse_order(long n, int chunk, long* perm) {
         long s = c * chunk, e = s + chunk < n ? s + chunk : n;
         for (long x = s; x < e; x++) perm[k++] = x;
     }
+}
+
+/* Read order of one Gaunt INTTWO bucket: TRBOUT (trbout.F:49-141) writes a
+ * record when 4(NBL+1) + 8(NBI+6) + 12 exceeds IRECL = 12 + 12 NIJSIZ, NBL
+ * entries and NBI stored reals so far (nparts[x] reals of entry x); GETHTBI
+ * reads the records newest first (gethtbi.F:31-44). */
+static void breit_chunk_order(long n, const int* nparts, long nijsiz, long* perm) {
+    const long irecl = 12 + 12 * nijsiz;
+    long* ends = (long*)malloc(sizeof(long) * (n + 1));
+    long nch = 0, nbl = 0, nbi = 0;
+    for (long x = 0; x < n; x++) {
+        nbl++;
+        nbi += nparts[x];
+        if (4 * (nbl + 1) + 8 * (nbi + 6) + 12 > irecl) {
+            ends[nch++] = x + 1;
+            nbl = nbi = 0;
+        }
+    }
+    if (nbl > 0) ends[nch++] = n; /* flushed by SR2FLSB */
+    long k = 0;
+    for (long c = nch - 1; c >= 0; c--) {
+        long s0 = c > 0 ? ends[c - 1] : 0;
+        for (long x = s0; x < ends[c]; x++) perm[k++] = x;
+    }
+    free(ends);
 }
 
 typedef struct {
@@ -437,12 +467,19 @@ static long ppsym(const skfile* f, const pplist* bk, int nsksiz, int nc2, int nk
     return nfinal;
 }
 
-/* MAKIND's Coulomb selection of pq blocks (makind.F:70-90) for C1. */
-static int pq_included(int p, int q, int nsc1, int mfil) {
+/* MAKIND's selection of pq blocks for C1: Coulomb (makind.F:70-90) or, for
+ * the Gaunt integrals, the SL blocks, p small and q large component
+ * (makind.F:91-95). */
+static int pq_included(int p, int q, int nsc1, int mfil, int breit) {
+    if (breit) return p > nsc1 && q <= nsc1;
     if (p > nsc1 && q <= nsc1) return 0;
     if (p > nsc1 && mfil < 3) return 0;
     return 1;
 }
+
+/* SORT1 reads files 1..MFIL, or file 4 alone for the Gaunt integrals
+ * (sort1.F:55-57); GETTW turns the sign of file 4 (gettw.F:51-55). */
+static int file_read(int f, int mfil, int breit) { return breit ? f == 4 : (f >= 1 && f <= mfil); }
 
 int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const int* kra,
             const int* krb, const int* ikrmo, long nrec, const int* rec_file, const int* rec_it,
@@ -451,8 +488,22 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     memset(out, 0, sizeof(*out));
     const int n = prm->nsc, nsc1 = prm->nsc1, m = prm->nsp, nkr = prm->nkr;
     if (n <= 0 || m != 2 * nkr || nsc1 < 0 || nsc1 > n || n > 65535) return 2;
+    const int breit = prm->breit != 0;
+    if (breit && n > 8191) return 2; /* 13-bit labels of the Gaunt buckets (trbout.F:28-34) */
     const cplx* qa = (const cplx*)qa_in; /* QA(p,i) = qa[p + i*n], 0-based */
 #define QA(p, i) qa[(p) + (long)(i) * n]
+    /* QB of the Kramers-paired spinors (kramers.F:134-150): QA(jbar) =
+     * -conj(QB(j)), QB(jbar) = conj(QA(j)) */
+    cplx* qbv = (cplx*)malloc(sizeof(cplx) * (size_t)n * m);
+    for (int i = 0; i < m; i++) {
+        const int t = itrmo[i];
+        const int pi = abs(t) - 1;
+        for (int p = 0; p < n; p++) {
+            cplx a = cconj(QA(p, pi));
+            qbv[p + (long)i * n] = t > 0 ? cscal(-1.0, a) : a;
+        }
+    }
+#define QB(p, i) qbv[(p) + (long)(i) * n]
 #ifdef _OPENMP
     if (prm->nthreads > 0) omp_set_num_threads(prm->nthreads);
 #endif
@@ -475,14 +526,14 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     long* cnt = (long*)calloc(nsctr + 1, sizeof(long));
     long nincl = 0;
     for (int p = 1; p <= n; p++)
-        for (int q = 1; q <= p; q++) nincl += pq_included(p, q, nsc1, prm->mfil);
+        for (int q = 1; q <= p; q++) nincl += pq_included(p, q, nsc1, prm->mfil, breit);
     long off = 0;
     for (long r = 0; r < nrec; r++) {
-        if (rec_file[r] < 1 || rec_file[r] > prm->mfil) { off += rec_nt[r]; continue; }
+        if (!file_read(rec_file[r], prm->mfil, breit)) { off += rec_nt[r]; continue; }
         for (long x = off; x < off + rec_nt[r]; x++) {
             int ip = (label1[x] >> 16) & 0xFFFF, iq = label1[x] & 0xFFFF;
-            if (ip < 1 || iq < 1 || ip > n || iq > ip) { free(cnt); free(vmx); return 3; }
-            if (!pq_included(ip, iq, nsc1, prm->mfil)) continue;
+            if (ip < 1 || iq < 1 || ip > n || iq > ip) { free(cnt); free(vmx); free(qbv); return 3; }
+            if (!pq_included(ip, iq, nsc1, prm->mfil, breit)) continue;
             cnt[(long)ip * (ip - 1) / 2 + iq]++;
         }
         off += rec_nt[r];
@@ -496,13 +547,13 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     memset(cnt, 0, sizeof(long) * (nsctr + 1));
     off = 0;
     for (long r = 0; r < nrec; r++) {
-        if (rec_file[r] < 1 || rec_file[r] > prm->mfil) { off += rec_nt[r]; continue; }
-        double fac = orc_gettw_factor(rec_it[r]);
+        if (!file_read(rec_file[r], prm->mfil, breit)) { off += rec_nt[r]; continue; }
+        double fac = orc_gettw_factor(rec_it[r]) * (breit ? -1.0 : 1.0);
         for (long x = off; x < off + rec_nt[r]; x++) {
             int ip = (label1[x] >> 16) & 0xFFFF, iq = label1[x] & 0xFFFF;
-            if (!pq_included(ip, iq, nsc1, prm->mfil)) continue;
+            if (!pq_included(ip, iq, nsc1, prm->mfil, breit)) continue;
             int ir = (label2[x] >> 16) & 0xFFFF, is = label2[x] & 0xFFFF;
-            if (ir < 1 || is < 1 || ir > n || is > n) { free(cnt); return 3; }
+            if (ir < 1 || is < 1 || ir > n || is > n) { free(cnt); free(vmx); free(qbv); return 3; }
             long pq = (long)ip * (ip - 1) / 2 + iq;
             long slot = bstart[pq] + cnt[pq]++;
             gval[slot] = rint[x] * fac;
@@ -514,7 +565,8 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     free(cnt);
 
     int nijsiz, nsksiz[4], nc2;
-    ref_buffer_sizes(n, nkr, m, (int)(nincl < 16384 ? nincl : 16384), &nijsiz, nsksiz, &nc2);
+    ref_buffer_sizes(n, nkr, m, (int)(nincl < 16384 ? nincl : 16384), breit, &nijsiz, nsksiz, &nc2);
+    const int nstr = breit ? 3 : 1; /* half-transformed streams per entry */
 
     /* ---------------- TRANS1 (trans1.F:48-103) ---------------- */
     /* The half-transformed integrals are held per transformed pq block
@@ -553,13 +605,14 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                 slot_of[pq] = nslot;
                 slot_pq[nslot++] = pq;
             }
-        hstore = (cplx*)calloc((size_t)(nslot ? nslot : 1) * nji, sizeof(cplx));
+        hstore = (cplx*)calloc((size_t)(nslot ? nslot : 1) * nji * nstr, sizeof(cplx));
         hkeep = (unsigned char*)calloc((size_t)(nslot ? nslot : 1) * nji, 1);
 #pragma omp parallel
         {
             cplx* ha = (cplx*)malloc(sizeof(cplx) * (size_t)n * m);
             cplx* ri = (cplx*)malloc(sizeof(cplx) * (size_t)m * m);
             cplx* ria = (cplx*)malloc(sizeof(cplx) * (size_t)m * m);
+            cplx* rib = (cplx*)malloc(sizeof(cplx) * (size_t)m * m);
             long* perm = (long*)malloc(sizeof(long) * 16);
             long permcap = 16;
 #pragma omp for schedule(dynamic, 1)
@@ -592,11 +645,12 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                         for (int l = 0; l < n; l++) tmp = cadd(tmp, cmul(cconj(QA(l, i)), ha[l + (long)j * n]));
                         ri[i + (long)j * m] = tmp;
                     }
-                /* MTIMHER(RIA,RI,+1) (mtimher.F:3-26) */
+                /* MTIMHER(RIA,RI,ISG) (mtimher.F:3-26), ISG = +1 Coulomb, -1 Gaunt */
                 for (int i = 1; i <= m; i++)
                     for (int j = 1; j <= m; j++) {
                         int itr = abs(itrmo[i - 1]), jtr = abs(itrmo[j - 1]);
                         int sg = (itrmo[i - 1] * itrmo[j - 1] >= 0) ? 1 : -1;
+                        if (breit) sg = -sg;
                         cplx a = ri[(j - 1) + (long)(i - 1) * m];
                         cplx b = ri[(itr - 1) + (long)(jtr - 1) * m];
                         cplx c = cconj(ri[(i - 1) + (long)(j - 1) * m]);
@@ -604,6 +658,49 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                         cplx h = cadd(cadd(cadd(a, cscal(sg, b)), c), cscal(sg, d));
                         ria[(j - 1) + (long)(i - 1) * m] = h;
                     }
+                if (breit) {
+                    /* ZGEMM('C','N') with QB: RI = QB^H * HA (trans1.F:91-96) */
+                    for (int j = 0; j < m; j++)
+                        for (int i = 0; i < m; i++) {
+                            cplx tmp = {0.0, 0.0};
+                            for (int l = 0; l < n; l++) tmp = cadd(tmp, cmul(cconj(QB(l, i)), ha[l + (long)j * n]));
+                            ri[i + (long)j * m] = tmp;
+                        }
+                    /* MTIMHR2(RIB,RI) (mtimhr2.F:2-20) */
+                    for (int i = 1; i <= m; i++)
+                        for (int j = 1; j <= m; j++) {
+                            int itr = abs(itrmo[i - 1]), jtr = abs(itrmo[j - 1]);
+                            int sg = (itrmo[i - 1] * itrmo[j - 1] >= 0) ? -1 : 1;
+                            rib[(j - 1) + (long)(i - 1) * m] =
+                                cadd(ri[(j - 1) + (long)(i - 1) * m], cscal(sg, ri[(itr - 1) + (long)(jtr - 1) * m]));
+                        }
+                    /* TRBOUT (trbout.F:1-148): three values per JI, fixed 1e-16
+                     * screen on their summed moduli, parts at or below 1e-16
+                     * not stored; the third stream holds conj(HB(I,J)) */
+                    const double TB = 1.0e-16;
+                    int ji = 0;
+                    for (int ibar = 1; ibar <= 2; ibar++)
+                        for (int ik = 1; ik <= nkr; ik++) {
+                            int i = (ibar == 1) ? kra[ik - 1] : krb[ik - 1];
+                            for (int jk = ik; jk <= nkr; jk++) {
+                                int j = krb[jk - 1];
+                                ji++;
+                                cplx a = ria[(j - 1) + (long)(i - 1) * m];
+                                cplx b = rib[(j - 1) + (long)(i - 1) * m];
+                                cplx c = rib[(i - 1) + (long)(j - 1) * m];
+                                if (cabs_(a) + cabs_(b) + cabs_(c) < TB) continue;
+                                cplx* h = &hstore[(slot_of[pq] * nji + (ji - 1)) * 3];
+                                h[0].re = fabs(a.re) > TB ? a.re : 0.0;
+                                h[0].im = fabs(a.im) > TB ? a.im : 0.0;
+                                h[1].re = fabs(b.re) > TB ? b.re : 0.0;
+                                h[1].im = fabs(b.im) > TB ? b.im : 0.0;
+                                h[2].re = fabs(c.re) > TB ? c.re : 0.0;
+                                h[2].im = fabs(c.im) > TB ? -c.im : 0.0;
+                                hkeep[slot_of[pq] * nji + (ji - 1)] = 1;
+                            }
+                        }
+                    continue;
+                }
                 /* TROUT (trout.F:1-63) */
                 double thrsh = vmx[ip - 1] * vmx[iq - 1];
                 if (thrsh < prm->thrgen) continue;
@@ -622,7 +719,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                         }
                     }
             }
-            free(ha); free(ri); free(ria); free(perm);
+            free(ha); free(ri); free(ria); free(rib); free(perm);
         }
         free(pqlist);
     }
@@ -705,8 +802,9 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
         long b1 = b0 + BATCH < ij_limit ? b0 + BATCH : ij_limit;
 #pragma omp parallel
         {
-            cplx* rj = (cplx*)malloc(sizeof(cplx) * maxmrj);
-            cplx* lv = (cplx*)malloc(sizeof(cplx) * maxmrj); /* the JI list in bucket order */
+            cplx* rj = (cplx*)malloc(sizeof(cplx) * maxmrj * nstr);
+            cplx* lv = (cplx*)malloc(sizeof(cplx) * maxmrj * nstr); /* the JI list in bucket order */
+            int* npart = (int*)malloc(sizeof(int) * maxmrj);
             int* lp = (int*)malloc(sizeof(int) * maxmrj);
             int* lq = (int*)malloc(sizeof(int) * maxmrj);
             cplx* rk = (cplx*)malloc(sizeof(cplx) * (size_t)n * m);
@@ -718,7 +816,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                 int I = items[t].i, J = items[t].j;
                 cplx* rl = &rlb[(t - b0) * (long)m * m];
                 int ji, conjug, is;
-                unique_(nkr, ikrmo, I, J, &ji, &conjug, &is);
+                unique_(nkr, ikrmo, breit, I, J, &ji, &conjug, &is);
                 long s0 = jcnt[ji], mrj = jcnt[ji + 1] - jcnt[ji];
                 if (mrj == 0) { /* GETHTI found nothing: REDME stays zero */
                     memset(rl, 0, sizeof(cplx) * (size_t)m * m);
@@ -730,7 +828,12 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                     for (long sl = 0; sl < nslot; sl++) {
                         size_t h = (size_t)sl * nji + (ji - 1);
                         if (!hkeep[h]) continue;
-                        lv[x] = hstore[h];
+                        for (int c = 0; c < nstr; c++) lv[x * nstr + c] = hstore[h * nstr + c];
+                        if (breit) {
+                            int k = 0;
+                            for (int c = 0; c < 3; c++) k += (lv[x * 3 + c].re != 0.0) + (lv[x * 3 + c].im != 0.0);
+                            npart[x] = k;
+                        }
                         lp[x] = slot_p[sl];
                         lq[x] = slot_q[sl];
                         x++;
@@ -742,18 +845,35 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                         lq[x] = hq[s0 + x];
                     }
                 }
-                chunk_reverse_order(mrj, nijsiz, perm); /* GETHTI read order */
-                for (long x = 0; x < mrj; x++) {
-                    cplx v = lv[perm[x]];
-                    if (conjug) v = cconj(v);
-                    if (is < 0) v = cscal(-1.0, v);
-                    rj[x] = v;
+                if (breit) {
+                    breit_chunk_order(mrj, npart, nijsiz, perm); /* GETHTBI read order */
+                    for (long x = 0; x < mrj; x++) {
+                        cplx a = lv[perm[x] * 3], b = lv[perm[x] * 3 + 1], c = lv[perm[x] * 3 + 2];
+                        if (conjug) { /* conjugate and swap the QB streams (trans2.F:131-148) */
+                            cplx t2 = cconj(b);
+                            a = cconj(a);
+                            b = cconj(c);
+                            c = t2;
+                        }
+                        if (is < 0) { a = cscal(-1.0, a); b = cscal(-1.0, b); c = cscal(-1.0, c); }
+                        rj[x * 3] = a;
+                        rj[x * 3 + 1] = b;
+                        rj[x * 3 + 2] = c;
+                    }
+                } else {
+                    chunk_reverse_order(mrj, nijsiz, perm); /* GETHTI read order */
+                    for (long x = 0; x < mrj; x++) {
+                        cplx v = lv[perm[x]];
+                        if (conjug) v = cconj(v);
+                        if (is < 0) v = cscal(-1.0, v);
+                        rj[x] = v;
+                    }
                 }
                 /* MATMUL3 (matmul3.F:3-34) */
                 memset(rk, 0, sizeof(cplx) * (size_t)n * m);
                 for (long x = 0; x < mrj; x++) {
                     int p = lp[perm[x]] - 1, q = lq[perm[x]] - 1;
-                    cplx a = rj[x];
+                    cplx a = rj[x * nstr];
                     for (int k = 0; k < m; k++) {
                         rk[p + (long)k * n] = cadd(rk[p + (long)k * n], cmul(a, QA(q, k)));
                         rk[q + (long)k * n] = cadd(rk[q + (long)k * n], cmul(a, QA(p, k)));
@@ -766,18 +886,42 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
                         for (int l = 0; l < n; l++) tmp = cadd(tmp, cmul(cconj(QA(l, i)), rk[l + (long)j * n]));
                         rlr[i + (long)j * m] = tmp;
                     }
-                /* MSUMTIM(RL,RLR,+1) (msumtim.F:3-21) */
+                /* MSUMTIM(RL,RLR,ISG) (msumtim.F:3-21), ISG = +1 Coulomb, -1 Gaunt */
                 for (int i = 1; i <= m; i++)
                     for (int j = 1; j <= m; j++) {
                         int itr = abs(itrmo[i - 1]), jtr = abs(itrmo[j - 1]);
                         int sg = (itrmo[i - 1] * itrmo[j - 1] >= 0) ? 1 : -1;
+                        if (breit) sg = -sg;
                         rl[(j - 1) + (long)(i - 1) * m] =
                             cadd(rlr[(j - 1) + (long)(i - 1) * m], cscal(sg, rlr[(itr - 1) + (long)(jtr - 1) * m]));
                     }
+                if (breit) {
+                    /* MATMUL7(RJB, QB) then RL += QA^H RK; MATMUL7(RJC, QA) then
+                     * RL += QB^H RK (trans2.F:166-177, matmul7.F:3-35) */
+                    for (int st = 1; st <= 2; st++) {
+                        memset(rk, 0, sizeof(cplx) * (size_t)n * m);
+                        for (long x = 0; x < mrj; x++) {
+                            int p = lp[perm[x]] - 1, q = lq[perm[x]] - 1;
+                            cplx a = rj[x * 3 + st];
+                            for (int k = 0; k < m; k++) {
+                                cplx bq = st == 1 ? QB(q, k) : QA(q, k), bp = st == 1 ? QB(p, k) : QA(p, k);
+                                rk[p + (long)k * n] = cadd(rk[p + (long)k * n], cscal(2.0, cmul(a, bq)));
+                                rk[q + (long)k * n] = cadd(rk[q + (long)k * n], cscal(2.0, cmul(a, bp)));
+                            }
+                        }
+                        for (int j = 0; j < m; j++)
+                            for (int i = 0; i < m; i++) {
+                                cplx tmp = {0.0, 0.0};
+                                for (int l = 0; l < n; l++)
+                                    tmp = cadd(tmp, cmul(cconj(st == 1 ? QA(l, i) : QB(l, i)), rk[l + (long)j * n]));
+                                rl[i + (long)j * m] = cadd(tmp, rl[i + (long)j * m]);
+                            }
+                    }
+                }
                 /* the reduced-matrix-element gather/scatter (trans2.F:199-265)
                  * is the identity for a single one-dimensional irrep */
             }
-            free(rj); free(lv); free(lp); free(lq); free(rk); free(rlr); free(perm);
+            free(rj); free(lv); free(npart); free(lp); free(lq); free(rk); free(rlr); free(perm);
         }
         /* OUTPP1 / OUTPP2 in TRANS2's loop order (trans2.F:272-310) */
         for (long t = b0; t < b1; t++) {
@@ -826,7 +970,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     }
     free(items); free(hval); free(hp); free(hq); free(jcnt);
     free(hstore); free(hkeep); free(slot_of); free(slot_pq); free(slot_p); free(slot_q);
-    free(bstart); free(vmx);
+    free(bstart); free(vmx); free(qbv);
 
     out->nrec = md.nrec;
     out->hdr = md.hdr;
@@ -844,6 +988,7 @@ int orc_run(const orc_params* prm, const double* qa_in, const int* itrmo, const 
     out->nijsiz = nijsiz;
     out->nc2 = nc2;
 #undef QA
+#undef QB
     return 0;
 }
 

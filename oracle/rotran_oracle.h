@@ -22,6 +22,8 @@ typedef struct orc_params {
     long n_pq_select;
     long fake_list_len;    /* >0 (timing samples): TRANS2 reads lists of this
                               length with synthetic values instead of TRANS1's */
+    int breit;             /* 1: the Gaunt (Breit) transformation of the SL|SL
+                              integrals of file 4 (SRTBREI) into MDBINT */
 } orc_params;
 
 typedef struct orc_result {
