@@ -37,6 +37,8 @@ SMALL = dict(name="c1_n64_k32", n_l=24, n_s=40, nkr=32, seed=0)
 # a profiling case: the same kernels at a size whose device footprint stays
 # near 1 GB (inputs still larger than L2)
 PROFILE = dict(name="profile_n128_k32", n_l=48, n_s=80, nkr=32, seed=0)
+# a second profiling case whose GEMM2/GEMM4 (M = 2m = 240) run as CTA pairs
+PROFILE2 = dict(name="profile_n200_k60", n_l=80, n_s=120, nkr=60, seed=0)
 # the large single transform: 192 L + 288 S AOs, 200 Kramers pairs, AOs in 4
 # irreps with the integrals zero outside the symmetry-allowed blocks
 LARGE = dict(name="large_c2v_n480_k200", n_l=192, n_s=288, nkr=200, seed=0, n_irrep=4)
@@ -421,7 +423,7 @@ def main():
     ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "c1", "profile", "large", "batched", "gemm", "files"])
+                    choices=["precision", "c1", "profile", "profile2", "large", "batched", "gemm", "files"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
@@ -437,7 +439,8 @@ def main():
         return run_gemm_case(args, rank)
     if args.workload == "files":
         return run_files_case(args, rank)
-    work = {"precision": WORKLOAD, "c1": SMALL, "profile": PROFILE, "large": LARGE}[args.workload]
+    work = {"precision": WORKLOAD, "c1": SMALL, "profile": PROFILE, "profile2": PROFILE2,
+            "large": LARGE}[args.workload]
 
     if args.impl == "reference":
         if rank != 0:

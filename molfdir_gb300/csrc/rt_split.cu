@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -887,6 +888,7 @@ struct SplitState {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     int num_sms = 152;
     int max_pairs = 0;  // CTA pairs of the pair kernel resident at once
+    bool use_pairs = true;  // RT_GEMM_KERNEL=single selects the single-CTA kernel throughout
     // constant operands
     ConstSlices qah;                 // A of GEMM2/4: rows 2m, K = 2n
     ConstSlices qahB;                // the barred rows of qah (both planes): rows m
@@ -996,6 +998,15 @@ static SplitState* state(rt_ctx* c) {
         set_smem_limit(k_split_gemm_pair<EpiFF_RowMajor>, need2, prop);
         set_smem_limit(k_split_gemm_pair<EpiFF_RK>, need2, prop);
         S->max_pairs = pair_capacity((const void*)k_split_gemm_pair<EpiFF_RowMajor>, need2, S->num_sms);
+        // Diagnostic choice between the two implementations of the same
+        // product (identical digit arithmetic and accumulation): the CTA-pair
+        // kernel for M > 128 (default) or the single-CTA kernel for all.
+        const char* kv = getenv("RT_GEMM_KERNEL");
+        S->use_pairs = !(kv && std::strcmp(kv, "single") == 0);
+        const char* tr = getenv("RT_TRACE");
+        if (tr && std::strcmp(tr, "0") != 0)
+            std::fprintf(stderr, "[rt] split GEMM: %s kernel, %d CTA pairs resident (%d SMs)\n",
+                         S->use_pairs ? "CTA-pair" : "single-CTA", S->max_pairs, S->num_sms);
         c->split = S;
     }
     return c->split;
@@ -1195,7 +1206,7 @@ static void run_gemm(rt_ctx* c, const void* a_sl, const int* a_exp, long long M,
     const bool nocp = test_no_copies();
     const unsigned long long wait_ns = nocp ? 50000000ull : WAIT_NS;
     // CTA pairs (256 rows per pair tile) unless one 128-row tile covers M
-    if (ksplit == 1 && M > SBM && S->max_pairs >= 1) {
+    if (ksplit == 1 && M > SBM && S->max_pairs >= 1 && S->use_pairs) {
         CUtensorMap ma2 = make_map(S, a_sl, M, Kp, s, PBM / 2);
         CUtensorMap mb2 = make_map(S, b_sl, N, Kp, s, PBN / 2, b_slice_rows);
         g.tiles_m = (int)((M + PBM - 1) / PBM);
