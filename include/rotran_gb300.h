@@ -51,7 +51,9 @@ typedef struct rt_config {
     int nsp;          /* NSP: active spinors */
     int nkr;          /* NKR: Kramers pairs, NSP = 2*NKR */
     int mfil;         /* MFIL: SRT files read (1 LL, 2 +SS|LL, 3 +SS|SS), readin.F:83-84 */
-    int breit;        /* BREIT: must be 0 (Coulomb); Gaunt is not implemented */
+    int breit;        /* BREIT (readin.F:17, default .FALSE. at readin.F:80): 0 Coulomb; 1 Gaunt, file 4 (SL|SL)
+                         only, result stream MDBINT (rt_transform only; needs
+                         0 < NSC1 < NSC; batches and rt_adjoint refuse it) */
     double thrgen;    /* THRGEN (readin.F:93) */
     double throut;    /* THROUT (readin.F:94): |x| > THROUT is written to MDCINT */
     int precision;    /* RT_PREC_FP64 or RT_PREC_SPLIT_BF16 */

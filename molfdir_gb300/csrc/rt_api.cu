@@ -103,10 +103,17 @@ void check_config(const rt_config* cfg) {
     if (cfg->nkr < 1 || cfg->nsp != 2 * cfg->nkr)
         throw Error(RT_ERR_USER, "NSP must equal 2*NKR with NKR >= 1");
     if (cfg->nkr > cfg->nsc) throw Error(RT_ERR_USER, "more Kramers pairs than scalar functions");
-    if (cfg->mfil < 1 || cfg->mfil > 3) throw Error(RT_ERR_USER, "MFIL must be 1, 2 or 3");
-    if (cfg->mfil == 1 && cfg->nsc != cfg->nsc1)
-        throw Error(RT_ERR_USER, "MFIL=1 transforms the large component only: NSC must equal NSC1");
-    if (cfg->breit) throw Error(RT_ERR_USER, "Breit (Gaunt) integrals are not implemented");
+    if (cfg->breit != 0 && cfg->breit != 1) throw Error(RT_ERR_USER, "BREIT must be 0 or 1");
+    if (cfg->breit) {
+        // the Gaunt transformation (BREIT = .TRUE., MFIL = 0: rotran.F:48-57)
+        // reads the SL|SL integrals of file 4; MFIL is not used
+        if (cfg->nsc1 < 1 || cfg->nsc1 >= cfg->nsc)
+            throw Error(RT_ERR_USER, "the Gaunt (Breit) transformation needs large and small component functions");
+    } else {
+        if (cfg->mfil < 1 || cfg->mfil > 3) throw Error(RT_ERR_USER, "MFIL must be 1, 2 or 3");
+        if (cfg->mfil == 1 && cfg->nsc != cfg->nsc1)
+            throw Error(RT_ERR_USER, "MFIL=1 transforms the large component only: NSC must equal NSC1");
+    }
     if (cfg->precision != RT_PREC_FP64 && cfg->precision != RT_PREC_SPLIT_BF16)
         throw Error(RT_ERR_USER, "unknown precision");
     if (cfg->slices != 0 && (cfg->slices < 2 || cfg->slices > 6))
@@ -170,6 +177,11 @@ void plan_ao(rt_ctx* c) {
     for (int p = 0; p < P.n; ++p)
         for (int q = 0; q <= p; ++q) {
             bool pl = p < P.nL, ql = q < P.nL;
+            if (cfg.breit) {  // the SL blocks only (makind.F:91-95)
+                if (pl == ql) continue;
+                pk.push_back({2, irr(p) ^ irr(q), (long long)p * (p + 1) / 2 + q, p, q});
+                continue;
+            }
             if (pl != ql) continue;  // no SL blocks for Coulomb (makind.F:75)
             pk.push_back({pl ? 0 : 1, irr(p) ^ irr(q), (long long)p * (p + 1) / 2 + q, p, q});
         }
@@ -198,29 +210,37 @@ void plan_ao(rt_ctx* c) {
         for (int rb = 0; rb < P.nblk; ++rb) {
             int comp = P.blk_comp[rb];
             bool present;
-            if (pg.cls == 0) present = comp == 0 || cfg.mfil >= 2;   // (LL|LL), (LL|SS)
+            if (pg.cls == 2) present = true;                          // (SL|SL): r in L or S
+            else if (pg.cls == 0) present = comp == 0 || cfg.mfil >= 2;   // (LL|LL), (LL|SS)
             else present = comp == 0 ? cfg.mfil >= 2 : cfg.mfil >= 3; // (SS|LL), (SS|SS)
             if (!present) continue;
+            // partner block of s: the same component (Coulomb) or the other
+            // one (Gaunt: G_pq(r,s) couples an L and an S function)
+            const int kcomp = pg.cls == 2 ? 1 - comp : comp;
             int kb = -1;
             for (int b = 0; b < P.nblk; ++b)
-                if (P.blk_comp[b] == comp && P.blk_irr[b] == (P.blk_irr[rb] ^ pg.gamma)) kb = b;
+                if (P.blk_comp[b] == kcomp && P.blk_irr[b] == (P.blk_irr[rb] ^ pg.gamma)) kb = b;
             if (kb < 0) continue;
             P.g1.push_back({g, rb, kb, 0, 0});
         }
     }
     (void)base;
-    // expansion tables per component
+    // expansion tables per row component: columns of the same component
+    // (Coulomb) or of the other one (Gaunt)
     for (int comp = 0; comp < 2; ++comp) {
+        const int oc = cfg.breit ? 1 - comp : comp;
         int nc = P.ncomp[comp], off = P.comp_off[comp];
-        P.pidx[comp].assign((size_t)nc * nc, -1);
+        int ncol = P.ncomp[oc], coff = P.comp_off[oc];
+        P.pidx_cols[comp] = ncol;
+        P.pidx[comp].assign((size_t)nc * ncol, -1);
         // sorted position -> reference index
         std::vector<int> ref_of(P.n);
         for (int p = 0; p < P.n; ++p) ref_of[P.ao_sorted[p]] = p;
         for (int a = 0; a < nc; ++a)
-            for (int b = 0; b < nc; ++b) {
-                int p = ref_of[off + a], q = ref_of[off + b];
+            for (int b = 0; b < ncol; ++b) {
+                int p = ref_of[off + a], q = ref_of[coff + b];
                 int hi = std::max(p, q), lo = std::min(p, q);
-                P.pidx[comp][(size_t)a * nc + b] = P.pair_of_orig[(long long)hi * (hi + 1) / 2 + lo];
+                P.pidx[comp][(size_t)a * ncol + b] = P.pair_of_orig[(long long)hi * (hi + 1) / 2 + lo];
             }
     }
     (void)ao_pos;
@@ -343,6 +363,47 @@ static void build_coef_device(rt_ctx* c) {
                 q3[(size_t)(nc + q) * 2 * m + m + k] = re;
             }
         upload(c, c->d_qar[comp], q3);
+    }
+    if (c->cfg.breit) {
+        // QB of the internal (Kramers-sorted) spinors from QA: QB(j) =
+        // -conj(QA(jbar)) for unbarred j, QB(jbar) = conj(QA(j))
+        // (kramers.F:134-150)
+        std::vector<double> br((size_t)n * m), bi((size_t)n * m);
+        for (int i = 0; i < m; ++i) {
+            const int t = c->itrmo[i], pi = std::abs(t) - 1;
+            const double sg = t > 0 ? -1.0 : 1.0;
+            for (int r = 0; r < n; ++r) {
+                br[(size_t)r * m + i] = sg * qr[(size_t)r * m + pi];
+                bi[(size_t)r * m + i] = -sg * qi[(size_t)r * m + pi];
+            }
+        }
+        std::vector<double> qbh((size_t)2 * m * 2 * n), qbhs((size_t)2 * m * 2 * n, 0.0);
+        for (int a = 0; a < m; ++a)
+            for (int r = 0; r < n; ++r) {
+                double re = br[(size_t)r * m + a], im = bi[(size_t)r * m + a];
+                qbh[(size_t)a * 2 * n + r] = re;
+                qbh[(size_t)a * 2 * n + n + r] = im;
+                qbh[(size_t)(m + a) * 2 * n + r] = -im;
+                qbh[(size_t)(m + a) * 2 * n + n + r] = re;
+                if (r >= P.nL)  // small-component rows only (trans1.F:91-96 reads HA's S rows)
+                    for (int x : {a * 2 * n + r, a * 2 * n + n + r, (m + a) * 2 * n + r, (m + a) * 2 * n + n + r})
+                        qbhs[(size_t)x] = qbh[(size_t)x];
+            }
+        upload(c, c->d_qbh, qbh);
+        upload(c, c->d_qbhS, qbhs);
+        for (int comp = 0; comp < 2; ++comp) {
+            int nc = P.ncomp[comp], off = P.comp_off[comp];
+            std::vector<double> q3((size_t)2 * nc * 2 * m);
+            for (int q = 0; q < nc; ++q)
+                for (int k = 0; k < m; ++k) {
+                    double re = br[(size_t)(off + q) * m + k], im = bi[(size_t)(off + q) * m + k];
+                    q3[(size_t)q * 2 * m + k] = re;
+                    q3[(size_t)q * 2 * m + m + k] = im;
+                    q3[(size_t)(nc + q) * 2 * m + k] = -im;
+                    q3[(size_t)(nc + q) * 2 * m + m + k] = re;
+                }
+            upload(c, c->d_qbr[comp], q3);
+        }
     }
     // split path: slice the constant operands once
     if (c->cfg.precision == RT_PREC_SPLIT_BF16) split_prepare_constants(c);
@@ -696,7 +757,7 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = fals
         c->d_jval = dalloc<double>(c, (size_t)2 * c->bucket_cap);
         c->d_jrs = dalloc<int>(c, (size_t)2 * c->bucket_cap);
     }
-    if (!c->d_hp) c->d_hp = dalloc<double>(c, (size_t)2 * KK1 * P.P);
+    if (!c->d_hp) c->d_hp = dalloc<double>(c, (size_t)2 * KK1 * P.P * (c->cfg.breit ? 3 : 1));
     for (int cc = 0; cc < 4; ++cc) {
         if (!c->d_oidx[cc]) {
             c->d_oidx[cc] = dalloc<int>(c, (size_t)2 * std::max(1LL, w.cap[cc]));
@@ -718,9 +779,12 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = fals
     // bytes per pair of stage A and per item of stage B
     long long a_pp = 0;
     for (long long v : P.pg_a_pp) a_pp = std::max(a_pp, v);
-    double per_pair = 16.0 * n * m + 16.0 * m * m + (S ? 0.0 : 8.0 * a_pp);
+    const bool breit = c->cfg.breit != 0;
+    // Gaunt: a second RI (QB^H HA) per pair; three RLR per item
+    double per_pair = 16.0 * n * m + (breit ? 32.0 : 16.0) * m * m + (S ? 0.0 : 8.0 * a_pp);
     int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
-    double per_item = 16.0 * ncmax * ncmax + 16.0 * n * m + 16.0 * m * m;
+    const double m3_el = breit ? (double)P.ncomp[0] * P.ncomp[1] : (double)ncmax * ncmax;
+    double per_item = 16.0 * m3_el + 16.0 * n * m + (breit ? 48.0 : 16.0) * m * m;
     if (S) {
         per_pair += split_stageA_bytes_per_pair(c);
         per_item += split_stageB_bytes_per_item(c);
@@ -774,7 +838,8 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
     for (int p = 0; p < P.n; ++p)
         for (int q = 0; q <= p; ++q) {
             bool pl = p < P.nL, ql = q < P.nL;
-            bool inc = !(!pl && ql) && !(!pl && c->cfg.mfil < 3);  // makind.F:75-77
+            bool inc = c->cfg.breit ? pl != ql  // the SL blocks of the Gaunt integrals (makind.F:91-95)
+                                    : !(!pl && ql) && !(!pl && c->cfg.mfil < 3);  // makind.F:75-77
             pqr[(long long)p * (p + 1) / 2 + q] = inc ? 1 : 0;
         }
     std::vector<int> pgroup(P.P), pgs, pgz, aopos(P.n), g1of(P.pgroups.size() * P.nblk, -1), g1k;
@@ -806,6 +871,51 @@ static void upload_tables(rt_ctx* c, DeviceTabs& T, std::vector<void*>& tmp) {
 
 namespace {
 
+// Gaunt items: for TRANS2's item (I, J), UNIQUE with the Breit sign
+// (unique.F:1-50; the sign is turned at unique.F:34) gives the pair JI whose
+// values TRBOUT stored, and TROUT's enumeration of JI (IBAR, IK, JK >= IK:
+// trbout.F:35-42) gives its spinors I' = KRA(IK) or KRB(IK), J' = KRB(JK).
+std::vector<BreitItem> breit_items(rt_ctx* c) {
+    const Plan& P = c->plan;
+    const int K = P.K;
+    std::vector<int2> ji_pair;  // JI-1 -> (I', J') internal, 0-based
+    for (int ibar = 1; ibar <= 2; ++ibar)
+        for (int ik = 1; ik <= K; ++ik)
+            for (int jk = ik; jk <= K; ++jk)
+                ji_pair.push_back(make_int2((ibar == 1 ? c->kra[ik - 1] : c->krb[ik - 1]) - 1, c->krb[jk - 1] - 1));
+    std::vector<BreitItem> out(P.items.size());
+    for (size_t t = 0; t < P.items.size(); ++t) {
+        const Item& it = P.items[t];
+        int ikr = c->ikrmo[it.I], jkr = c->ikrmo[it.J];
+        int iikr, jjkr;
+        bool conj;
+        if (std::abs(ikr) >= std::abs(jkr)) { iikr = ikr; jjkr = jkr; conj = false; }
+        else { iikr = jkr; jjkr = ikr; conj = true; }
+        int is = 1;
+        if (iikr > 0) {
+            is = (iikr * jjkr >= 0) ? 1 : -1;
+            is = -is;  // Breit
+            iikr = -iikr;
+            jjkr = -jjkr;
+            conj = !conj;
+        }
+        const int off = K * (K + 1) / 2;
+        const int ij = jjkr > 0 ? (jjkr - 1) * (2 * K - jjkr) / 2 - iikr : off - (jjkr + 1) * (2 * K + jjkr) / 2 - iikr;
+        if (ij < 1 || ij > (int)ji_pair.size()) throw Error(RT_ERR_INTERNAL, "Gaunt item outside the JI list");
+        const int I2 = ji_pair[ij - 1].x, J2 = ji_pair[ij - 1].y;
+        BreitItem b;
+        b.x = J2;
+        b.y = I2;
+        b.xb = std::abs(c->itrmo[J2]) - 1;
+        b.yb = std::abs(c->itrmo[I2]) - 1;
+        b.s = ((c->itrmo[J2] > 0) == (c->itrmo[I2] > 0)) ? -1.0f : 1.0f;
+        b.conj = conj ? 1 : 0;
+        b.neg = is < 0 ? 1 : 0;
+        out[t] = b;
+    }
+    return out;
+}
+
 // Device tables and temporaries of one pass over the integral records
 // (rt_transform and rt_adjoint), freed when the pass ends.
 struct Pass {
@@ -819,6 +929,7 @@ struct Pass {
     double* d_pvmx = nullptr;
     int *d_kra = nullptr, *d_krb = nullptr, *d_itrmo = nullptr;
     int* d_pidx[2] = {nullptr, nullptr};
+    BreitItem* d_bitems = nullptr;  // Gaunt: UNIQUE's stored pair per item
     unsigned long long* d_stat = nullptr;
     int pair_chunk = 0, item_chunk = 0;
     int launches = 0;
@@ -864,6 +975,10 @@ void pass_setup(Pass& ps, bool exact = false) {
     ps.d_krb = ps.upload(ctx->krb.data(), (size_t)K);
     ps.d_itrmo = ps.upload(ctx->itrmo.data(), (size_t)m);
     for (int cc = 0; cc < 2; ++cc) ps.d_pidx[cc] = ps.upload(P.pidx[cc].data(), P.pidx[cc].size());
+    if (ctx->cfg.breit) {
+        const std::vector<BreitItem> bi = breit_items(ctx);
+        ps.d_bitems = ps.upload(bi.data(), bi.size());
+    }
     ps.d_stat = ps.alloc<unsigned long long>(8);
     RT_CUDA(cudaMemsetAsync(ps.d_stat, 0, 8 * sizeof(unsigned long long), ctx->stream));
 }
@@ -889,6 +1004,7 @@ void pass_bucketing(Pass& ps) {
     ScatterTabs tb{P.n, ctx->cfg.mfil, P.nblk, T.pq_read, T.pair_of_orig, T.pair_group, T.pg_start,
                    T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk,
                    T.jb_base, T.jb_band, T.pg_bbase, T.pg_njobs};
+    tb.breit = ctx->cfg.breit;
     launch_bucket(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, ctx->n_int, ps.d_roff, ps.d_rmeta,
                   (int)ctx->rec_off.size(), tb, P.P, ctx->d_bcount, ctx->d_boff, ctx->d_bval,
                   ctx->d_brs, P.nbuckets, ctx->d_jstart, ctx->d_jcount, ctx->d_jval, ctx->d_jrs,
@@ -934,9 +1050,11 @@ void pass_stage_a(Pass& ps, double thrgen) {
     const int nsl = split ? ctx->cfg.slices : 0;
     float* d_pthr = pass_pair_thr(ps, thrgen);
     tr.mark("A: job and threshold tables");
+    const bool breit = ctx->cfg.breit != 0;
     double* ha = ctx->d_ha;
     double* ri = ha + (size_t)2 * n * m * pair_chunk;
-    double* a1 = ri + (size_t)2 * m * m * pair_chunk;  // FP64 GEMM1 operand (plain path)
+    double* ri2 = ri + (size_t)2 * m * m * pair_chunk;  // Gaunt: QB^H HA
+    double* a1 = (breit ? ri2 : ri) + (size_t)2 * m * m * pair_chunk;  // FP64 GEMM1 operand (plain path)
     for (size_t g = 0; g < P.pgroups.size(); ++g) {
         const PairGroup& pg = P.pgroups[g];
         // does every r block meet this pair group?
@@ -973,6 +1091,26 @@ void pass_stage_a(Pass& ps, double thrgen) {
             }
             tr.mark("A: GEMM1");
             EpiRowMajor e2{ri, (long long)m * npc, 0};
+            if (breit) {
+                // Gaunt (trans1.F:81-100): RIA = QA^H HA, RI2 = QB^H HA (S rows),
+                // then TRBOUT's three streams for every item
+                EpiRowMajor e2b{ri2, (long long)m * npc, 0};
+                gemm_begin();
+                if (split)
+                    split_gemm2_breit(ctx, ha, 2 * n, (long long)m * npc, e2, e2b, &ps.launches);
+                else {
+                    gemm_f64(st, ctx->d_qah, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2);
+                    gemm_f64(st, ctx->d_qbhS, 2 * n, 0, ha, (long long)m * npc, 0, 2 * m, m * npc, 2 * n, 1, e2b);
+                    ps.launches += 2;
+                }
+                gemm_end(2.0 * 2.0 * 2 * m * (double)m * npc * 2 * n);
+                tr.mark("A: slice HA + GEMM2 (QA and QB)");
+                launch_trb_select(st, split, ri, ri2, m, npc, pg.start + c0, P.P, ps.d_bitems, KK1, ctx->d_hp,
+                                  ps.d_stat + 1);
+                ps.launches += (KK1 + 65534) / 65535;
+                tr.mark("A: Gaunt selection");
+                continue;
+            }
             gemm_begin();
             if (split)
                 split_gemm2_kramers(ctx, ha, 2 * n, (long long)m * npc, e2, &ps.launches);
@@ -991,18 +1129,24 @@ void pass_stage_a(Pass& ps, double thrgen) {
 
 // Algorithmic FLOPs of the transformation (dense-block count of the
 // reference algorithm).
-double algorithmic_flops(const Plan& P) {
+double algorithmic_flops(const Plan& P, double KK1, bool breit) {
     const int n = P.n, m = P.m;
-    const double KK1 = (double)P.items.size();
     double f1 = 0.0;
     for (auto& gg : P.g1)
         f1 += 2.0 * P.blk_size[gg.rblk] * (double)P.pgroups[gg.pg].size * P.blk_size[gg.kblk] * 2.0 * m;
-    f1 += (double)P.P * 8.0 * n * (double)m * m;
+    // Gaunt: the second ZGEMM with QB (trans1.F:91-96)
+    f1 += (breit ? 2.0 : 1.0) * (double)P.P * 8.0 * n * (double)m * m;
     double f2 = 0.0;
-    for (int cc = 0; cc < 2; ++cc) f2 += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
-    f2 = KK1 * (f2 + 8.0 * n * (double)m * m);
+    if (breit)  // three streams, each MATMUL3/7 across the components and a ZGEMM
+        f2 = KK1 * 3.0 * (2.0 * 8.0 * (double)P.ncomp[0] * P.ncomp[1] * m + 8.0 * n * (double)m * m);
+    else {
+        for (int cc = 0; cc < 2; ++cc) f2 += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
+        f2 = KK1 * (f2 + 8.0 * n * (double)m * m);
+    }
     return f1 + f2;
 }
+
+double algorithmic_flops(const Plan& P, bool breit) { return algorithmic_flops(P, (double)P.items.size(), breit); }
 
 }  // namespace
 
@@ -1046,8 +1190,12 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     // ---- stage B: second half-transformation (TRANS2) + PPSYM per item chunk ----
     double* m3 = ctx->d_ha;
     int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
-    double* rk = m3 + (size_t)2 * ncmax * ncmax * item_chunk;
+    const bool breit = ctx->cfg.breit != 0;
+    const size_t m3_el = breit ? (size_t)P.ncomp[0] * P.ncomp[1] : (size_t)ncmax * ncmax;
+    double* rk = m3 + 2 * m3_el * item_chunk;
     double* rlr = rk + (size_t)2 * n * m * item_chunk;
+    double* rlr_b = rlr + (size_t)2 * m * m * item_chunk;   // Gaunt streams 2 and 3
+    double* rlr_c = rlr_b + (size_t)2 * m * m * item_chunk;
     EmitRec* d_recs = ps.alloc<EmitRec>((size_t)3 * item_chunk);
     OutStreams os;
     for (int cc = 0; cc < 4; ++cc) {
@@ -1061,10 +1209,41 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     for (int i0 = 0; i0 < KK1; i0 += item_chunk) {
         const int nij = std::min(item_chunk, KK1 - i0);
         const long long rkplane = (long long)n * nij * m;
-        for (int cc = 0; cc < 2; ++cc) {
+        // Gaunt (trans2.F:129-177): stream 1 MATMUL3 with QA then QA^H,
+        // stream 2 MATMUL7 (x2) with QB then QA^H, stream 3 MATMUL7 (x2)
+        // with QA then QB^H; rows of one component meet the other one's
+        for (int sx = 0; breit && sx < 3; ++sx) {
+            const double* hps = ctx->d_hp + (size_t)sx * 2 * KK1 * P.P;
+            for (int rc = 0; rc < 2; ++rc) {
+                const int oc = 1 - rc, nrow = P.ncomp[rc], ncol = P.ncomp[oc];
+                if (nrow == 0 || ncol == 0) continue;
+                launch_expand(st, hps, P.P, KK1, i0, nij, ps.d_pidx[rc], nrow, ncol, m3, sx > 0, split);
+                ++ps.launches;
+                EpiRK e3{rk, m, (long long)P.comp_off[rc] * nij, rkplane};
+                gemm_begin();
+                if (split)
+                    split_gemm3_op(ctx, sx == 1 ? 1 : 0, oc, m3, nrow, ncol, nij, e3, &ps.launches);
+                else
+                    gemm_f64(st, m3, 2 * ncol, 0, sx == 1 ? ctx->d_qbr[oc] : ctx->d_qar[oc], 2 * m, 0, nrow * nij,
+                             2 * m, 2 * ncol, 1, e3), ++ps.launches;
+                gemm_end(2.0 * nrow * (double)nij * 2 * m * 2 * ncol);
+            }
+            tr.mark("B: Gaunt expand + GEMM3");
+            double* out = sx == 0 ? rlr : sx == 1 ? rlr_b : rlr_c;
+            EpiRowMajor e4{out, (long long)nij * m, 0};
+            gemm_begin();
+            if (split)
+                split_gemm4_op(ctx, sx == 2 ? 1 : 0, rk, 2 * n, (long long)nij * m, e4, &ps.launches);
+            else
+                gemm_f64(st, sx == 2 ? ctx->d_qbh : ctx->d_qah, 2 * n, 0, rk, (long long)nij * m, 0, 2 * m, nij * m,
+                         2 * n, 1, e4), ++ps.launches;
+            gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
+            tr.mark("B: Gaunt GEMM4");
+        }
+        for (int cc = 0; cc < 2 && !breit; ++cc) {
             const int nc = P.ncomp[cc];
             if (nc == 0) continue;
-            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, m3);
+            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, nc, m3);
             ++ps.launches;
             tr.mark("B: expand M_ij(p,q)");
             EpiRK e3{rk, m, (long long)P.comp_off[cc] * nij, rkplane};
@@ -1076,22 +1255,29 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             gemm_end(2.0 * nc * (double)nij * 2 * m * 2 * nc);
             tr.mark("B: GEMM3");
         }
-        EpiRowMajor e4{rlr, (long long)nij * m, 0};
-        gemm_begin();
-        if (split)
-            split_gemm24(ctx, rk, 2 * n, (long long)nij * m, e4, &ps.launches);
-        else
-            gemm_f64(st, ctx->d_qah, 2 * n, 0, rk, (long long)nij * m, 0, 2 * m, nij * m, 2 * n, 1, e4), ++ps.launches;
-        gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
-        tr.mark("B: slice RK + GEMM4");
+        if (!breit) {
+            EpiRowMajor e4{rlr, (long long)nij * m, 0};
+            gemm_begin();
+            if (split)
+                split_gemm24(ctx, rk, 2 * n, (long long)nij * m, e4, &ps.launches);
+            else
+                gemm_f64(st, ctx->d_qah, 2 * n, 0, rk, (long long)nij * m, 0, 2 * m, nij * m, 2 * n, 1, e4),
+                    ++ps.launches;
+            gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
+            tr.mark("B: slice RK + GEMM4");
+        }
         // MDCINT selection for the records of this chunk
         chunk_recs.assign(w.recs.begin() + w.item_rec0[i0], w.recs.begin() + w.item_rec0[i0 + nij]);
         for (int t = i0; t < i0 + nij; ++t)
             for (int r = w.item_rec0[t]; r < w.item_rec0[t + 1]; ++r)
                 chunk_recs[r - w.item_rec0[i0]].ijl = t - i0;
         RT_CUDA(cudaMemcpyAsync(d_recs, chunk_recs.data(), chunk_recs.size() * sizeof(EmitRec), cudaMemcpyHostToDevice, st));
-        launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), ps.d_kra, ps.d_krb,
-                    ps.d_itrmo, ctx->cfg.throut, os);
+        if (breit)  // MSUMTIM with ISG = -1 on stream 1, plus streams 2 and 3
+            launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), ps.d_kra, ps.d_krb,
+                        ps.d_itrmo, ctx->cfg.throut, os, rlr_b, rlr_c, -1.0);
+        else
+            launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), ps.d_kra, ps.d_krb,
+                        ps.d_itrmo, ctx->cfg.throut, os);
         ps.launches += 3;
         // the host copy of chunk_recs must outlive the async copy
         RT_CUDA(cudaStreamSynchronize(st));
@@ -1126,7 +1312,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         S.nfinal[cc] = tot[cc];
         S.nrec[cc] = w.nrec[cc];
     }
-    S.flops_algorithmic = algorithmic_flops(P);
+    S.flops_algorithmic = algorithmic_flops(P, ctx->cfg.breit != 0);
     S.device_bytes = (long long)ctx->dev_peak;
     S.gpu_launches = ps.launches;
     S.gemm_launches = kt.launches;
@@ -1180,6 +1366,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     API_TRY
     if (!gamma || !dedc) throw Error(RT_ERR_USER, "rt_adjoint: null gamma or dEdC");
     if (ctx->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
+    if (ctx->cfg.breit) throw Error(RT_ERR_USER, "the adjoint is built for the Coulomb transformation");
     if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
     Plan& P = ctx->plan;
     cudaStream_t st = ctx->stream;
@@ -1266,7 +1453,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
         for (int cc = 0; cc < 2; ++cc) {
             const int nc = P.ncomp[cc];
             if (nc == 0) continue;
-            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, m3);
+            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, nc, m3);
             ++ps.launches;
             if (split) {
                 unsigned char* save = wp;
@@ -1358,7 +1545,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     S.ms_total = tot_ms;
     double fx = 0.0;
     for (int cc = 0; cc < 2; ++cc) fx += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
-    S.flops_algorithmic = (algorithmic_flops(P) - (double)KK1 * (fx + 8.0 * n * (double)m * m)) +
+    S.flops_algorithmic = (algorithmic_flops(P, false) - (double)KK1 * (fx + 8.0 * n * (double)m * m)) +
                           (double)KK1 * (fx + 16.0 * n * (double)m * m);
     S.device_bytes = (long long)ctx->dev_peak;
     S.gpu_launches = ps.launches;
@@ -1520,7 +1707,7 @@ void batch_enqueue(rt_batch* b, bool timed) {
             const Plan& P = c->plan;
             const int nc = P.ncomp[cc], KK1 = (int)P.items.size();
             if (nc == 0) return;
-            launch_expand(ss, c->d_hp, P.P, KK1, 0, KK1, I.ps->d_pidx[cc], nc, c->d_ha);
+            launch_expand(ss, c->d_hp, P.P, KK1, 0, KK1, I.ps->d_pidx[cc], nc, nc, c->d_ha);
             ++L;
             split_prep_gemm3(c, c->d_ha, nc, KK1, ss, &L);
         });
@@ -1575,6 +1762,7 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
             if (!c) throw Error(RT_ERR_USER, "null context in batch");
             if (c->device != B->device) throw Error(RT_ERR_USER, "batch contexts on different devices");
             if (!c->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
+            if (c->cfg.breit) throw Error(RT_ERR_USER, "batched transforms are Coulomb only");
             if (c->cfg.precision != RT_PREC_SPLIT_BF16)
                 throw Error(RT_ERR_USER, "batched transforms use precision RT_PREC_SPLIT_BF16");
             for (int j = 0; j < i; ++j)
@@ -1672,7 +1860,7 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
         B->gev.resize(2 * B->all.size());
         for (auto& e : B->gev) RT_CUDA(cudaEventCreate(&e));
         B->stats.instances = count;
-        for (BatchInst& I : B->inst) B->stats.flops_algorithmic += algorithmic_flops(I.c->plan);
+        for (BatchInst& I : B->inst) B->stats.flops_algorithmic += algorithmic_flops(I.c->plan, false);
         for (SplitGroup* g : B->all) B->stats.flops_gemm_executed += split_group_flops(g, true);
     } catch (const Error& e) {
         rt::set_thread_error(e.msg);
@@ -1780,7 +1968,7 @@ extern "C" int rt_batch_run(rt_batch* b) {
                 c->stats.nrec[cc] = w.nrec[cc];
             }
             c->stats.nhalft = (long long)hs[1];
-            c->stats.flops_algorithmic = algorithmic_flops(c->plan);
+            c->stats.flops_algorithmic = algorithmic_flops(c->plan, c->cfg.breit != 0);
             c->transformed = true;
         }
     } catch (const Error& e) {
@@ -1896,7 +2084,7 @@ extern "C" int rt_plan(const rt_config* cfg, rt_plan_info* out) {
     if (cfg->n_irrep == 4) tmp.ao_irrep.assign(cfg->ao_irrep, cfg->ao_irrep + cfg->nsc);
     plan_ao(&tmp);
     const Plan& P = tmp.plan;
-    const int K = P.K, m = P.m, n = P.n;
+    const int K = P.K;
     const long long KK1 = (long long)K * (K + 1);
     out->npairs = P.P;
     out->nitems = KK1;
@@ -1904,7 +2092,7 @@ extern "C" int rt_plan(const rt_config* cfg, rt_plan_info* out) {
     long long a_pp = 0;
     for (long long v : tmp.plan.pg_a_pp) a_pp = std::max(a_pp, v);
     out->expand_bytes_per_pair = a_pp * 8;
-    out->hp_bytes = 2 * KK1 * P.P * 8;
+    out->hp_bytes = 2 * KK1 * P.P * 8 * (cfg->breit ? 3 : 1);
     const bool all = cfg->throut < 0.0;
     for (int i = 1; i <= K; ++i)
         for (int j = 1; j <= i; ++j) {
@@ -1915,14 +2103,7 @@ extern "C" int rt_plan(const rt_config* cfg, rt_plan_info* out) {
                 out->elem_cap[c] += set_size(c, i, j, K, all);
             }
         }
-    double f1 = 0.0;
-    for (auto& gg : P.g1)
-        f1 += 2.0 * P.blk_size[gg.rblk] * (double)P.pgroups[gg.pg].size * P.blk_size[gg.kblk] * 2.0 * m;
-    f1 += (double)P.P * 8.0 * n * (double)m * m;
-    double f2 = 0.0;
-    for (int cc = 0; cc < 2; ++cc) f2 += 8.0 * (double)P.ncomp[cc] * P.ncomp[cc] * m;
-    f2 = (double)KK1 * (f2 + 8.0 * n * (double)m * m);
-    out->flops_algorithmic = f1 + f2;
+    out->flops_algorithmic = algorithmic_flops(P, (double)KK1, cfg->breit != 0);
     return RT_OK;
     }
     catch (const rt::Error& e) {

@@ -68,7 +68,7 @@ struct G1Group {
 };
 
 struct PairGroup {
-    int cls;         // 0 = LL, 1 = SS
+    int cls;         // 0 = LL, 1 = SS, 2 = SL (Gaunt integrals)
     int gamma;       // pair irrep
     int start, size; // range in pair order
 };
@@ -113,7 +113,9 @@ struct Plan {
     int n_cls1 = 0, n_cls234 = 0;
     // expansion tables: per component block c (0 = L, 1 = S) the pair index
     // of (p, q) in component-local sorted positions, -1 if none
+    // (Gaunt: row component c against the other component's columns)
     std::vector<int> pidx[2];
+    int pidx_cols[2] = {0, 0};    // columns of pidx[c]: n_c (Coulomb) or n of the other component
     int ncomp[2] = {0, 0};
     int comp_off[2] = {0, 0};
 };
@@ -262,6 +264,11 @@ struct rt_ctx {
     double* d_qap = nullptr;     // [s_sorted][plane*m + b]     (n x 2m)
     double* d_qah = nullptr;     // [(plane',a)][(plane,r)]     (2m x 2n)
     double* d_qar[2] = {nullptr, nullptr};  // per component: [(plane,q)][(plane',k)] (2nc x 2m)
+    // Gaunt (Breit) transformation: the same operands built from QB (the
+    // beta coefficients, QB(j) = -conj(QA(jbar)), QB(jbar) = conj(QA(j)))
+    double* d_qbh = nullptr;     // like d_qah
+    double* d_qbhS = nullptr;    // like d_qah with the large-component columns zero
+    double* d_qbr[2] = {nullptr, nullptr};  // like d_qar
     // second bucket level: (pq, expansion job) buckets
     long long* d_jstart = nullptr;
     int* d_jcount = nullptr;

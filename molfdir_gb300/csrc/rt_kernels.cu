@@ -118,6 +118,10 @@ __device__ __forceinline__ float mag32(float a, float b) {
 struct F64El {
     typedef double T;
     static __device__ __forceinline__ T comb(T a, T b, double sg) { return a + sg * b; }
+    static __device__ __forceinline__ T neg(T a) { return -a; }
+    static __device__ __forceinline__ double mag(T re, T im) { return hypot(re, im); }
+    // a part of magnitude at most thr is not stored (trbout.F:61-115)
+    static __device__ __forceinline__ T keep(T a, double thr) { return fabs(a) > thr ? a : 0.0; }
     static __device__ __forceinline__ double val(T a) { return a; }
     static __device__ __forceinline__ T zero() { return 0.0; }
     static __device__ __forceinline__ T from(double v) { return v; }
@@ -131,6 +135,11 @@ struct F64El {
 struct FFEl {
     typedef float2 T;
     static __device__ __forceinline__ T comb(T a, T b, double sg) { return ff_add(a, b, (float)sg); }
+    static __device__ __forceinline__ T neg(T a) { return make_float2(-a.x, -a.y); }
+    static __device__ __forceinline__ double mag(T re, T im) { return (double)mag32(re.x, im.x); }
+    static __device__ __forceinline__ T keep(T a, double thr) {
+        return fabsf(a.x) > (float)thr ? a : make_float2(0.f, 0.f);
+    }
     static __device__ __forceinline__ double val(T a) { return ff_to_double(a); }
     static __device__ __forceinline__ T zero() { return make_float2(0.f, 0.f); }
     static __device__ __forceinline__ bool nonzero(T re, T im) { return re.x != 0.f || im.x != 0.f; }
@@ -188,26 +197,102 @@ __global__ void k_tr_select(const typename E::T* __restrict__ ri, int m, int npc
 }
 
 // ---------------------------------------------------------------------------
+// Gaunt (Breit) selection: the three half-transformed streams TRBOUT stores
+// for the Kramers-unique pair (I', J') that UNIQUE (with the Breit sign,
+// unique.F:34) gives for TRANS2's item (I, J), transformed as TRANS2 does
+// (conjugate and swap the QB streams, negate: trans2.F:129-155):
+//   A = HA(J',I'),  B = HB(J',I'),  C = conj(HB(I',J')),
+//   HA(x,y) = RIA(x,y) + s RIA(ybar,xbar)   (MTIMHER with ISG = -1)
+//   HB(x,y) = RI2(x,y) + s RI2(ybar,xbar)   (MTIMHR2), s = -sign(ITRMO(x) ITRMO(y)),
+// RIA = QA^H G QA over the whole pair block, RI2 = QB^H G QA over its
+// small-component rows.  TRBOUT's fixed screen: nothing is kept when
+// |A| + |B| + |HB(I',J')| < 1e-16, and parts of magnitude at most 1e-16 are
+// zero (trbout.F:35-115).  Output: three streams [stream][plane][item][pair].
+// ---------------------------------------------------------------------------
+template <class E>
+__global__ void k_trb_select(const typename E::T* __restrict__ ria, const typename E::T* __restrict__ ri2,
+                             int m, int npc, int pq0, int P, const BreitItem* __restrict__ items, int it0,
+                             int nitems, typename E::T* __restrict__ hp, unsigned long long* __restrict__ kept) {
+    typedef typename E::T T;
+    const int it = it0 + blockIdx.y;
+    const int pql = blockIdx.x * blockDim.x + threadIdx.x;
+    int keep = 0;
+    if (pql < npc && it < nitems) {
+        const BreitItem w = items[it];
+        const double s = w.s;
+        const long long plane = (long long)m * m * npc;
+        auto at = [&](int a, int b) { return ((long long)a * m + b) * npc + pql; };
+        const long long xy = at(w.x, w.y), yx = at(w.y, w.x), ybxb = at(w.yb, w.xb), xbyb = at(w.xb, w.yb);
+        T ar = E::comb(ria[xy], ria[ybxb], s), ai = E::comb(ria[plane + xy], ria[plane + ybxb], s);
+        T br = E::comb(ri2[xy], ri2[ybxb], s), bi = E::comb(ri2[plane + xy], ri2[plane + ybxb], s);
+        T cr = E::comb(ri2[yx], ri2[xbyb], s), ci = E::comb(ri2[plane + yx], ri2[plane + xbyb], s);
+        const double TB = 1.0e-16;
+        if (E::mag(ar, ai) + E::mag(br, bi) + E::mag(cr, ci) < TB) {
+            ar = ai = br = bi = cr = ci = E::zero();
+        } else {
+            keep = 1;
+            ar = E::keep(ar, TB); ai = E::keep(ai, TB);
+            br = E::keep(br, TB); bi = E::keep(bi, TB);
+            cr = E::keep(cr, TB); ci = E::neg(E::keep(ci, TB));  // C = conj(HB(I',J'))
+        }
+        if (w.conj) {  // conjugate all three, swap B and C
+            T tr = cr, ti = ci;
+            ai = E::neg(ai);
+            cr = br; ci = E::neg(bi);
+            br = tr; bi = E::neg(ti);
+        }
+        if (w.neg) {
+            ar = E::neg(ar); ai = E::neg(ai);
+            br = E::neg(br); bi = E::neg(bi);
+            cr = E::neg(cr); ci = E::neg(ci);
+        }
+        const long long o = (long long)it * P + pq0 + pql, st = 2LL * nitems * P, pl = (long long)nitems * P;
+        hp[o] = ar; hp[pl + o] = ai;
+        hp[st + o] = br; hp[st + pl + o] = bi;
+        hp[2 * st + o] = cr; hp[2 * st + pl + o] = ci;
+    }
+    keep = __syncthreads_count(keep);
+    if (threadIdx.x == 0 && keep) atomicAdd(kept, (unsigned long long)keep);
+}
+
+// ---------------------------------------------------------------------------
 // Symmetric expansion of the half-transformed integrals of one component
 // block (the role of MATMUL3's two updates, matmul3.F:25-32):
 //   M3[p][ij][plane][q] = Hp[plane][ij][pair(p,q)]
 // ---------------------------------------------------------------------------
 // The row blocks of one item are adjacent in launch order (blockIdx.x), so
 // the item's half-transformed row stays in L2 while they gather from it.
+// Rows p of one component against columns q of the same component
+// (Coulomb) or of the other one (Gaunt: M(p,q) = M(q,p) = H(pq), p and q in
+// different components); `two` doubles the values (MATMUL7's factor 2,
+// matmul7.F:3-35; exact, also on float-float pairs).
+template <bool FF>
 __global__ void k_expand(const double* __restrict__ hp, int P, int nitems, int it0, int nij,
-                         const int* __restrict__ pidx, int nc, double* __restrict__ m3) {
+                         const int* __restrict__ pidx, int nrow, int ncol, bool two,
+                         double* __restrict__ m3) {
     const int ijl = blockIdx.y;
     const int it = it0 + ijl;
     const double* hr = hp + (long long)it * P;
     const double* hi = hp + (long long)nitems * P + (long long)it * P;
-    for (int p = blockIdx.x; p < nc; p += gridDim.x) {
-        double* row = m3 + ((long long)p * nij + ijl) * (2LL * nc);
-        for (int q = threadIdx.x; q < nc; q += blockDim.x) {
-            int pq = pidx[p * nc + q];
+    for (int p = blockIdx.x; p < nrow; p += gridDim.x) {
+        double* row = m3 + ((long long)p * nij + ijl) * (2LL * ncol);
+        for (int q = threadIdx.x; q < ncol; q += blockDim.x) {
+            int pq = pidx[p * ncol + q];
             double re = 0.0, im = 0.0;
             if (pq >= 0) { re = hr[pq]; im = hi[pq]; }
+            if (two) {
+                if (FF) {
+                    float2 a = *reinterpret_cast<float2*>(&re), b = *reinterpret_cast<float2*>(&im);
+                    a.x *= 2.f; a.y *= 2.f; b.x *= 2.f; b.y *= 2.f;
+                    re = *reinterpret_cast<double*>(&a);
+                    im = *reinterpret_cast<double*>(&b);
+                } else {
+                    re *= 2.0;
+                    im *= 2.0;
+                }
+            }
             row[q] = re;
-            row[nc + q] = im;
+            row[ncol + q] = im;
         }
     }
 }
@@ -239,7 +324,9 @@ __global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ 
                                               const int* __restrict__ kra,
                                               const int* __restrict__ krb,
                                               const int* __restrict__ itrmo, double throut,
-                                              int mode, OutStreams os) {
+                                              int mode, OutStreams os,
+                                              const typename E::T* __restrict__ rlr_b,
+                                              const typename E::T* __restrict__ rlr_c, double msign) {
     __shared__ int wsum[8];
     __shared__ int base;
     const EmitRec R = rec[blockIdx.x];
@@ -269,8 +356,12 @@ __global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ 
                 const double sg = ((itrmo[Ks] > 0) == (itrmo[Ls] > 0)) ? 1.0 : -1.0;
                 const long long a = ((long long)Ks * nij + ijl) * m + Ls;
                 const long long b = ((long long)Lb * nij + ijl) * m + Kb;
-                vr = E::comb(rlr[a], rlr[b], sg);
-                vi = E::comb(rlr[plane + a], rlr[plane + b], sg);
+                vr = E::comb(rlr[a], rlr[b], sg * msign);
+                vi = E::comb(rlr[plane + a], rlr[plane + b], sg * msign);
+                if (rlr_b) {  // Gaunt: + QA^H RK(B) + QB^H RK(C) (trans2.F:166-177)
+                    vr = E::comb(E::comb(vr, rlr_b[a], 1.0), rlr_c[a], 1.0);
+                    vi = E::comb(E::comb(vi, rlr_b[plane + a], 1.0), rlr_c[plane + a], 1.0);
+                }
             }
             emit = E::above(vr, vi, throut);
             if (emit && mode == 1) {  // FP64 values only for the elements written
@@ -352,24 +443,42 @@ void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc
 }
 
 void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
-                   const int* pidx, int nc, double* m3) {
+                   const int* pidx, int nrow, int ncol, double* m3, bool two, bool ff) {
     if (nij > 65535) throw_dim("expansion: more than 65535 items per chunk");
-    dim3 grid(nc < 64 ? nc : 64, nij);
-    k_expand<<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nc, m3);
+    if (nrow <= 0 || ncol <= 0) return;
+    dim3 grid(nrow < 64 ? nrow : 64, nij);
+    if (ff) k_expand<true><<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nrow, ncol, two, m3);
+    else k_expand<false><<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nrow, ncol, two, m3);
+}
+
+void launch_trb_select(cudaStream_t st, bool ff, const double* ria, const double* ri2, int m, int npc,
+                       int pq0, int P, const BreitItem* items, int nitems, double* hp,
+                       unsigned long long* kept) {
+    for (int y0 = 0; y0 < nitems; y0 += 65535) {
+        int ny = nitems - y0 < 65535 ? nitems - y0 : 65535;
+        dim3 grid((npc + 255) / 256, ny);
+        if (ff)
+            k_trb_select<FFEl><<<grid, 256, 0, st>>>((const float2*)ria, (const float2*)ri2, m, npc, pq0, P,
+                                                    items, y0, nitems, (float2*)hp, kept);
+        else
+            k_trb_select<F64El><<<grid, 256, 0, st>>>(ria, ri2, m, npc, pq0, P, items, y0, nitems, hp, kept);
+    }
 }
 
 void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, int K,
                  const EmitRec* rec, int nrec, const int* kra, const int* krb, const int* itrmo,
-                 double throut, const OutStreams& os) {
+                 double throut, const OutStreams& os, const double* rlr_b, const double* rlr_c,
+                 double msign) {
     if (nrec <= 0) return;
     for (int mode = 0; mode < 2; ++mode) {
         if (mode == 1) k_scan_records<<<1, 1024, 0, st>>>(rec, nrec, os);
         if (ff)
             k_emit<FFEl><<<nrec, 256, 0, st>>>((const float2*)rlr, m, nij, K, rec, kra, krb, itrmo,
-                                              throut, mode, os);
+                                              throut, mode, os, (const float2*)rlr_b,
+                                              (const float2*)rlr_c, msign);
         else
             k_emit<F64El><<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, mode,
-                                               os);
+                                               os, rlr_b, rlr_c, msign);
     }
 }
 
@@ -449,7 +558,8 @@ __device__ __forceinline__ int decode_integral(const RecWords& w, int rec, const
                                                const ScatterTabs& tb, unsigned int* status,
                                                int* pqs, int* rss, double& v) {
     const int2 meta = rec_meta[rec];
-    if (meta.x < 1 || meta.x > tb.mfil) return 0;  // SORT1 reads files 1..MFIL only
+    // SORT1 reads files 1..MFIL, or file 4 alone for the Gaunt integrals (sort1.F:55-57)
+    if (tb.breit ? meta.x != 4 : (meta.x < 1 || meta.x > tb.mfil)) return 0;
     const int L2 = w.L2, L1 = w.L1;
     int a = (L2 >> 16) & 0xFFFF, b = L2 & 0xFFFF;
     int c = (L1 >> 16) & 0xFFFF, d = L1 & 0xFFFF;
@@ -463,6 +573,7 @@ __device__ __forceinline__ int decode_integral(const RecWords& w, int rec, const
     if (!tb.pq_read[cdo]) return 0;  // INDPQ(pq) == 0: never transformed
     const int coinc = (pa == pb) + (c == d) + (pa == c && pb == d);
     v = w.v * gettw_factor(meta.y) * (double)(1 << coinc);
+    if (tb.breit) v = -v;  // GETTW turns the sign of file 4 (gettw.F:51-55)
     const int abo = pa * (pa + 1) / 2 + pb;
     int ne = 0;
     for (int dir = 0; dir < 2; ++dir) {

@@ -29,6 +29,7 @@ struct ScatterTabs {
     const int* jb_band;            // [npg*nblk] rows per band of those jobs
     const long long* pg_bbase;     // [npg] first bucket of the pair group
     const int* pg_njobs;           // [npg] expansion jobs per pair
+    int breit = 0;                 // Gaunt integrals: file 4 only, sign turned (gettw.F:51-55)
 };
 
 // One MDCINT record of the current item chunk.
@@ -119,10 +120,24 @@ void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc
                       const double* pair_vmx, const float* pair_thr, double thrgen, double* hp,
                       unsigned long long* kept);
 void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
-                   const int* pidx, int nc, double* m3);
+                   const int* pidx, int nrow, int ncol, double* m3, bool two = false, bool ff = false);
+// One Gaunt item: the stored pair (x, y) = (J', I') of UNIQUE(I, J) (internal
+// 0-based spinors), their partners, s = -sign(ITRMO(x) ITRMO(y)), and
+// TRANS2's conjugation and sign for the item.
+struct BreitItem {
+    int x, y, xb, yb;
+    float s;
+    int conj, neg;
+};
+void launch_trb_select(cudaStream_t st, bool ff, const double* ria, const double* ri2, int m, int npc,
+                       int pq0, int P, const BreitItem* items, int nitems, double* hp,
+                       unsigned long long* kept);
+// rlr_b / rlr_c (Gaunt only, else null) are added to the complete integral;
+// msign multiplies the time-reversal term (MSUMTIM's ISG)
 void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, int K,
                  const EmitRec* rec, int nrec, const int* kra, const int* krb, const int* itrmo,
-                 double throut, const OutStreams& os);
+                 double throut, const OutStreams& os, const double* rlr_b = nullptr,
+                 const double* rlr_c = nullptr, double msign = 1.0);
 
 // ---- adjoint (dE/dC) ----
 // Gamma <- (Gamma + Gamma^T) / 2 with Gamma seen as an m^2 x m^2 complex

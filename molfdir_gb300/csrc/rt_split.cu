@@ -345,6 +345,46 @@ __device__ __forceinline__ TileRef tile_ref(const Tab& tab, long long t) {
     return r;
 }
 
+// The digit products of one staged K block, unrolled for S slices: A slice
+// t times B slice u for t + u < S into accumulator min(t + u, 3) (one exact
+// sum per product diagonal, the rest together).  A tile's first K block
+// overwrites each accumulator with its first product.  Descriptors advance
+// through the stage by adding byte offsets / 16 to the start-address field
+// (stage addresses stay below 2^18, so the 14-bit field does not carry).
+template <int S, bool PAIR>
+__device__ __forceinline__ void issue_digit_products(uint32_t tmem, uint32_t acc_cols, uint64_t da0, uint64_t db0,
+                                                     uint32_t slice_a16, uint32_t slice_b16, uint32_t idesc,
+                                                     bool first) {
+#pragma unroll
+    for (int t = 0; t < S; ++t)
+#pragma unroll
+        for (int u = 0; u + t < S; ++u) {
+            const uint32_t dt = tmem + (uint32_t)(t + u < 3 ? t + u : 3) * acc_cols;
+            const uint64_t da = da0 + (uint64_t)(t * slice_a16), db = db0 + (uint64_t)(u * slice_b16);
+#pragma unroll
+            for (int kk = 0; kk < SBK / 16; ++kk) {
+                const uint32_t accumulate = (first && t == 0 && kk == 0 && u <= 3) ? 0u : 1u;
+                if (PAIR)
+                    umma_bf16_pair(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, accumulate);
+                else
+                    umma_bf16(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, accumulate);
+            }
+        }
+}
+
+template <bool PAIR>
+__device__ __forceinline__ void issue_stage(int s, uint32_t tmem, uint32_t acc_cols, uint64_t da0, uint64_t db0,
+                                            uint32_t slice_a16, uint32_t slice_b16, uint32_t idesc, bool first) {
+    switch (s) {
+        case 1: issue_digit_products<1, PAIR>(tmem, acc_cols, da0, db0, slice_a16, slice_b16, idesc, first); break;
+        case 2: issue_digit_products<2, PAIR>(tmem, acc_cols, da0, db0, slice_a16, slice_b16, idesc, first); break;
+        case 3: issue_digit_products<3, PAIR>(tmem, acc_cols, da0, db0, slice_a16, slice_b16, idesc, first); break;
+        case 4: issue_digit_products<4, PAIR>(tmem, acc_cols, da0, db0, slice_a16, slice_b16, idesc, first); break;
+        case 5: issue_digit_products<5, PAIR>(tmem, acc_cols, da0, db0, slice_a16, slice_b16, idesc, first); break;
+        default: issue_digit_products<6, PAIR>(tmem, acc_cols, da0, db0, slice_a16, slice_b16, idesc, first); break;
+    }
+}
+
 // The GEMM body: BN = output tile width (128 or 64), s slices.
 template <int BN, class Epi, class Tab>
 __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* error,
@@ -420,7 +460,6 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
                     break;
                 }
                 tc_fence_after();
-                bool started[4] = {false, false, false, false};
                 const TileRef r = tile_ref(tab, tile);
                 for (int kb = r.kb0; kb < r.kb1; ++kb, ++gk) {
                     const int st = (int)(gk % NSTAGE);
@@ -433,20 +472,9 @@ __device__ __forceinline__ void split_gemm_body(const Tab& tab, int s, int* erro
                     issued[st] = 0;
                     tc_fence_after();
                     unsigned char* base = smem + (size_t)st * stage_bytes;
-                    for (int t = 0; t < s; ++t)
-                        for (int u = 0; u + t < s; ++u) {
-                            const int acc = t + u < 3 ? t + u : 3;
-                            const uint32_t dt = tmem + (uint32_t)(acc * BN);
-                            const uint64_t da = umma_sdesc(base + t * slice_a, 512, UMMA_SWIZZLE_64B);
-                            const uint64_t db = umma_sdesc(base + (size_t)s * slice_a + u * slice_b, 512,
-                                                           UMMA_SWIZZLE_64B);
-#pragma unroll
-                            for (int kk = 0; kk < SBK / 16; ++kk) {
-                                umma_bf16(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc,
-                                          started[acc] ? 1u : 0u);
-                                started[acc] = true;
-                            }
-                        }
+                    issue_stage<false>(s, tmem, BN, umma_sdesc(base, 512, UMMA_SWIZZLE_64B),
+                                       umma_sdesc(base + (size_t)s * slice_a, 512, UMMA_SWIZZLE_64B),
+                                       slice_a >> 4, slice_b >> 4, idesc, kb == r.kb0);
                     umma_commit(&empty[st]);
                 }
                 if (abort_flag) break;
@@ -649,7 +677,6 @@ __device__ __forceinline__ void split_gemm_pair_body(const Tab& tab, int s, int*
                     break;
                 }
                 tc_fence_after();
-                bool started[4] = {false, false, false, false};
                 for (int kb = r.kb0; kb < r.kb1; ++kb, ++gk) {
                     const int st = (int)(gk % PSTAGE);
                     const uint32_t ph = (uint32_t)((gk / PSTAGE) & 1);
@@ -659,20 +686,9 @@ __device__ __forceinline__ void split_gemm_pair_body(const Tab& tab, int s, int*
                     }
                     tc_fence_after();
                     unsigned char* base = smem + (size_t)st * stage_bytes;
-                    for (int t = 0; t < s; ++t)
-                        for (int u = 0; u + t < s; ++u) {
-                            const int acc = t + u < 3 ? t + u : 3;
-                            const uint32_t dt = tmem + (uint32_t)(acc * PBN);
-                            const uint64_t da = umma_sdesc(base + t * slice_a, 512, UMMA_SWIZZLE_64B);
-                            const uint64_t db = umma_sdesc(base + (size_t)s * slice_a + u * slice_b, 512,
-                                                           UMMA_SWIZZLE_64B);
-#pragma unroll
-                            for (int kk = 0; kk < SBK / 16; ++kk) {
-                                umma_bf16_pair(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc,
-                                               started[acc] ? 1u : 0u);
-                                started[acc] = true;
-                            }
-                        }
+                    issue_stage<true>(s, tmem, PBN, umma_sdesc(base, 512, UMMA_SWIZZLE_64B),
+                                      umma_sdesc(base + (size_t)s * slice_a, 512, UMMA_SWIZZLE_64B),
+                                      slice_a >> 4, slice_b >> 4, idesc, kb == r.kb0);
                     umma_commit_pair(&empty[st], (uint16_t)3);
                 }
                 if (abort_flag) break;
@@ -888,13 +904,17 @@ struct SplitState {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     int num_sms = 152;
     int max_pairs = 0;  // CTA pairs of the pair kernel resident at once
-    bool use_pairs = true;  // RT_GEMM_KERNEL=single selects the single-CTA kernel throughout
+    bool use_pairs = false;  // RT_GEMM_KERNEL=pair selects the CTA-pair kernel for M > 128
     // constant operands
     ConstSlices qah;                 // A of GEMM2/4: rows 2m, K = 2n
     ConstSlices qahB;                // the barred rows of qah (both planes): rows m
     std::vector<ConstSlices> qap;    // B of GEMM1 per AO block: N = 2m, K = block size
     ConstSlices qar[2];              // B of GEMM3 per component: N = 2m, K = 2nc
     ConstSlices qc[2];               // B of the adjoint's X GEMM per component: N = 2m, K = nc
+    // Gaunt (Breit) transformation: the operands built from QB
+    ConstSlices qbh;                 // A of GEMM4 for the third stream: rows 2m, K = 2n
+    ConstSlices qbhS;                // A of the QB^H HA GEMM (large-component columns zero)
+    ConstSlices qbr[2];              // B of GEMM3 for the second stream, per component
     // work buffers
     __nv_bfloat16* a_sl = nullptr;
     int* a_exp = nullptr;
@@ -998,11 +1018,12 @@ static SplitState* state(rt_ctx* c) {
         set_smem_limit(k_split_gemm_pair<EpiFF_RowMajor>, need2, prop);
         set_smem_limit(k_split_gemm_pair<EpiFF_RK>, need2, prop);
         S->max_pairs = pair_capacity((const void*)k_split_gemm_pair<EpiFF_RowMajor>, need2, S->num_sms);
-        // Diagnostic choice between the two implementations of the same
-        // product (identical digit arithmetic and accumulation): the CTA-pair
-        // kernel for M > 128 (default) or the single-CTA kernel for all.
+        // Choice between the two implementations of the same product
+        // (identical digit arithmetic and accumulation): the single-CTA
+        // kernel (default; measured faster on GB300 for these shapes) or,
+        // with RT_GEMM_KERNEL=pair, the CTA-pair kernel for M > 128.
         const char* kv = getenv("RT_GEMM_KERNEL");
-        S->use_pairs = !(kv && std::strcmp(kv, "single") == 0);
+        S->use_pairs = kv && std::strcmp(kv, "pair") == 0;
         const char* tr = getenv("RT_TRACE");
         if (tr && std::strcmp(tr, "0") != 0)
             std::fprintf(stderr, "[rt] split GEMM: %s kernel, %d CTA pairs resident (%d SMs)\n",
@@ -1101,6 +1122,51 @@ void split_prepare_constants(rt_ctx* c) {
             }
         host_slice_cols(bc.data(), nc, 2 * m, 2 * m, kpad(nc), s, sl, ex);
         upload_const(S, S->qc[comp], sl, ex, 2 * m, nc);
+    }
+    if (!c->cfg.breit) return;
+    // QB in sorted AO order from QA (QB(j) = -conj(QA(jbar)) for unbarred j,
+    // QB(jbar) = conj(QA(j)); internal spinor order)
+    std::vector<double> br((size_t)n * m), bi((size_t)n * m);
+    for (int i = 0; i < m; ++i) {
+        const int t = c->itrmo[i], pi = std::abs(t) - 1;
+        const double sg = t > 0 ? -1.0 : 1.0;
+        for (int r = 0; r < n; ++r) {
+            br[(size_t)r * m + i] = sg * qr[(size_t)r * m + pi];
+            bi[(size_t)r * m + i] = -sg * qi[(size_t)r * m + pi];
+        }
+    }
+    {
+        std::vector<double> a((size_t)2 * m * 2 * n), as((size_t)2 * m * 2 * n, 0.0);
+        for (int i = 0; i < m; ++i)
+            for (int r = 0; r < n; ++r) {
+                double re = br[(size_t)r * m + i], im = bi[(size_t)r * m + i];
+                size_t x[4] = {(size_t)i * 2 * n + r, (size_t)i * 2 * n + n + r, (size_t)(m + i) * 2 * n + r,
+                               (size_t)(m + i) * 2 * n + n + r};
+                double v[4] = {re, im, -im, re};
+                for (int t = 0; t < 4; ++t) {
+                    a[x[t]] = v[t];
+                    if (r >= P.nL) as[x[t]] = v[t];  // small-component rows of HA only
+                }
+            }
+        host_slice_rows(a, 2 * m, 2 * n, kpad(2 * n), s, sl, ex);
+        upload_const(S, S->qbh, sl, ex, 2 * m, 2 * n);
+        host_slice_rows(as, 2 * m, 2 * n, kpad(2 * n), s, sl, ex);
+        upload_const(S, S->qbhS, sl, ex, 2 * m, 2 * n);
+    }
+    for (int comp = 0; comp < 2; ++comp) {
+        const int nc = P.ncomp[comp], off = P.comp_off[comp];
+        if (nc == 0) continue;
+        std::vector<double> bm((size_t)2 * nc * 2 * m);
+        for (int q = 0; q < nc; ++q)
+            for (int k = 0; k < m; ++k) {
+                double re = br[(size_t)(off + q) * m + k], im = bi[(size_t)(off + q) * m + k];
+                bm[(size_t)q * 2 * m + k] = re;
+                bm[(size_t)q * 2 * m + m + k] = im;
+                bm[(size_t)(nc + q) * 2 * m + k] = -im;
+                bm[(size_t)(nc + q) * 2 * m + m + k] = re;
+            }
+        host_slice_cols(bm.data(), 2 * nc, 2 * m, 2 * m, kpad(2 * nc), s, sl, ex);
+        upload_const(S, S->qbr[comp], sl, ex, 2 * m, 2 * nc);
     }
 }
 
@@ -1329,6 +1395,45 @@ void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const E
     const ConstSlices& B = S->qar[comp];
     EpiFF_RK epi{(float2*)e.rk, e.m, e.rowoff, e.plane};
     run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * c->plan.m, K, Kp, epi, launches);
+}
+
+// Gaunt stage A: RIA = QA^H HA over all blocks and RI2 = QB^H HA over the
+// small-component rows of HA (trans1.F:81-97), both from one slicing of HA.
+void split_gemm2_breit(rt_ctx* c, const double* Bsrc, int K, long long N, const EpiRowMajor& ria,
+                       const EpiRowMajor& ri2, int* launches) {
+    SplitState* S = state(c);
+    const int Kp = kpad(K);
+    split_prep_gemm24(c, Bsrc, K, N, c->stream, launches);
+    run_gemm(c, S->qah.d, S->qah.exps, S->qah.rows, S->a_sl, S->b_exp, N, K, Kp,
+             EpiFF_RowMajor{(float2*)ria.c, ria.ldc}, launches);
+    run_gemm(c, S->qbhS.d, S->qbhS.exps, S->qbhS.rows, S->a_sl, S->b_exp, N, K, Kp,
+             EpiFF_RowMajor{(float2*)ri2.c, ri2.ldc}, launches);
+}
+
+// GEMM3 of a rectangular expansion: rows (p, ij) of row component `rcomp`
+// (nrow functions), K = 2 ncol over the functions of component kcomp, B =
+// [[Q_r, Q_i], [-Q_i, Q_r]] of QA (op 0) or QB (op 1).
+void split_gemm3_op(rt_ctx* c, int op, int kcomp, const double* m3, int nrow, int ncol, int nij,
+                    const EpiRK& e, int* launches) {
+    SplitState* S = state(c);
+    const int K = 2 * ncol, Kp = kpad(K);
+    const long long M = (long long)nrow * nij;
+    launch_slice_rows(S->s, RowsFF{(const float2*)m3, (long long)K}, M, K, Kp, S->a_sl, S->a_exp, c->stream);
+    ++*launches;
+    const ConstSlices& B = op ? S->qbr[kcomp] : S->qar[kcomp];
+    EpiFF_RK epi{(float2*)e.rk, e.m, e.rowoff, e.plane};
+    run_gemm(c, S->a_sl, S->a_exp, M, B.d, B.exps, 2LL * c->plan.m, K, Kp, epi, launches);
+}
+
+// GEMM4 with A = QA^H (op 0) or QB^H (op 1)
+void split_gemm4_op(rt_ctx* c, int op, const double* Bsrc, int K, long long N, const EpiRowMajor& e,
+                    int* launches) {
+    SplitState* S = state(c);
+    const int Kp = kpad(K);
+    split_prep_gemm24(c, Bsrc, K, N, c->stream, launches);
+    const ConstSlices& A = op ? S->qbh : S->qah;
+    run_gemm(c, A.d, A.exps, A.rows, S->a_sl, S->b_exp, N, K, Kp, EpiFF_RowMajor{(float2*)e.c, e.ldc},
+             launches);
 }
 
 // ---------------------------------------------------------------------------

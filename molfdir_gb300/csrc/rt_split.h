@@ -30,6 +30,13 @@ void split_gemm3(rt_ctx* c, int comp, const double* m3, int nc, int nij, const E
 void split_gemm2_kramers(rt_ctx* c, const double* B, int K, long long N, const EpiRowMajor& epi,
                          int* launches);
 void split_release(rt_ctx* c);
+// Gaunt (Breit) transformation
+void split_gemm2_breit(rt_ctx* c, const double* B, int K, long long N, const EpiRowMajor& ria,
+                       const EpiRowMajor& ri2, int* launches);
+void split_gemm3_op(rt_ctx* c, int op, int kcomp, const double* m3, int nrow, int ncol, int nij,
+                    const EpiRK& e, int* launches);
+void split_gemm4_op(rt_ctx* c, int op, const double* B, int K, long long N, const EpiRowMajor& e,
+                    int* launches);
 // operand slicing of GEMM2/4 and GEMM3 on stream st (the GEMM itself apart)
 void split_prep_gemm24(rt_ctx* c, const double* Bsrc, int K, long long N, cudaStream_t st,
                        int* launches);

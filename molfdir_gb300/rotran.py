@@ -151,9 +151,11 @@ def _p(a, t):
 
 
 def make_config(nsc, nsc1, nkr, mfil=3, thrgen=1e-16, throut=1e-16,
-                precision=RT_PREC_FP64, slices=0, ao_irrep=None, mem_budget=0):
-    cfg = RtConfig(nsc, nsc1, 2 * nkr, nkr, mfil, 0, thrgen, throut, precision, slices,
-                   1, None, mem_budget)
+                precision=RT_PREC_FP64, slices=0, ao_irrep=None, mem_budget=0, breit=False):
+    """``breit``: the Gaunt transform of file 4 into MDBINT (BREIT in rotran's
+    namelist) instead of the Coulomb transform of files 1..MFIL."""
+    cfg = RtConfig(nsc, nsc1, 2 * nkr, nkr, mfil, 1 if breit else 0, thrgen, throut, precision,
+                   slices, 1, None, mem_budget)
     keep = None
     if ao_irrep is not None and int(np.max(ao_irrep)) > 0:
         keep = np.ascontiguousarray(ao_irrep, dtype=np.int32)
@@ -202,6 +204,8 @@ class Rotran:
 
     @classmethod
     def for_problem(cls, problem, **kw):
+        """A context for a synthetic problem; ``breit=True`` transforms its
+        Gaunt file instead of the Coulomb files."""
         cfg, keep = make_config(problem.n, problem.nsc1, problem.nkr, mfil=problem.mfil,
                                 ao_irrep=problem.model.irrep if problem.model.n_irrep > 1 else None,
                                 **kw)

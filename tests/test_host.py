@@ -56,7 +56,9 @@ def test_plan_matches_oracle_counts():
 
 
 @pytest.mark.parametrize("kw,code", [
-    (dict(nsc=10, nsc1=4, nkr=3, mfil=3, breit=1), 2),
+    (dict(nsc=10, nsc1=10, nkr=3, mfil=3, breit=1), 2),
+    (dict(nsc=10, nsc1=0, nkr=3, mfil=3, breit=1), 2),
+    (dict(nsc=10, nsc1=4, nkr=3, mfil=3, breit=2), 2),
     (dict(nsc=10, nsc1=4, nkr=3, mfil=1), 2),
     (dict(nsc=70000, nsc1=4, nkr=3, mfil=3), 3),
     (dict(nsc=10, nsc1=11, nkr=3, mfil=3), 2),
@@ -70,6 +72,19 @@ def test_plan_rejects_bad_config(kw, code):
     with pytest.raises(rotran.RotranError) as e:
         rotran.plan(cfg)
     assert e.value.code == code
+
+
+def test_plan_of_the_gaunt_transform():
+    """BREIT: the SL pair blocks only (makind.F:91-95), MFIL not used, three
+    streams in TRANS2 and the second TRANS1 ZGEMM with QB in the FLOP count."""
+    cfg, _ = rotran.make_config(64, 24, 32, mfil=0, breit=True)
+    pi = rotran.plan(cfg)
+    assert pi.npairs == 24 * 40
+    assert pi.nitems == 32 * 33
+    n, m, k, P = 64, 64, 32, pi.npairs
+    f1 = 2 * 2 * m * (P * 2 * 24 * 40) + 2 * P * 8 * n * m * m
+    f2 = k * (k + 1) * 3 * (2 * 8 * 24 * 40 * m + 8 * n * m * m)
+    assert pi.flops_algorithmic == pytest.approx(f1 + f2)
 
 
 def test_create_without_gpu_fails_loudly():
