@@ -758,6 +758,7 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = fals
         c->d_jrs = dalloc<int>(c, (size_t)2 * c->bucket_cap);
     }
     if (!c->d_hp) c->d_hp = dalloc<double>(c, (size_t)2 * KK1 * P.P * (c->cfg.breit ? 3 : 1));
+    if (c->cfg.breit && !c->d_rl_all) c->d_rl_all = dalloc<double>(c, (size_t)2 * KK1 * m * m);
     for (int cc = 0; cc < 4; ++cc) {
         if (!c->d_oidx[cc]) {
             c->d_oidx[cc] = dalloc<int>(c, (size_t)2 * std::max(1LL, w.cap[cc]));
@@ -930,6 +931,7 @@ struct Pass {
     int *d_kra = nullptr, *d_krb = nullptr, *d_itrmo = nullptr;
     int* d_pidx[2] = {nullptr, nullptr};
     BreitItem* d_bitems = nullptr;  // Gaunt: UNIQUE's stored pair per item
+    int* d_item_of = nullptr;       // Gaunt: item of Kramers (i, j), [J barred][i][j]
     unsigned long long* d_stat = nullptr;
     int pair_chunk = 0, item_chunk = 0;
     int launches = 0;
@@ -978,6 +980,12 @@ void pass_setup(Pass& ps, bool exact = false) {
     if (ctx->cfg.breit) {
         const std::vector<BreitItem> bi = breit_items(ctx);
         ps.d_bitems = ps.upload(bi.data(), bi.size());
+        std::vector<int> item_of((size_t)2 * K * K, -1);
+        for (int t = 0; t < KK1; ++t) {
+            const Item& it = P.items[t];
+            item_of[((size_t)it.cls1 * K + it.ikr - 1) * K + it.jkr - 1] = t;
+        }
+        ps.d_item_of = ps.upload(item_of.data(), item_of.size());
     }
     ps.d_stat = ps.alloc<unsigned long long>(8);
     RT_CUDA(cudaMemsetAsync(ps.d_stat, 0, 8 * sizeof(unsigned long long), ctx->stream));
@@ -1240,6 +1248,12 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
             tr.mark("B: Gaunt GEMM4");
         }
+        if (breit) {  // the records need other items' RL: emitted after all chunks
+            launch_rl_store(st, split, rlr, rlr_b, rlr_c, m, nij, i0, ps.d_itrmo, ctx->d_rl_all);
+            ++ps.launches;
+            tr.mark("B: Gaunt RL store");
+            continue;
+        }
         for (int cc = 0; cc < 2 && !breit; ++cc) {
             const int nc = P.ncomp[cc];
             if (nc == 0) continue;
@@ -1272,16 +1286,26 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             for (int r = w.item_rec0[t]; r < w.item_rec0[t + 1]; ++r)
                 chunk_recs[r - w.item_rec0[i0]].ijl = t - i0;
         RT_CUDA(cudaMemcpyAsync(d_recs, chunk_recs.data(), chunk_recs.size() * sizeof(EmitRec), cudaMemcpyHostToDevice, st));
-        if (breit)  // MSUMTIM with ISG = -1 on stream 1, plus streams 2 and 3
-            launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), ps.d_kra, ps.d_krb,
-                        ps.d_itrmo, ctx->cfg.throut, os, rlr_b, rlr_c, -1.0);
-        else
-            launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), ps.d_kra, ps.d_krb,
-                        ps.d_itrmo, ctx->cfg.throut, os);
+        launch_emit(st, split, rlr, m, nij, K, d_recs, (int)chunk_recs.size(), ps.d_kra, ps.d_krb,
+                    ps.d_itrmo, ctx->cfg.throut, os);
         ps.launches += 3;
         // the host copy of chunk_recs must outlive the async copy
         RT_CUDA(cudaStreamSynchronize(st));
         tr.mark("B: MDCINT selection");
+    }
+    // Gaunt: MDBINT records from the RL of all items (PPSYM's two halves)
+    for (int i0 = 0; breit && i0 < KK1; i0 += item_chunk) {
+        const int nij = std::min(item_chunk, KK1 - i0);
+        chunk_recs.assign(w.recs.begin() + w.item_rec0[i0], w.recs.begin() + w.item_rec0[i0 + nij]);
+        for (int t = i0; t < i0 + nij; ++t)
+            for (int r = w.item_rec0[t]; r < w.item_rec0[t + 1]; ++r)
+                chunk_recs[r - w.item_rec0[i0]].ijl = t - i0;
+        RT_CUDA(cudaMemcpyAsync(d_recs, chunk_recs.data(), chunk_recs.size() * sizeof(EmitRec), cudaMemcpyHostToDevice, st));
+        launch_emit_breit(st, ctx->d_rl_all, m, K, i0, d_recs, (int)chunk_recs.size(), ps.d_item_of, ps.d_kra,
+                          ps.d_krb, ctx->cfg.throut, os);
+        ps.launches += 3;
+        RT_CUDA(cudaStreamSynchronize(st));
+        tr.mark("B: MDBINT records");
     }
     RT_CUDA(cudaGetLastError());
     RT_CUDA(cudaEventRecord(ctx->ev[4], st));

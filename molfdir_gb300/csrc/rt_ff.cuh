@@ -1,3 +1,4 @@
+#pragma once
 // rt_ff.cuh -- float-float (unevaluated sum of two FP32 numbers, about 48
 // significant bits) arithmetic and the exact integer slicing of FP64 and
 // float-float values into pre-scaled 7-bit BF16 digits.
@@ -19,7 +20,6 @@
 constexpr int KMAX_NARROW = 819;
 constexpr int KMAX_EXACT = 1365;
 __host__ __device__ __forceinline__ int slicing_wide(long long K) { return K > KMAX_NARROW ? 1 : 0; }
-#pragma once
 
 #include <cuda_bf16.h>
 #include <stdint.h>

@@ -279,6 +279,7 @@ struct rt_ctx {
     size_t ha_len = 0;  // doubles in d_ha
     double* d_ri = nullptr;
     double* d_hp = nullptr;
+    double* d_rl_all = nullptr;  // Gaunt: RL of every item, [item][K][L] (re, im)
     double* d_m3 = nullptr;
     double* d_rk = nullptr;
     double* d_rlr = nullptr;

@@ -324,9 +324,7 @@ __global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ 
                                               const int* __restrict__ kra,
                                               const int* __restrict__ krb,
                                               const int* __restrict__ itrmo, double throut,
-                                              int mode, OutStreams os,
-                                              const typename E::T* __restrict__ rlr_b,
-                                              const typename E::T* __restrict__ rlr_c, double msign) {
+                                              int mode, OutStreams os) {
     __shared__ int wsum[8];
     __shared__ int base;
     const EmitRec R = rec[blockIdx.x];
@@ -356,12 +354,8 @@ __global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ 
                 const double sg = ((itrmo[Ks] > 0) == (itrmo[Ls] > 0)) ? 1.0 : -1.0;
                 const long long a = ((long long)Ks * nij + ijl) * m + Ls;
                 const long long b = ((long long)Lb * nij + ijl) * m + Kb;
-                vr = E::comb(rlr[a], rlr[b], sg * msign);
-                vi = E::comb(rlr[plane + a], rlr[plane + b], sg * msign);
-                if (rlr_b) {  // Gaunt: + QA^H RK(B) + QB^H RK(C) (trans2.F:166-177)
-                    vr = E::comb(E::comb(vr, rlr_b[a], 1.0), rlr_c[a], 1.0);
-                    vi = E::comb(E::comb(vi, rlr_b[plane + a], 1.0), rlr_c[plane + a], 1.0);
-                }
+                vr = E::comb(rlr[a], rlr[b], sg);
+                vi = E::comb(rlr[plane + a], rlr[plane + b], sg);
             }
             emit = E::above(vr, vi, throut);
             if (emit && mode == 1) {  // FP64 values only for the elements written
@@ -390,6 +384,144 @@ __global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ 
         __syncthreads();
     }
     if (threadIdx.x == 0 && mode == 0) os.cnt[cls][R.rank] = base;
+}
+
+// ---------------------------------------------------------------------------
+// Gaunt (Breit) records.  rotran's TRANS1 buckets each (SL|SL) integral under
+// its LABEL1 pair only, so the value RL_IJ(K,L) that TRANS2 forms for item
+// (I, J) (MSUMTIM with ISG = -1 on stream 1, plus the two MATMUL7 streams:
+// trans2.F:129-177) is half of a Gaunt integral; PPSYM adds the other half,
+// pushed by OUTPP2 from the item whose Kramers indices are the element's
+// (ppsym.F:67-91, outpp2.F:1-139).  Unlike the Coulomb halves, the two Gaunt
+// halves are not related by a symmetry of the item's own result, so all
+// items' RL are kept (rl_all) and each element is assembled as PPSYM does:
+//   OUTPP1's part of the record's item (outpp1.F:1-74: loop 1 at (x, y),
+//   loop 2 at the transposed position for classes 1 and 4), plus
+//   OUTPP2's loop-1 part of item (x, y) when the record lies in that item's
+//   range, plus its loop-2 part (conjugated, classes 1 and 4) of item (y, x).
+// Classes 3 and 4 push CJVEC / CJNVEC images of RL (trans2.F:284-303).
+// ---------------------------------------------------------------------------
+template <class E>
+__global__ void k_rl_store(const typename E::T* __restrict__ rlr, const typename E::T* __restrict__ rlr_b,
+                           const typename E::T* __restrict__ rlr_c, int m, int nij, int it0,
+                           const int* __restrict__ itrmo, double2* __restrict__ rl_all) {
+    const int ijl = blockIdx.y;
+    const long long plane = (long long)m * nij * m;
+    for (int kl = blockIdx.x * blockDim.x + threadIdx.x; kl < m * m; kl += gridDim.x * blockDim.x) {
+        const int k = kl / m, l = kl - k * m;
+        const int kb = abs(itrmo[k]) - 1, lb = abs(itrmo[l]) - 1;
+        const double sg = ((itrmo[k] > 0) == (itrmo[l] > 0)) ? -1.0 : 1.0;  // ISG = -1
+        const long long a = ((long long)k * nij + ijl) * m + l;
+        const long long b = ((long long)lb * nij + ijl) * m + kb;
+        typename E::T vr = E::comb(rlr[a], rlr[b], sg), vi = E::comb(rlr[plane + a], rlr[plane + b], sg);
+        vr = E::comb(E::comb(vr, rlr_b[a], 1.0), rlr_c[a], 1.0);
+        vi = E::comb(E::comb(vi, rlr_b[plane + a], 1.0), rlr_c[plane + a], 1.0);
+        rl_all[((long long)(it0 + ijl) * m + k) * m + l] = make_double2(E::val(vr), E::val(vi));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_emit_breit(const double2* __restrict__ rl_all, int m, int K, int it0,
+                                                    const EmitRec* __restrict__ rec,
+                                                    const int* __restrict__ item_of,
+                                                    const int* __restrict__ kra, const int* __restrict__ krb,
+                                                    double throut, int mode, OutStreams os) {
+    __shared__ int wsum[8];
+    __shared__ int base;
+    const EmitRec R = rec[blockIdx.x];
+    const int c = R.cls + 1, a = R.ikr, b = R.jkr;  // class 1..4, record (a, b), 1-based
+    const double2* own = rl_all + (long long)(it0 + R.ijl) * m * m;
+    // spinor tables of OUTPP1 (krk1, krl1) and OUTPP2 (krk2, krl2) per class
+    const int* krk1 = (c == 3 || c == 4) ? kra : krb;
+    const int* krl1 = (c == 2 || c == 4) ? kra : krb;
+    const int* krk2 = (c == 3 || c == 4) ? kra : krb;
+    const int* krl2 = c == 2 ? kra : krb;
+    const int* pitem = item_of + ((c == 1 || c == 4) ? 1 : 0) * K * K;  // pushing items: J barred for 1, 4
+    const int ks = (c == 3 || c == 4) ? 1 : -1;                            // element label signs
+    const int ls = (c == 2 || c == 4) ? 1 : -1;                            // (rotran.F:306-328)
+    long long dst = 0;
+    if (mode == 1) dst = os.off[R.cls][R.rank];
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int KK = K * K;
+    // the pushed image of an item's RL: RL, conj (CJVEC), -conj (CJNVEC)
+    auto pushed = [&](double2 v) {
+        if (c == 3) return make_double2(v.x, -v.y);
+        if (c == 4) return make_double2(-v.x, v.y);
+        return v;
+    };
+    for (int t0 = 0; t0 < KK; t0 += blockDim.x) {
+        const int pos = t0 + threadIdx.x;
+        bool emit = false;
+        double re = 0.0, im = 0.0;
+        int x = 0, y = 0;
+        if (pos < KK) {
+            x = pos / K + 1;
+            y = pos - (x - 1) * K + 1;
+            const int xmax = c == 4 ? K : a;
+            // OUTPP1 loop 1 at (x, y)
+            if (x <= xmax && y <= ((c <= 3 && x == a) ? b : x)) {
+                const double2 v = own[(long long)(krk1[x - 1] - 1) * m + krl1[y - 1] - 1];
+                re += v.x; im += v.y;
+            }
+            // OUTPP1 loop 2: position (y', x') = (x, y)
+            if ((c == 1 && a != b) || c == 4) {
+                const int xp = y, yp = x;
+                if (xp <= xmax) {
+                    int ym = (c <= 3 && xp == a) ? b : xp;
+                    if (ym == xp) --ym;
+                    if (yp <= ym) {
+                        const double2 v = own[(long long)(krl1[yp - 1] - 1) * m + krk1[xp - 1] - 1];
+                        re += v.x; im += v.y;
+                    }
+                }
+            }
+            // OUTPP2 loop 1 of item (x, y)
+            if (y <= x) {
+                const int kmin = c == 4 ? 1 : x, lmin = (c <= 3 && a == x) ? y : 1;
+                const int t = pitem[(x - 1) * K + (y - 1)];
+                if (t >= 0 && a >= kmin && b >= lmin && b <= a) {
+                    const double2 v =
+                        pushed(rl_all[((long long)t * m + krk2[a - 1] - 1) * m + krl2[b - 1] - 1]);
+                    re += v.x; im += v.y;
+                }
+            }
+            // OUTPP2 loop 2 of item (y, x), conjugated, at position (x, y)
+            if (x < y && (c == 1 || c == 4)) {
+                const int i = y, j = x;
+                const int kmin = c == 4 ? 1 : i, lmin = (c <= 3 && a == i) ? j : 1;
+                const int t = pitem[(i - 1) * K + (j - 1)];
+                if (t >= 0 && a >= kmin && b >= lmin && b <= a - 1) {
+                    const double2 v =
+                        pushed(rl_all[((long long)t * m + krl2[b - 1] - 1) * m + krk2[a - 1] - 1]);
+                    re += v.x; im -= v.y;
+                }
+            }
+            // the positions OUTPP1/OUTPP2 reach are the canonical set, which
+            // also bounds the record's output (all K*K with THROUT < 0)
+            emit = (throut < 0.0 || in_set(R.cls, x, y, a, b)) && hypot(re, im) > throut;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, emit);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        int off = base, tot = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            if (w < warp) off += wsum[w];
+            tot += wsum[w];
+        }
+        off += __popc(bal & ((1u << lane) - 1u));
+        if (emit && mode == 1) {
+            const long long o = dst + off;
+            os.idx[R.cls][2 * o] = x * ks;
+            os.idx[R.cls][2 * o + 1] = y * ls;
+            os.val[R.cls][2 * o] = re;
+            os.val[R.cls][2 * o + 1] = im;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) base += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && mode == 0) os.cnt[R.cls][R.rank] = base;
 }
 
 // Exclusive scan of the element counts of one chunk's records, per class,
@@ -467,18 +599,38 @@ void launch_trb_select(cudaStream_t st, bool ff, const double* ria, const double
 
 void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, int K,
                  const EmitRec* rec, int nrec, const int* kra, const int* krb, const int* itrmo,
-                 double throut, const OutStreams& os, const double* rlr_b, const double* rlr_c,
-                 double msign) {
+                 double throut, const OutStreams& os) {
     if (nrec <= 0) return;
     for (int mode = 0; mode < 2; ++mode) {
         if (mode == 1) k_scan_records<<<1, 1024, 0, st>>>(rec, nrec, os);
         if (ff)
             k_emit<FFEl><<<nrec, 256, 0, st>>>((const float2*)rlr, m, nij, K, rec, kra, krb, itrmo,
-                                              throut, mode, os, (const float2*)rlr_b,
-                                              (const float2*)rlr_c, msign);
+                                              throut, mode, os);
         else
-            k_emit<F64El><<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, mode,
-                                               os, rlr_b, rlr_c, msign);
+            k_emit<F64El><<<nrec, 256, 0, st>>>(rlr, m, nij, K, rec, kra, krb, itrmo, throut, mode, os);
+    }
+}
+
+void launch_rl_store(cudaStream_t st, bool ff, const double* rlr, const double* rlr_b, const double* rlr_c,
+                     int m, int nij, int it0, const int* itrmo, double* rl_all) {
+    if (nij <= 0) return;
+    if (nij > 65535) throw_dim("item chunk too large for the RL store grid");
+    dim3 grid((m * m + 255) / 256, nij);
+    if (ff)
+        k_rl_store<FFEl><<<grid, 256, 0, st>>>((const float2*)rlr, (const float2*)rlr_b, (const float2*)rlr_c, m,
+                                                nij, it0, itrmo, (double2*)rl_all);
+    else
+        k_rl_store<F64El><<<grid, 256, 0, st>>>(rlr, rlr_b, rlr_c, m, nij, it0, itrmo, (double2*)rl_all);
+}
+
+void launch_emit_breit(cudaStream_t st, const double* rl_all, int m, int K, int it0, const EmitRec* rec,
+                       int nrec, const int* item_of, const int* kra, const int* krb, double throut,
+                       const OutStreams& os) {
+    if (nrec <= 0) return;
+    for (int mode = 0; mode < 2; ++mode) {
+        if (mode == 1) k_scan_records<<<1, 1024, 0, st>>>(rec, nrec, os);
+        k_emit_breit<<<nrec, 256, 0, st>>>((const double2*)rl_all, m, K, it0, rec, item_of, kra, krb, throut,
+                                           mode, os);
     }
 }
 
@@ -572,12 +724,15 @@ __device__ __forceinline__ int decode_integral(const RecWords& w, int rec, const
     const int cdo = c * (c + 1) / 2 + d;
     if (!tb.pq_read[cdo]) return 0;  // INDPQ(pq) == 0: never transformed
     const int coinc = (pa == pb) + (c == d) + (pa == c && pb == d);
-    v = w.v * gettw_factor(meta.y) * (double)(1 << coinc);
-    if (tb.breit) v = -v;  // GETTW turns the sign of file 4 (gettw.F:51-55)
+    // Coulomb: the unique integral under both pairs (its complete symmetric
+    // form).  Gaunt: rotran's half, under LABEL1's pair only with GETTW's
+    // factor as it is and its sign turned for file 4 (gettw.F:51-55); the
+    // records add the pair-interchanged half (k_emit_breit).
+    v = tb.breit ? -w.v * gettw_factor(meta.y) : w.v * gettw_factor(meta.y) * (double)(1 << coinc);
     const int abo = pa * (pa + 1) / 2 + pb;
     int ne = 0;
     for (int dir = 0; dir < 2; ++dir) {
-        if (dir == 1 && abo == cdo) break;
+        if (dir == 1 && (abo == cdo || tb.breit)) break;
         const int pq = tb.pair_of_orig[dir == 0 ? cdo : abo];
         const int r = dir == 0 ? pa : c, s = dir == 0 ? pb : d;
         if (pq < 0) { atomicOr(status, ST_BAD_BLOCK); return 0; }

@@ -132,12 +132,19 @@ struct BreitItem {
 void launch_trb_select(cudaStream_t st, bool ff, const double* ria, const double* ri2, int m, int npc,
                        int pq0, int P, const BreitItem* items, int nitems, double* hp,
                        unsigned long long* kept);
-// rlr_b / rlr_c (Gaunt only, else null) are added to the complete integral;
-// msign multiplies the time-reversal term (MSUMTIM's ISG)
 void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, int K,
                  const EmitRec* rec, int nrec, const int* kra, const int* krb, const int* itrmo,
-                 double throut, const OutStreams& os, const double* rlr_b = nullptr,
-                 const double* rlr_c = nullptr, double msign = 1.0);
+                 double throut, const OutStreams& os);
+// Gaunt: RL of the items it0 .. it0+nij-1 (MSUMTIM(-1) of stream 1 plus
+// streams 2 and 3) into rl_all[item][K][L] as FP64 (re, im)
+void launch_rl_store(cudaStream_t st, bool ff, const double* rlr, const double* rlr_b, const double* rlr_c,
+                     int m, int nij, int it0, const int* itrmo, double* rl_all);
+// Gaunt records: each element is OUTPP1's part of the record's own item plus
+// OUTPP2's parts of the items that PPSYM adds into it; item_of[b][i][j] is the
+// item of Kramers pair indices (i, j), J barred (b = 1) or not (b = 0)
+void launch_emit_breit(cudaStream_t st, const double* rl_all, int m, int K, int it0, const EmitRec* rec,
+                       int nrec, const int* item_of, const int* kra, const int* krb, double throut,
+                       const OutStreams& os);
 
 // ---- adjoint (dE/dC) ----
 // Gamma <- (Gamma + Gamma^T) / 2 with Gamma seen as an m^2 x m^2 complex

@@ -5,9 +5,12 @@ rotran with BREIT = .TRUE. reads only the (SL|SL) Gaunt file (class 4, sign
 turned by GETTW), transforms the SL pair blocks with QA and with QB
 (TRANS1's Gaunt branch: MTIMHER(-1), MTIMHR2, TRBOUT's three streams), and
 in TRANS2 contracts the three streams with QA/QB (MATMUL3, MATMUL7 x2,
-MSUMTIM(-1)) before the same OUTPP/PPSYM record stream as MDCINT.  The
-GPU runs the same algebra as batched GEMMs over all pairs and items; its
-record stream must match the oracle's record for record."""
+MSUMTIM(-1)) before the same OUTPP/PPSYM record stream as MDCINT.  Each
+stored element is the sum of two halves that PPSYM adds (the record's own
+item and the item OUTPP2 pushes from); for the Gaunt integrals those halves
+are not images of each other, so the GPU keeps every item's RL and
+assembles the records as PPSYM does.  The record stream must match the
+oracle's record for record."""
 
 import numpy as np
 import pytest
@@ -80,6 +83,6 @@ def test_breit_refused_by_batches_and_the_adjoint():
         with pytest.raises(rotran.RotranError):
             rotran.Batch([rt])
         with pytest.raises(rotran.RotranError):
-            rt.adjoint(np.eye(p.m, dtype=np.complex128))
+            rt.adjoint(np.zeros((p.m,) * 4, dtype=np.complex128))
     finally:
         rt.close()
