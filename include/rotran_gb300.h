@@ -63,6 +63,15 @@ typedef struct rt_config {
     const int* ao_irrep; /* NSC labels 0..n_irrep-1 (NULL when n_irrep == 1) */
     long long mem_budget; /* device bytes the context may use (0: 85% of the free
                              memory plus the work arena the context already holds) */
+    int half_buckets; /* 1: bucket every integral under its LABEL1 pair only, as
+                         rotran's SORT1 does (sort1.F:78-142), so the half-
+                         transformed values, THRGEN's screen and NHALFT are
+                         rotran's, and assemble each record from the two halves
+                         as OUTPP1/OUTPP2/PPSYM do, THROUT on each half; holds
+                         NKR(NKR+1)*NSP^2*16 more bytes (every item's result).
+                         Always on for BREIT.  0 (default): each integral
+                         under both of its pairs, complete sums, no extra
+                         memory; equal to rotran's output at THRGEN <= 1e-16 */
 } rt_config;
 
 typedef struct rt_stats {

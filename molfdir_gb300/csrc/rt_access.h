@@ -5,6 +5,7 @@
 #include "../../include/rotran_gb300.h"
 
 int rt_internal_mfil(rt_ctx* c);
+int rt_internal_breit(rt_ctx* c);
 int rt_internal_nkr(rt_ctx* c);
 int rt_internal_nsc(rt_ctx* c);
 int rt_internal_nsc1(rt_ctx* c);

@@ -104,6 +104,7 @@ void check_config(const rt_config* cfg) {
         throw Error(RT_ERR_USER, "NSP must equal 2*NKR with NKR >= 1");
     if (cfg->nkr > cfg->nsc) throw Error(RT_ERR_USER, "more Kramers pairs than scalar functions");
     if (cfg->breit != 0 && cfg->breit != 1) throw Error(RT_ERR_USER, "BREIT must be 0 or 1");
+    if (cfg->half_buckets != 0 && cfg->half_buckets != 1) throw Error(RT_ERR_USER, "half_buckets must be 0 or 1");
     if (cfg->breit) {
         // the Gaunt transformation (BREIT = .TRUE., MFIL = 0: rotran.F:48-57)
         // reads the SL|SL integrals of file 4; MFIL is not used
@@ -119,9 +120,9 @@ void check_config(const rt_config* cfg) {
     if (cfg->slices != 0 && (cfg->slices < 2 || cfg->slices > 6))
         throw Error(RT_ERR_USER, "slices must be 0 or 2..6");
     if (cfg->n_irrep != 1 && cfg->n_irrep != 4) throw Error(RT_ERR_USER, "n_irrep must be 1 or 4");
-    // bucket entries pack (block, position) in 3 + 10 bits per index
-    if (cfg->nsc1 > 1023 || cfg->nsc - cfg->nsc1 > 1023)
-        throw Error(RT_ERR_DIM, "more than 1023 functions of one component");
+    // bucket entries pack (block, position) in 3 + 12 bits per index
+    if (cfg->nsc1 > 4095 || cfg->nsc - cfg->nsc1 > 4095)
+        throw Error(RT_ERR_DIM, "more than 4095 functions of one component");
     if (cfg->n_irrep == 4) {
         if (!cfg->ao_irrep) throw Error(RT_ERR_USER, "ao_irrep required when n_irrep == 4");
         for (int p = 0; p < cfg->nsc; ++p)
@@ -727,6 +728,10 @@ extern "C" int rt_clear_ao_records(rt_ctx* ctx) {
 // ---------------------------------------------------------------------------
 namespace {
 
+// rotran's half buckets (LABEL1 pair only) and the two-half record assembly:
+// always for the Gaunt transform, on request for the Coulomb one
+bool uses_halves(const rt_ctx* c) { return c->cfg.breit != 0 || c->cfg.half_buckets != 0; }
+
 void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = false) {
     Plan& P = c->plan;
     Work& w = W(c);
@@ -758,7 +763,7 @@ void ensure_fixed(rt_ctx* c, int& pair_chunk, int& item_chunk, bool exact = fals
         c->d_jrs = dalloc<int>(c, (size_t)2 * c->bucket_cap);
     }
     if (!c->d_hp) c->d_hp = dalloc<double>(c, (size_t)2 * KK1 * P.P * (c->cfg.breit ? 3 : 1));
-    if (c->cfg.breit && !c->d_rl_all) c->d_rl_all = dalloc<double>(c, (size_t)2 * KK1 * m * m);
+    if (uses_halves(c) && !c->d_rl_all) c->d_rl_all = dalloc<double>(c, (size_t)2 * KK1 * m * m);
     for (int cc = 0; cc < 4; ++cc) {
         if (!c->d_oidx[cc]) {
             c->d_oidx[cc] = dalloc<int>(c, (size_t)2 * std::max(1LL, w.cap[cc]));
@@ -980,6 +985,8 @@ void pass_setup(Pass& ps, bool exact = false) {
     if (ctx->cfg.breit) {
         const std::vector<BreitItem> bi = breit_items(ctx);
         ps.d_bitems = ps.upload(bi.data(), bi.size());
+    }
+    if (uses_halves(ctx)) {
         std::vector<int> item_of((size_t)2 * K * K, -1);
         for (int t = 0; t < KK1; ++t) {
             const Item& it = P.items[t];
@@ -1004,7 +1011,7 @@ float* pass_pair_thr(Pass& ps, double thrgen) {
 }
 
 // Sort the records into pq buckets (SORT1) and check their labels.
-void pass_bucketing(Pass& ps) {
+void pass_bucketing(Pass& ps, bool halves) {
     rt_ctx* ctx = ps.c;
     Plan& P = ctx->plan;
     cudaStream_t st = ctx->stream;
@@ -1013,6 +1020,7 @@ void pass_bucketing(Pass& ps) {
                    T.pg_size, T.ao_block, T.ao_pos, T.blk_size, T.g1_of, T.g1_kblk,
                    T.jb_base, T.jb_band, T.pg_bbase, T.pg_njobs};
     tb.breit = ctx->cfg.breit;
+    tb.half = halves ? 1 : 0;
     launch_bucket(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, ctx->n_int, ps.d_roff, ps.d_rmeta,
                   (int)ctx->rec_off.size(), tb, P.P, ctx->d_bcount, ctx->d_boff, ctx->d_bval,
                   ctx->d_brs, P.nbuckets, ctx->d_jstart, ctx->d_jcount, ctx->d_jval, ctx->d_jrs,
@@ -1189,7 +1197,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     long long* d_off[4];
     for (int cc = 0; cc < 4; ++cc) d_off[cc] = ps.alloc<long long>(std::max(1LL, w.nrec[cc]));
     // ---- sort the records into pq buckets (SORT1) ----
-    pass_bucketing(ps);
+    pass_bucketing(ps, uses_halves(ctx));
     RT_CUDA(cudaEventRecord(ctx->ev[2], st));
     // ---- stage A: first half-transformation (TRANS1) per pair chunk ----
     pass_stage_a(ps, ctx->cfg.thrgen);
@@ -1198,7 +1206,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     // ---- stage B: second half-transformation (TRANS2) + PPSYM per item chunk ----
     double* m3 = ctx->d_ha;
     int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
-    const bool breit = ctx->cfg.breit != 0;
+    const bool breit = ctx->cfg.breit != 0, halves = uses_halves(ctx);
     const size_t m3_el = breit ? (size_t)P.ncomp[0] * P.ncomp[1] : (size_t)ncmax * ncmax;
     double* rk = m3 + 2 * m3_el * item_chunk;
     double* rlr = rk + (size_t)2 * n * m * item_chunk;
@@ -1248,8 +1256,8 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
             tr.mark("B: Gaunt GEMM4");
         }
-        if (breit) {  // the records need other items' RL: emitted after all chunks
-            launch_rl_store(st, split, rlr, rlr_b, rlr_c, m, nij, i0, ps.d_itrmo, ctx->d_rl_all);
+        if (breit) {  // the records need other items' RL: assembled after all chunks
+            launch_rl_store(st, split, rlr, rlr_b, rlr_c, m, nij, i0, ps.d_itrmo, -1.0, ctx->d_rl_all);
             ++ps.launches;
             tr.mark("B: Gaunt RL store");
             continue;
@@ -1257,7 +1265,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         for (int cc = 0; cc < 2 && !breit; ++cc) {
             const int nc = P.ncomp[cc];
             if (nc == 0) continue;
-            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, nc, m3);
+            launch_expand(st, ctx->d_hp, P.P, KK1, i0, nij, ps.d_pidx[cc], nc, nc, m3, false, split, halves);
             ++ps.launches;
             tr.mark("B: expand M_ij(p,q)");
             EpiRK e3{rk, m, (long long)P.comp_off[cc] * nij, rkplane};
@@ -1280,6 +1288,12 @@ extern "C" int rt_transform(rt_ctx* ctx) {
             gemm_end(2.0 * 2 * m * (double)nij * m * 2 * n);
             tr.mark("B: slice RK + GEMM4");
         }
+        if (halves) {  // rotran's halves: MSUMTIM (ISG = +1) into every item's RL
+            launch_rl_store(st, split, rlr, nullptr, nullptr, m, nij, i0, ps.d_itrmo, 1.0, ctx->d_rl_all);
+            ++ps.launches;
+            tr.mark("B: RL store");
+            continue;
+        }
         // MDCINT selection for the records of this chunk
         chunk_recs.assign(w.recs.begin() + w.item_rec0[i0], w.recs.begin() + w.item_rec0[i0 + nij]);
         for (int t = i0; t < i0 + nij; ++t)
@@ -1293,19 +1307,19 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         RT_CUDA(cudaStreamSynchronize(st));
         tr.mark("B: MDCINT selection");
     }
-    // Gaunt: MDBINT records from the RL of all items (PPSYM's two halves)
-    for (int i0 = 0; breit && i0 < KK1; i0 += item_chunk) {
+    // rotran's halves: the records from the RL of all items (PPSYM)
+    for (int i0 = 0; halves && i0 < KK1; i0 += item_chunk) {
         const int nij = std::min(item_chunk, KK1 - i0);
         chunk_recs.assign(w.recs.begin() + w.item_rec0[i0], w.recs.begin() + w.item_rec0[i0 + nij]);
         for (int t = i0; t < i0 + nij; ++t)
             for (int r = w.item_rec0[t]; r < w.item_rec0[t + 1]; ++r)
                 chunk_recs[r - w.item_rec0[i0]].ijl = t - i0;
         RT_CUDA(cudaMemcpyAsync(d_recs, chunk_recs.data(), chunk_recs.size() * sizeof(EmitRec), cudaMemcpyHostToDevice, st));
-        launch_emit_breit(st, ctx->d_rl_all, m, K, i0, d_recs, (int)chunk_recs.size(), ps.d_item_of, ps.d_kra,
-                          ps.d_krb, ctx->cfg.throut, os);
+        launch_emit_halves(st, ctx->d_rl_all, m, K, i0, d_recs, (int)chunk_recs.size(), ps.d_item_of, ps.d_kra,
+                           ps.d_krb, ctx->cfg.throut, os);
         ps.launches += 3;
         RT_CUDA(cudaStreamSynchronize(st));
-        tr.mark("B: MDBINT records");
+        tr.mark("B: records from both halves");
     }
     RT_CUDA(cudaGetLastError());
     RT_CUDA(cudaEventRecord(ctx->ev[4], st));
@@ -1436,7 +1450,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     auto gemm_begin = [&]() { if (!split) kt.begin(); };
     auto gemm_end = [&](double fl) { if (!split) kt.end(fl, fl); };
     RT_CUDA(cudaEventRecord(ctx->ev[1], st));
-    pass_bucketing(ps);
+    pass_bucketing(ps, false);  // the adjoint differentiates the complete sums
     RT_CUDA(cudaEventRecord(ctx->ev[2], st));
     // recompute the half-transformed integrals, unscreened
     pass_stage_a(ps, 0.0);
@@ -1787,6 +1801,8 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
             if (c->device != B->device) throw Error(RT_ERR_USER, "batch contexts on different devices");
             if (!c->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
             if (c->cfg.breit) throw Error(RT_ERR_USER, "batched transforms are Coulomb only");
+            if (c->cfg.half_buckets)
+                throw Error(RT_ERR_USER, "batched transforms use complete sums (half_buckets = 0)");
             if (c->cfg.precision != RT_PREC_SPLIT_BF16)
                 throw Error(RT_ERR_USER, "batched transforms use precision RT_PREC_SPLIT_BF16");
             for (int j = 0; j < i; ++j)
@@ -2090,6 +2106,7 @@ extern "C" void rt_destroy(rt_ctx* ctx) {
 }
 
 int rt_internal_mfil(rt_ctx* c) { return c->cfg.mfil; }
+int rt_internal_breit(rt_ctx* c) { return c->cfg.breit; }
 int rt_internal_nkr(rt_ctx* c) { return c->cfg.nkr; }
 int rt_internal_nsc(rt_ctx* c) { return c->cfg.nsc; }
 int rt_internal_nsc1(rt_ctx* c) { return c->cfg.nsc1; }

@@ -405,11 +405,13 @@ extern "C" int rt_read_srtpq_files(rt_ctx* ctx, const char* dir, int nranks) {
 // SORT1's file loop (sort1.F:60-147) with GETTW's record reads (gettw.F:15-29).
 extern "C" int rt_read_srt_files(rt_ctx* ctx, const char* dir) {
     if (!ctx || !dir) return RT_ERR_USER;
-    static const char* tw[3] = {"SRTTWLL", "SRTTWSL", "SRTTWSS"};
-    static const char* lb[3] = {"SRTLBLL", "SRTLBSL", "SRTLBSS"};
+    // files 1..MFIL, or the Gaunt file 4 alone (mfdata3.F:15-22, 41-42; sort1.F:55-57)
+    static const char* tw[4] = {"SRTTWLL", "SRTTWSL", "SRTTWSS", "SRTBREI"};
+    static const char* lb[4] = {"SRTLBLL", "SRTLBSL", "SRTLBSS", "SRTBREL"};
+    const bool breit = rt_internal_breit(ctx) != 0;
     const int mfil = rt_internal_mfil(ctx);
     std::vector<char> a, b;
-    for (int fi = 0; fi < mfil; ++fi) {
+    for (int fi = breit ? 3 : 0; fi < (breit ? 4 : mfil); ++fi) {
         std::string pa = std::string(dir) + "/" + tw[fi], pb = std::string(dir) + "/" + lb[fi];
         File fa(fopen(pa.c_str(), "rb")), fb(fopen(pb.c_str(), "rb"));
         if (!fa.f || !fb.f) {

@@ -268,7 +268,7 @@ __global__ void k_trb_select(const typename E::T* __restrict__ ria, const typena
 // matmul7.F:3-35; exact, also on float-float pairs).
 template <bool FF>
 __global__ void k_expand(const double* __restrict__ hp, int P, int nitems, int it0, int nij,
-                         const int* __restrict__ pidx, int nrow, int ncol, bool two,
+                         const int* __restrict__ pidx, int nrow, int ncol, bool two, bool diag2,
                          double* __restrict__ m3) {
     const int ijl = blockIdx.y;
     const int it = it0 + ijl;
@@ -280,15 +280,20 @@ __global__ void k_expand(const double* __restrict__ hp, int P, int nitems, int i
             int pq = pidx[p * ncol + q];
             double re = 0.0, im = 0.0;
             if (pq >= 0) { re = hr[pq]; im = hi[pq]; }
-            if (two) {
+            // x2 (MATMUL7) and x2 on the diagonal of rotran's half buckets
+            // (MATMUL3's two updates of p = q): exact, also on FF halves
+            const int e = (two ? 1 : 0) + (diag2 && p == q ? 1 : 0);
+            if (e) {
                 if (FF) {
+                    const float f = e == 2 ? 4.f : 2.f;
                     float2 a = *reinterpret_cast<float2*>(&re), b = *reinterpret_cast<float2*>(&im);
-                    a.x *= 2.f; a.y *= 2.f; b.x *= 2.f; b.y *= 2.f;
+                    a.x *= f; a.y *= f; b.x *= f; b.y *= f;
                     re = *reinterpret_cast<double*>(&a);
                     im = *reinterpret_cast<double*>(&b);
                 } else {
-                    re *= 2.0;
-                    im *= 2.0;
+                    const double f = e == 2 ? 4.0 : 2.0;
+                    re *= f;
+                    im *= f;
                 }
             }
             row[q] = re;
@@ -387,40 +392,50 @@ __global__ void __launch_bounds__(256) k_emit(const typename E::T* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// Gaunt (Breit) records.  rotran's TRANS1 buckets each (SL|SL) integral under
-// its LABEL1 pair only, so the value RL_IJ(K,L) that TRANS2 forms for item
-// (I, J) (MSUMTIM with ISG = -1 on stream 1, plus the two MATMUL7 streams:
-// trans2.F:129-177) is half of a Gaunt integral; PPSYM adds the other half,
-// pushed by OUTPP2 from the item whose Kramers indices are the element's
-// (ppsym.F:67-91, outpp2.F:1-139).  Unlike the Coulomb halves, the two Gaunt
-// halves are not related by a symmetry of the item's own result, so all
+// Records from rotran's two halves.  rotran's TRANS1 buckets each integral
+// under its LABEL1 pair only (sort1.F:78-142), so the value RL_IJ(K,L) that
+// TRANS2 forms for item (I, J) is half of an integral; PPSYM adds the other
+// half, pushed by OUTPP2 from the item whose Kramers indices are the
+// element's (ppsym.F:67-91, outpp2.F:1-139).  For the Gaunt integrals
+// (MSUMTIM with ISG = -1 plus the two MATMUL7 streams, trans2.F:129-177) the
+// two halves are not related by a symmetry of the item's own result, so all
 // items' RL are kept (rl_all) and each element is assembled as PPSYM does:
 //   OUTPP1's part of the record's item (outpp1.F:1-74: loop 1 at (x, y),
 //   loop 2 at the transposed position for classes 1 and 4), plus
 //   OUTPP2's loop-1 part of item (x, y) when the record lies in that item's
-//   range, plus its loop-2 part (conjugated, classes 1 and 4) of item (y, x).
-// Classes 3 and 4 push CJVEC / CJNVEC images of RL (trans2.F:284-303).
+//   range, plus its loop-2 part (conjugated, classes 1 and 4) of item (y, x);
+// each part is kept only above THROUT, as OUTPP1/OUTPP2 test it (outpp1.F:34,
+// outpp2.F:40), and the sum is tested again as PPSYM does.  Classes 3 and 4
+// push CJVEC / CJNVEC images of RL (trans2.F:284-303).  The Coulomb
+// transform takes this path on request (rotran's exact intermediate).
 // ---------------------------------------------------------------------------
 template <class E>
 __global__ void k_rl_store(const typename E::T* __restrict__ rlr, const typename E::T* __restrict__ rlr_b,
                            const typename E::T* __restrict__ rlr_c, int m, int nij, int it0,
-                           const int* __restrict__ itrmo, double2* __restrict__ rl_all) {
+                           const int* __restrict__ itrmo, double isg, double2* __restrict__ rl_all) {
     const int ijl = blockIdx.y;
     const long long plane = (long long)m * nij * m;
     for (int kl = blockIdx.x * blockDim.x + threadIdx.x; kl < m * m; kl += gridDim.x * blockDim.x) {
         const int k = kl / m, l = kl - k * m;
         const int kb = abs(itrmo[k]) - 1, lb = abs(itrmo[l]) - 1;
-        const double sg = ((itrmo[k] > 0) == (itrmo[l] > 0)) ? -1.0 : 1.0;  // ISG = -1
+        const double sg = ((itrmo[k] > 0) == (itrmo[l] > 0)) ? isg : -isg;
         const long long a = ((long long)k * nij + ijl) * m + l;
         const long long b = ((long long)lb * nij + ijl) * m + kb;
         typename E::T vr = E::comb(rlr[a], rlr[b], sg), vi = E::comb(rlr[plane + a], rlr[plane + b], sg);
-        vr = E::comb(E::comb(vr, rlr_b[a], 1.0), rlr_c[a], 1.0);
-        vi = E::comb(E::comb(vi, rlr_b[plane + a], 1.0), rlr_c[plane + a], 1.0);
+        if (rlr_b) {
+            vr = E::comb(E::comb(vr, rlr_b[a], 1.0), rlr_c[a], 1.0);
+            vi = E::comb(E::comb(vi, rlr_b[plane + a], 1.0), rlr_c[plane + a], 1.0);
+        }
         rl_all[((long long)(it0 + ijl) * m + k) * m + l] = make_double2(E::val(vr), E::val(vi));
     }
 }
 
-__global__ void __launch_bounds__(256) k_emit_breit(const double2* __restrict__ rl_all, int m, int K, int it0,
+// one half of an element, kept when above THROUT
+__device__ __forceinline__ void add_half(double& re, double& im, double2 v, double throut) {
+    if (hypot(v.x, v.y) > throut) { re += v.x; im += v.y; }
+}
+
+__global__ void __launch_bounds__(256) k_emit_halves(const double2* __restrict__ rl_all, int m, int K, int it0,
                                                     const EmitRec* __restrict__ rec,
                                                     const int* __restrict__ item_of,
                                                     const int* __restrict__ kra, const int* __restrict__ krb,
@@ -460,31 +475,25 @@ __global__ void __launch_bounds__(256) k_emit_breit(const double2* __restrict__ 
             y = pos - (x - 1) * K + 1;
             const int xmax = c == 4 ? K : a;
             // OUTPP1 loop 1 at (x, y)
-            if (x <= xmax && y <= ((c <= 3 && x == a) ? b : x)) {
-                const double2 v = own[(long long)(krk1[x - 1] - 1) * m + krl1[y - 1] - 1];
-                re += v.x; im += v.y;
-            }
+            if (x <= xmax && y <= ((c <= 3 && x == a) ? b : x))
+                add_half(re, im, own[(long long)(krk1[x - 1] - 1) * m + krl1[y - 1] - 1], throut);
             // OUTPP1 loop 2: position (y', x') = (x, y)
             if ((c == 1 && a != b) || c == 4) {
                 const int xp = y, yp = x;
                 if (xp <= xmax) {
                     int ym = (c <= 3 && xp == a) ? b : xp;
                     if (ym == xp) --ym;
-                    if (yp <= ym) {
-                        const double2 v = own[(long long)(krl1[yp - 1] - 1) * m + krk1[xp - 1] - 1];
-                        re += v.x; im += v.y;
-                    }
+                    if (yp <= ym)
+                        add_half(re, im, own[(long long)(krl1[yp - 1] - 1) * m + krk1[xp - 1] - 1], throut);
                 }
             }
             // OUTPP2 loop 1 of item (x, y)
             if (y <= x) {
                 const int kmin = c == 4 ? 1 : x, lmin = (c <= 3 && a == x) ? y : 1;
                 const int t = pitem[(x - 1) * K + (y - 1)];
-                if (t >= 0 && a >= kmin && b >= lmin && b <= a) {
-                    const double2 v =
-                        pushed(rl_all[((long long)t * m + krk2[a - 1] - 1) * m + krl2[b - 1] - 1]);
-                    re += v.x; im += v.y;
-                }
+                if (t >= 0 && a >= kmin && b >= lmin && b <= a)
+                    add_half(re, im, pushed(rl_all[((long long)t * m + krk2[a - 1] - 1) * m + krl2[b - 1] - 1]),
+                             throut);
             }
             // OUTPP2 loop 2 of item (y, x), conjugated, at position (x, y)
             if (x < y && (c == 1 || c == 4)) {
@@ -494,7 +503,7 @@ __global__ void __launch_bounds__(256) k_emit_breit(const double2* __restrict__ 
                 if (t >= 0 && a >= kmin && b >= lmin && b <= a - 1) {
                     const double2 v =
                         pushed(rl_all[((long long)t * m + krl2[b - 1] - 1) * m + krk2[a - 1] - 1]);
-                    re += v.x; im -= v.y;
+                    add_half(re, im, make_double2(v.x, -v.y), throut);
                 }
             }
             // the positions OUTPP1/OUTPP2 reach are the canonical set, which
@@ -575,12 +584,12 @@ void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc
 }
 
 void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
-                   const int* pidx, int nrow, int ncol, double* m3, bool two, bool ff) {
+                   const int* pidx, int nrow, int ncol, double* m3, bool two, bool ff, bool diag2) {
     if (nij > 65535) throw_dim("expansion: more than 65535 items per chunk");
     if (nrow <= 0 || ncol <= 0) return;
     dim3 grid(nrow < 64 ? nrow : 64, nij);
-    if (ff) k_expand<true><<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nrow, ncol, two, m3);
-    else k_expand<false><<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nrow, ncol, two, m3);
+    if (ff) k_expand<true><<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nrow, ncol, two, diag2, m3);
+    else k_expand<false><<<grid, 128, 0, st>>>(hp, P, nitems, it0, nij, pidx, nrow, ncol, two, diag2, m3);
 }
 
 void launch_trb_select(cudaStream_t st, bool ff, const double* ria, const double* ri2, int m, int npc,
@@ -612,25 +621,25 @@ void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, in
 }
 
 void launch_rl_store(cudaStream_t st, bool ff, const double* rlr, const double* rlr_b, const double* rlr_c,
-                     int m, int nij, int it0, const int* itrmo, double* rl_all) {
+                     int m, int nij, int it0, const int* itrmo, double isg, double* rl_all) {
     if (nij <= 0) return;
     if (nij > 65535) throw_dim("item chunk too large for the RL store grid");
     dim3 grid((m * m + 255) / 256, nij);
     if (ff)
         k_rl_store<FFEl><<<grid, 256, 0, st>>>((const float2*)rlr, (const float2*)rlr_b, (const float2*)rlr_c, m,
-                                                nij, it0, itrmo, (double2*)rl_all);
+                                                nij, it0, itrmo, isg, (double2*)rl_all);
     else
-        k_rl_store<F64El><<<grid, 256, 0, st>>>(rlr, rlr_b, rlr_c, m, nij, it0, itrmo, (double2*)rl_all);
+        k_rl_store<F64El><<<grid, 256, 0, st>>>(rlr, rlr_b, rlr_c, m, nij, it0, itrmo, isg, (double2*)rl_all);
 }
 
-void launch_emit_breit(cudaStream_t st, const double* rl_all, int m, int K, int it0, const EmitRec* rec,
-                       int nrec, const int* item_of, const int* kra, const int* krb, double throut,
-                       const OutStreams& os) {
+void launch_emit_halves(cudaStream_t st, const double* rl_all, int m, int K, int it0, const EmitRec* rec,
+                        int nrec, const int* item_of, const int* kra, const int* krb, double throut,
+                        const OutStreams& os) {
     if (nrec <= 0) return;
     for (int mode = 0; mode < 2; ++mode) {
         if (mode == 1) k_scan_records<<<1, 1024, 0, st>>>(rec, nrec, os);
-        k_emit_breit<<<nrec, 256, 0, st>>>((const double2*)rl_all, m, K, it0, rec, item_of, kra, krb, throut,
-                                           mode, os);
+        k_emit_halves<<<nrec, 256, 0, st>>>((const double2*)rl_all, m, K, it0, rec, item_of, kra, krb, throut,
+                                            mode, os);
     }
 }
 
@@ -724,15 +733,20 @@ __device__ __forceinline__ int decode_integral(const RecWords& w, int rec, const
     const int cdo = c * (c + 1) / 2 + d;
     if (!tb.pq_read[cdo]) return 0;  // INDPQ(pq) == 0: never transformed
     const int coinc = (pa == pb) + (c == d) + (pa == c && pb == d);
-    // Coulomb: the unique integral under both pairs (its complete symmetric
-    // form).  Gaunt: rotran's half, under LABEL1's pair only with GETTW's
-    // factor as it is and its sign turned for file 4 (gettw.F:51-55); the
-    // records add the pair-interchanged half (k_emit_breit).
-    v = tb.breit ? -w.v * gettw_factor(meta.y) : w.v * gettw_factor(meta.y) * (double)(1 << coinc);
+    // Complete sums: the unique integral under both pairs (its full symmetric
+    // form).  Half buckets: rotran's entry, under LABEL1's pair only with
+    // GETTW's factor as it is; r = s counts twice, as MTIMHER's transposed
+    // orientation counts it (mtimher.F:3-26), which the symmetric storage of
+    // G_pq holds once (p = q is doubled after TROUT's screen, in k_expand,
+    // as MATMUL3's second update does).  The records add the
+    // pair-interchanged half (k_emit_halves).  GETTW turns the sign of the
+    // Gaunt file (gettw.F:51-55).
+    v = w.v * gettw_factor(meta.y) * (tb.half ? (pa == pb ? 2.0 : 1.0) : (double)(1 << coinc));
+    if (tb.breit) v = -v;
     const int abo = pa * (pa + 1) / 2 + pb;
     int ne = 0;
     for (int dir = 0; dir < 2; ++dir) {
-        if (dir == 1 && (abo == cdo || tb.breit)) break;
+        if (dir == 1 && (abo == cdo || tb.half)) break;
         const int pq = tb.pair_of_orig[dir == 0 ? cdo : abo];
         const int r = dir == 0 ? pa : c, s = dir == 0 ? pb : d;
         if (pq < 0) { atomicOr(status, ST_BAD_BLOCK); return 0; }
@@ -742,8 +756,8 @@ __device__ __forceinline__ int decode_integral(const RecWords& w, int rec, const
         if (tb.jb_base[pg * tb.nblk + tb.ao_block[s]] < 0) { atomicOr(status, ST_BAD_BLOCK); return 0; }
         pqs[ne] = pq;
         // (block, position) of r and s, and whether r == s
-        rss[ne] = (int)(((unsigned)tb.ao_block[r] << 29) | ((unsigned)tb.ao_pos[r] << 19) |
-                        ((unsigned)tb.ao_block[s] << 16) | ((unsigned)tb.ao_pos[s] << 6) |
+        rss[ne] = (int)(((unsigned)tb.ao_block[r] << 29) | ((unsigned)tb.ao_pos[r] << 17) |
+                        ((unsigned)tb.ao_block[s] << 14) | ((unsigned)tb.ao_pos[s] << 2) |
                         (r == s ? 1u : 0u));
         ++ne;
     }
@@ -898,8 +912,8 @@ __global__ void __launch_bounds__(256) k_bucket_split(const long long* __restric
         for (int u = 0; u < SPLIT_U; ++u) {
             const bool on = t0 + (long long)u * blockDim.x < n;
             const unsigned rs = rsu[u];
-            const int br = (int)(rs >> 29), pr = (int)((rs >> 19) & 0x3FF);
-            const int bs = (int)((rs >> 16) & 0x7), ps = (int)((rs >> 6) & 0x3FF);
+            const int br = (int)(rs >> 29), pr = (int)((rs >> 17) & 0xFFF);
+            const int bs = (int)((rs >> 14) & 0x7), ps = (int)((rs >> 2) & 0xFFF);
             const int j1 = on ? job_of(jbb, jbd, tb.nblk, nj, br, pr) : -1;
             smem_agg_add(cnt, j1 >= 0 ? j1 : 0, j1 >= 0);
             const int j2 = on && !(rs & 1u) ? job_of(jbb, jbd, tb.nblk, nj, bs, ps) : -1;
@@ -931,8 +945,8 @@ __global__ void __launch_bounds__(256) k_bucket_split(const long long* __restric
             const bool on = t0 + (long long)u * blockDim.x < n;
             const unsigned rs = rsu[u];
             const double v = vu[u];
-            const int br = (int)(rs >> 29), pr = (int)((rs >> 19) & 0x3FF);
-            const int bs = (int)((rs >> 16) & 0x7), ps = (int)((rs >> 6) & 0x3FF);
+            const int br = (int)(rs >> 29), pr = (int)((rs >> 17) & 0xFFF);
+            const int bs = (int)((rs >> 14) & 0x7), ps = (int)((rs >> 2) & 0xFFF);
             const int j1 = on ? job_of(jbb, jbd, tb.nblk, nj, br, pr) : -1;
             const int s1 = smem_agg_add(cur, j1 >= 0 ? j1 : 0, j1 >= 0);
             if (j1 >= 0) {

@@ -30,6 +30,7 @@ struct ScatterTabs {
     const long long* pg_bbase;     // [npg] first bucket of the pair group
     const int* pg_njobs;           // [npg] expansion jobs per pair
     int breit = 0;                 // Gaunt integrals: file 4 only, sign turned (gettw.F:51-55)
+    int half = 0;                  // rotran's half buckets: LABEL1 pair only (sort1.F:78-142)
 };
 
 // One MDCINT record of the current item chunk.
@@ -119,8 +120,12 @@ void launch_tr_select(cudaStream_t st, bool ff, const double* ri, int m, int npc
                       const int4* items, const float* item_sign, int nitems,
                       const double* pair_vmx, const float* pair_thr, double thrgen, double* hp,
                       unsigned long long* kept);
+// M3 rows p (nrow) against columns q (ncol) of the half-transformed values;
+// two: x2 (MATMUL7); ff: float-float values; diag2: x2 on p = q (rotran's
+// half buckets, whose MATMUL3 adds the diagonal pair twice)
 void launch_expand(cudaStream_t st, const double* hp, int P, int nitems, int it0, int nij,
-                   const int* pidx, int nrow, int ncol, double* m3, bool two = false, bool ff = false);
+                   const int* pidx, int nrow, int ncol, double* m3, bool two = false, bool ff = false,
+                   bool diag2 = false);
 // One Gaunt item: the stored pair (x, y) = (J', I') of UNIQUE(I, J) (internal
 // 0-based spinors), their partners, s = -sign(ITRMO(x) ITRMO(y)), and
 // TRANS2's conjugation and sign for the item.
@@ -135,16 +140,17 @@ void launch_trb_select(cudaStream_t st, bool ff, const double* ria, const double
 void launch_emit(cudaStream_t st, bool ff, const double* rlr, int m, int nij, int K,
                  const EmitRec* rec, int nrec, const int* kra, const int* krb, const int* itrmo,
                  double throut, const OutStreams& os);
-// Gaunt: RL of the items it0 .. it0+nij-1 (MSUMTIM(-1) of stream 1 plus
-// streams 2 and 3) into rl_all[item][K][L] as FP64 (re, im)
+// RL of the items it0 .. it0+nij-1 into rl_all[item][K][L] as FP64 (re, im):
+// MSUMTIM with ISG = isg, plus (Gaunt, else null) the streams rlr_b, rlr_c
 void launch_rl_store(cudaStream_t st, bool ff, const double* rlr, const double* rlr_b, const double* rlr_c,
-                     int m, int nij, int it0, const int* itrmo, double* rl_all);
-// Gaunt records: each element is OUTPP1's part of the record's own item plus
-// OUTPP2's parts of the items that PPSYM adds into it; item_of[b][i][j] is the
-// item of Kramers pair indices (i, j), J barred (b = 1) or not (b = 0)
-void launch_emit_breit(cudaStream_t st, const double* rl_all, int m, int K, int it0, const EmitRec* rec,
-                       int nrec, const int* item_of, const int* kra, const int* krb, double throut,
-                       const OutStreams& os);
+                     int m, int nij, int it0, const int* itrmo, double isg, double* rl_all);
+// Records from rotran's two halves: each element is OUTPP1's part of the
+// record's own item plus OUTPP2's part of the item that PPSYM adds into it,
+// each kept when above THROUT; item_of[b][i][j] is the item of Kramers pair
+// indices (i, j), J barred (b = 1) or not (b = 0)
+void launch_emit_halves(cudaStream_t st, const double* rl_all, int m, int K, int it0, const EmitRec* rec,
+                        int nrec, const int* item_of, const int* kra, const int* krb, double throut,
+                        const OutStreams& os);
 
 // ---- adjoint (dE/dC) ----
 // Gamma <- (Gamma + Gamma^T) / 2 with Gamma seen as an m^2 x m^2 complex

@@ -26,7 +26,8 @@ import struct
 
 import numpy as np
 
-SRT_NAMES = {1: ("SRTTWLL", "SRTLBLL"), 2: ("SRTTWSL", "SRTLBSL"), 3: ("SRTTWSS", "SRTLBSS")}
+SRT_NAMES = {1: ("SRTTWLL", "SRTLBLL"), 2: ("SRTTWSL", "SRTLBSL"), 3: ("SRTTWSS", "SRTLBSS"),
+             4: ("SRTBREI", "SRTBREL")}  # reltwel/mfdata3.F:41-42
 
 
 def write_record(f, payload: bytes):
@@ -64,10 +65,12 @@ def read_record(f):
 
 
 def write_srt_files(problem, directory: str):
-    """Write SRTTW*/SRTLB* files of a synthetic problem (files 1..MFIL)."""
+    """Write SRTTW*/SRTLB* files of a synthetic problem (files 1..MFIL), and
+    SRTBREI/SRTBREL when it has Gaunt integrals."""
     os.makedirs(directory, exist_ok=True)
-    keys = {1: "LL", 2: "SL", 3: "SS"}
-    for cls in range(1, problem.mfil + 1):
+    keys = {1: "LL", 2: "SL", 3: "SS", 4: "BR"}
+    classes = list(range(1, problem.mfil + 1)) + ([4] if "BR" in problem.files else [])
+    for cls in classes:
         tw, lb = SRT_NAMES[cls]
         recs = problem.files.get(keys[cls], [])
         with open(os.path.join(directory, tw), "wb") as fa, open(os.path.join(directory, lb), "wb") as fb:

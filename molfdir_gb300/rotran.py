@@ -53,7 +53,7 @@ class RtConfig(C.Structure):
                 ("mfil", C.c_int), ("breit", C.c_int), ("thrgen", C.c_double),
                 ("throut", C.c_double), ("precision", C.c_int), ("slices", C.c_int),
                 ("n_irrep", C.c_int), ("ao_irrep", C.POINTER(C.c_int)),
-                ("mem_budget", C.c_longlong)]
+                ("mem_budget", C.c_longlong), ("half_buckets", C.c_int)]
 
 
 class RtStats(C.Structure):
@@ -151,11 +151,14 @@ def _p(a, t):
 
 
 def make_config(nsc, nsc1, nkr, mfil=3, thrgen=1e-16, throut=1e-16,
-                precision=RT_PREC_FP64, slices=0, ao_irrep=None, mem_budget=0, breit=False):
+                precision=RT_PREC_FP64, slices=0, ao_irrep=None, mem_budget=0, breit=False,
+                half_buckets=False):
     """``breit``: the Gaunt transform of file 4 into MDBINT (BREIT in rotran's
-    namelist) instead of the Coulomb transform of files 1..MFIL."""
+    namelist) instead of the Coulomb transform of files 1..MFIL.
+    ``half_buckets``: rotran's own half-transformed intermediate (each
+    integral under its LABEL1 pair; THRGEN and NHALFT exactly rotran's)."""
     cfg = RtConfig(nsc, nsc1, 2 * nkr, nkr, mfil, 1 if breit else 0, thrgen, throut, precision,
-                   slices, 1, None, mem_budget)
+                   slices, 1, None, mem_budget, 1 if half_buckets else 0)
     keep = None
     if ao_irrep is not None and int(np.max(ao_irrep)) > 0:
         keep = np.ascontiguousarray(ao_irrep, dtype=np.int32)

@@ -6,8 +6,8 @@ issuer's wait for operand tiles runs out, the launch stops all its roles
 (producer, MMA issuer, epilogue; for the CTA-pair kernel in both CTAs),
 drains its MMAs, frees TMEM and returns status 2.  The transform then fails
 with class 6, and the same context transforms correctly afterwards.  The
-case below runs both GEMM kernels: the single-CTA one (GEMM2 and GEMM4, M =
-2m = 40 rows) and the CTA-pair one (GEMM1 and GEMM3, hundreds of rows)."""
+cases below run the default single-CTA kernel; the CTA-pair kernel's abort
+path is run in tests/test_gpu_pair_kernel.py."""
 
 import numpy as np
 import pytest
@@ -37,7 +37,7 @@ def test_gemm_abort_reports_class6_and_context_recovers(monkeypatch):
 
 
 def test_split_dgemm_abort_then_correct(monkeypatch):
-    """The same through rt_split_dgemm on a CTA-pair shape (M = 300)."""
+    """The same through rt_split_dgemm (M = 300, three row tiles)."""
     rng = np.random.default_rng(3)
     a = rng.standard_normal((300, 256))
     b = rng.standard_normal((256, 200))

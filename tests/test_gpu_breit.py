@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 import pyoracle
-from molfdir_gb300 import rotran, synth
+from molfdir_gb300 import fortio, rotran, synth
 from util import compare_streams
 
 pytestmark = pytest.mark.gpu
@@ -86,3 +86,17 @@ def test_breit_refused_by_batches_and_the_adjoint():
             rt.adjoint(np.zeros((p.m,) * 4, dtype=np.complex128))
     finally:
         rt.close()
+
+
+def test_breit_reads_srtbrei_srtbrel(tmp_path):
+    """rt_read_srt_files of a Gaunt context reads SRTBREI/SRTBREL (file 4)
+    alone, as SORT1 does with BREIT; the stream equals the bulk input's."""
+    p = synth.make_problem(5, 7, 4, seed=9, breit=True)
+    fortio.write_srt_files(p, str(tmp_path))
+    with rotran.Rotran.for_problem(p, breit=True) as rt:
+        rt.set_problem_coefficients(p)
+        rt.read_srt_files(str(tmp_path))
+        rt.transform()
+        got = rt.result()
+    bulk, _ = run_gpu(p, rotran.RT_PREC_FP64)
+    assert compare_streams(got, bulk, 0.0) == 0.0

@@ -84,6 +84,31 @@ def test_fp64_thresholds(thrgen, throut):
     assert compare_streams(got, ref, tol, presence_tol=max(tol, 2 * throut)) <= tol
 
 
+FP64, SPLIT = rotran.RT_PREC_FP64, rotran.RT_PREC_SPLIT_BF16
+
+
+# (the split path screens in FP32, so a coarse THRGEN is checked on FP64)
+@pytest.mark.parametrize("thrgen,throut,precision", [
+    (1e-16, 1e-16, FP64), (1e-5, 1e-16, FP64), (1e-3, 1e-16, FP64), (1e-16, 1e-3, FP64), (1e-6, 1e-4, FP64),
+    (1e-16, -1.0, FP64), (1e-16, 1e-16, SPLIT), (1e-16, 1e-3, SPLIT), (1e-16, -1.0, SPLIT)])
+def test_half_buckets_are_rotrans_intermediate(thrgen, throut, precision):
+    """half_buckets = 1: each integral under its LABEL1 pair only (SORT1), so
+    TROUT's THRGEN screen sees rotran's own half-transformed values and the
+    records add OUTPP1's and OUTPP2's halves, each tested against THROUT, as
+    PPSYM does: the same stream as the oracle at any thresholds, and the same
+    NHALFT."""
+    p = synth.make_problem(6, 8, 4, seed=14)
+    img, ref = ref_stream(p, thrgen=thrgen, throut=throut)
+    got, st = run_gpu(p, precision=precision, thrgen=thrgen, throut=throut, half_buckets=True)
+    tol = TOL_FP64 if precision == rotran.RT_PREC_FP64 else 1e-10
+    # the split path's values differ from the oracle's by rounding, so an
+    # element within that of THROUT may be present on one side only
+    assert compare_streams(got, ref, tol, presence_tol=abs(throut) + tol) <= tol
+    if precision == rotran.RT_PREC_FP64:
+        assert st.nhalft == img.nhalft
+        assert list(st.nfinal) == [int(x) for x in img.nfinal]
+
+
 def test_per_record_calls_and_srt_files_match_bulk(tmp_path):
     p = synth.make_problem(6, 8, 4, seed=15)
     bulk, _ = run_gpu(p, bulk=True)

@@ -74,6 +74,18 @@ def test_plan_rejects_bad_config(kw, code):
     assert e.value.code == code
 
 
+def test_plan_reaches_the_reference_basis_limit():
+    """N22 = 3000 scalar functions (vecs.inc:4) plan, with 12-bit positions in
+    the bucket entries; more than 4095 functions of one component do not."""
+    cfg, _ = rotran.make_config(3000, 1500, 8)
+    pi = rotran.plan(cfg)
+    assert pi.npairs == 2 * (1500 * 1501 // 2)
+    cfg, _ = rotran.make_config(5000, 4096, 8)
+    with pytest.raises(rotran.RotranError) as e:
+        rotran.plan(cfg)
+    assert e.value.code == 3
+
+
 def test_plan_of_the_gaunt_transform():
     """BREIT: the SL pair blocks only (makind.F:91-95), MFIL not used, three
     streams in TRANS2 and the second TRANS1 ZGEMM with QB in the FLOP count."""
