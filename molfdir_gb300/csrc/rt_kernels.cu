@@ -2,6 +2,8 @@
 // record scatter, FP64 GEMM, the Kramers selection / transpose between the
 // two half-transformations, the symmetric expansion of the half-transformed
 // integrals, and the MDCINT element selection and compaction.
+#include <map>
+#include <mutex>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -1068,6 +1070,18 @@ void launch_bucket(cudaStream_t st, const double* rint, const int* l2, const int
         k_bucket_split<<<(unsigned)P, 256, 0, st>>>(off, bval, brs, tb, jstart, jcount, jval, jrs);
 }
 
+void raise_dyn_smem(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> set;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;  // the launch reports the error
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& cur = set[{kernel, dev}];
+    if (bytes <= cur) return;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
+        cur = bytes;
+}
+
 void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const int* brs,
                         const long long* jstart, const int* jcount, const ExpandJob* jobs, int njobs,
                         long long bbase, int npc, size_t smem, double* out_f64,
@@ -1075,8 +1089,7 @@ void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const 
     dim3 grid(njobs, npc);
 #define RT_EXPAND(NSV)                                                                          \
     do {                                                                                        \
-        cudaFuncSetAttribute(k_expand_rows<NSV>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
-                             (int)smem);                                                        \
+        raise_dyn_smem((const void*)k_expand_rows<NSV>, smem);                                  \
         k_expand_rows<NSV><<<grid, 256, smem, st>>>(bval, brs, jstart, jcount, jobs, bbase, npc, \
                                                     out_f64, out_sl, out_exp);                  \
     } while (0)

@@ -112,6 +112,11 @@ void launch_bucket(cudaStream_t st, const double* rint, const int* l2, const int
                    int P, int* count, long long* off, double* bval, int* brs, long long nb,
                    long long* jstart, int* jcount, double* jval, int* jrs, unsigned int* status);
 // expansion of one pair chunk: bucket of (pair pql, job j) = bbase + pql * njobs + j
+// Raise a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device; never lowered, so kernels recorded earlier with larger
+// sizes (CUDA graph nodes of a batch) stay launchable whatever the order of
+// later launches.
+void raise_dyn_smem(const void* kernel, size_t bytes);
 void launch_expand_rows(cudaStream_t st, int nslices, const double* bval, const int* brs,
                         const long long* jstart, const int* jcount, const ExpandJob* jobs, int njobs,
                         long long bbase, int npc, size_t smem, double* out_f64,
