@@ -233,6 +233,59 @@ def run_gemm_case(args, rank):
                           "seconds_per_call_with_host_work": dt}))
 
 
+def run_breit_case(args, rank):
+    """The Gaunt transform (BREIT, (SL|SL) integrals to MDBINT) at n = 200
+    (80 L + 120 S AOs), 60 Kramers pairs, seed 0: 4.6e7 Gaunt integrals
+    (host-generated), the split path timed over the steps after the warm-ups
+    and one FP64 transform as the accuracy and speed reference."""
+    import torch
+    from molfdir_gb300 import rotran, synth
+    if rank != 0:
+        return
+    prob = synth.make_problem(80, 120, 60, seed=0, breit=True, mfil=1)
+    recs = prob.flat_records()
+    keep = recs[0] == 4
+    off = np.concatenate([[0], np.cumsum(recs[2])])
+    sel = np.concatenate([np.arange(off[r], off[r + 1]) for r in np.nonzero(keep)[0]])
+    cls, its, nts = recs[0][keep], recs[1][keep], recs[2][keep]
+    v, l2, l1 = recs[3][sel], recs[4][sel], recs[5][sel]
+    out = {"workload": "breit_n200_k60", "n": prob.n, "n_large": prob.nsc1, "nkr": prob.nkr,
+           "integrals": int(v.size), "steps": args.steps, "warmup": args.warmup}
+    legs = {}
+    for name, prec, steps, warm in (("split", rotran.RT_PREC_SPLIT_BF16, args.steps, args.warmup),
+                                    ("fp64", rotran.RT_PREC_FP64, 1, 0)):
+        with rotran.Rotran.for_problem(prob, precision=prec, breit=True) as rt:
+            rt.set_problem_coefficients(prob)
+            rt.add_records_bulk(cls, nts, its, v, l2, l1)
+            for _ in range(warm):
+                rt.transform()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ms = []
+            for _ in range(max(1, steps)):
+                rt.transform()
+                ms.append(rt.stats().ms_total)
+            sec = max((time.perf_counter() - t0) / max(1, steps), statistics.mean(ms) / 1e3)
+            st = rt.stats()
+            legs[name] = {"sec": sec, "flops": st.flops_algorithmic, "result": rt.result(),
+                          "ms_gemm": st.ms_gemm, "nfinal": list(st.nfinal)}
+    sh, si, sv = legs["split"]["result"]
+    fh, fi, fv = legs["fp64"]["result"]
+    same = np.array_equal(sh, fh) and np.array_equal(si, fi)
+    out.update({
+        "value": legs["split"]["flops"] / legs["split"]["sec"] / 1e12, "unit": "TFLOP/s",
+        "ms_per_step": legs["split"]["sec"] * 1e3, "ms_gemm": legs["split"]["ms_gemm"],
+        "flops_algorithmic": legs["split"]["flops"],
+        "fp64": {"value": legs["fp64"]["flops"] / legs["fp64"]["sec"] / 1e12,
+                 "ms_per_step": legs["fp64"]["sec"] * 1e3,
+                 "split_speedup": legs["fp64"]["sec"] / legs["split"]["sec"]},
+        "split_vs_fp64": {"same_elements": bool(same),
+                          "max_abs_err": float(np.abs(sv - fv).max()) if same and sv.size else None,
+                          "max_abs_value": float(np.abs(fv).max()) if fv.size else 0.0},
+        "mdbint": {"records": int(fh.shape[0]), "elements": int(fv.size), "nfinal": legs["fp64"]["nfinal"]}})
+    print(json.dumps(out))
+
+
 def run_files_case(args, rank):
     """Integral input from files at n = 160 (64 L + 96 S AOs), 40 Kramers
     pairs, 2.27e7 integrals: the serial SRTTW/SRTLB files (SORT1's input)
@@ -423,7 +476,8 @@ def main():
     ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "c1", "profile", "profile2", "large", "batched", "gemm", "files"])
+                    choices=["precision", "c1", "profile", "profile2", "large", "batched", "gemm", "files",
+                             "breit"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
@@ -439,6 +493,8 @@ def main():
         return run_gemm_case(args, rank)
     if args.workload == "files":
         return run_files_case(args, rank)
+    if args.workload == "breit":
+        return run_breit_case(args, rank)
     work = {"precision": WORKLOAD, "c1": SMALL, "profile": PROFILE, "profile2": PROFILE2,
             "large": LARGE}[args.workload]
 

@@ -190,7 +190,10 @@ int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double* energy);
  * stage over all contexts.  rt_batch_run runs the transforms; its first call
  * times every grouped GEMM with 128- and 64-wide output tiles, keeps the
  * faster, and captures the whole sequence as a CUDA graph that later calls
- * replay.  The results are then read per context with rt_result_sizes /
+ * replay.  With RT_TUNE_CACHE naming a file in the environment, the choices
+ * are stored there under each stage's shape class (a flat JSON object), and
+ * a batch whose stages are all in the file skips the timing runs
+ * (ms_tune = 0).  The results are then read per context with rt_result_sizes /
  * rt_copy_result / rt_write_mdcint.  All contexts: same device, precision
  * RT_PREC_SPLIT_BF16, coefficients and records set before rt_batch_create
  * and left unchanged while the batch lives (RT_ERR_MISMATCH otherwise).
@@ -204,7 +207,7 @@ typedef struct rt_batch_stats {
     int graph_nodes;       /* nodes of the captured graph */
     int tile128, tile64;   /* grouped launches tuned to 128- / 64-wide tiles */
     double ms_last;        /* device time of the last run (graph launch) */
-    double ms_tune;        /* device time of the two tuning runs */
+    double ms_tune;        /* device time of the two tuning runs (0: from the cache) */
     double flops_algorithmic;   /* summed algorithmic FLOPs of the transforms */
     double flops_gemm_executed; /* tensor FLOPs of the grouped GEMMs per run */
 } rt_batch_stats;

@@ -1913,6 +1913,54 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
     return RT_OK;
 }
 
+namespace {
+
+// Tile-width cache of the batch tuner: a flat JSON object {"shape": width}
+// in the file named by RT_TUNE_CACHE (shape from split_group_shape).
+std::vector<std::pair<std::string, int>> tune_cache_read(const char* path) {
+    std::vector<std::pair<std::string, int>> out;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return out;
+    std::string t;
+    char buf[4096];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0 && t.size() < (1u << 20)) t.append(buf, n);
+    std::fclose(f);
+    size_t i = 0;
+    while ((i = t.find('"', i)) != std::string::npos) {
+        const size_t j = t.find('"', i + 1);
+        if (j == std::string::npos) break;
+        const std::string key = t.substr(i + 1, j - i - 1);
+        size_t k = j + 1;
+        while (k < t.size() && (t[k] == ' ' || t[k] == ':' || t[k] == '\n' || t[k] == '\t')) ++k;
+        const int v = std::atoi(t.c_str() + k);
+        if (v == 64 || v == 128) out.push_back({key, v});
+        i = j + 1;
+    }
+    return out;
+}
+
+void tune_cache_write(const char* path, const std::vector<std::pair<std::string, int>>& add) {
+    std::vector<std::pair<std::string, int>> all = tune_cache_read(path);
+    for (const auto& kv : add) {
+        bool found = false;
+        for (auto& e : all)
+            if (e.first == kv.first) { e.second = kv.second; found = true; }
+        if (!found) all.push_back(kv);
+    }
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return;  // the cache is an optimisation: an unwritable path only costs the tuning
+    std::fprintf(f, "{\n");
+    for (size_t i = 0; i < all.size(); ++i)
+        std::fprintf(f, "  \"%s\": %d%s\n", all[i].first.c_str(), all[i].second, i + 1 < all.size() ? "," : "");
+    std::fprintf(f, "}\n");
+    std::fclose(f);
+    std::rename(tmp.c_str(), path);
+}
+
+}  // namespace
+
 extern "C" int rt_batch_run(rt_batch* b) {
     if (!b) return RT_ERR_USER;
     try {
@@ -1921,10 +1969,32 @@ extern "C" int rt_batch_run(rt_batch* b) {
             if (I.c->gen != I.gen)
                 throw Error(RT_ERR_MISMATCH, "a context of the batch changed after rt_batch_create");
         }
-        if (!b->tuned) {
+        // tile widths from the cache when every stage's shape is in it
+        const char* cache = std::getenv("RT_TUNE_CACHE");
+        bool cached = false;
+        if (!b->tuned && cache && *cache) {
+            const auto entries = tune_cache_read(cache);
+            cached = true;
+            std::vector<int> bn(b->all.size(), 128);
+            for (size_t i = 0; i < b->all.size() && cached; ++i) {
+                if (split_group_size(b->all[i]) == 0) continue;
+                const std::string key = split_group_shape(b->all[i]);
+                bool hit = false;
+                for (const auto& e : entries)
+                    if (e.first == key) { bn[i] = e.second; hit = true; }
+                cached = hit;
+            }
+            if (cached) {
+                b->stats.tile128 = b->stats.tile64 = 0;
+                for (size_t i = 0; i < b->all.size(); ++i) {
+                    b->bn[i] = bn[i];
+                    if (split_group_size(b->all[i]) > 0) ++(bn[i] == 64 ? b->stats.tile64 : b->stats.tile128);
+                }
+                b->stats.ms_tune = 0.0;  // no tuning runs
+            }
+        }
+        if (!b->tuned && !cached) {
             // tile width per grouped stage: time every stage at 128 and at 64
-            const double t0 = 0.0;
-            (void)t0;
             std::vector<float> ms[2];
             cudaEvent_t a, z;
             RT_CUDA(cudaEventCreate(&a));
@@ -1952,6 +2022,14 @@ extern "C" int rt_batch_run(rt_batch* b) {
                 ++(b->bn[i] == 64 ? b->stats.tile64 : b->stats.tile128);
             }
             b->stats.ms_tune = tune_ms;
+            if (cache && *cache) {
+                std::vector<std::pair<std::string, int>> add;
+                for (size_t i = 0; i < b->all.size(); ++i)
+                    if (split_group_size(b->all[i]) > 0) add.push_back({split_group_shape(b->all[i]), b->bn[i]});
+                tune_cache_write(cache, add);
+            }
+        }
+        if (!b->tuned) {
             // capture the tuned sequence once
             RT_CUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
             try {

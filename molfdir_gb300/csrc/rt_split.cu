@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -1612,6 +1613,14 @@ void split_group_launch(SplitGroup* G, int bn, cudaStream_t st, int* err) {
 }
 
 int split_group_size(const SplitGroup* G) { return (int)G->probs.size(); }
+
+std::string split_group_shape(const SplitGroup* g) {
+    char buf[160];
+    std::snprintf(buf, sizeof(buf), "kind%d:s%d:p%zu:t%lld:t%lld:f%d", g->kind, g->s, g->probs.size(),
+                  g->ntiles[0], g->ntiles[1],
+                  g->flops_exec > 0 ? (int)std::lround(std::log2(g->flops_exec)) : 0);
+    return buf;
+}
 double split_group_flops(const SplitGroup* G, bool executed) {
     return executed ? G->flops_exec : G->flops_alg;
 }

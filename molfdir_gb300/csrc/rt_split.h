@@ -1,6 +1,7 @@
 // rt_split.h -- split-precision (BF16 slices on the tensor cores) variants
 // of the four GEMMs of the transformation.
 #pragma once
+#include <string>
 
 #include "rt_internal.h"
 #include "rt_kernels.h"
@@ -53,6 +54,9 @@ void split_group_add_gemm2_kramers(SplitGroup* g, rt_ctx* c, int K, long long N,
 void split_group_build(SplitGroup* g, rt_ctx* c0);
 void split_group_launch(SplitGroup* g, int bn, cudaStream_t st, int* err);
 int split_group_size(const SplitGroup* g);
+// shape class of a group for the tile-width cache: kind, slices, problems,
+// tiles at both widths, executed FLOPs rounded to a power of two
+std::string split_group_shape(const SplitGroup* g);
 double split_group_flops(const SplitGroup* g, bool executed);
 void split_group_free(SplitGroup* g);
 // adjoint: X GEMM of one component and the split-K contraction

@@ -83,3 +83,31 @@ def test_batch_needs_split_precision():
     with pytest.raises(rotran.RotranError):
         rotran.Batch([rt])
     rt.close()
+
+
+def test_tile_width_cache(tmp_path, monkeypatch):
+    """RT_TUNE_CACHE: the first batch times both tile widths per grouped stage
+    and writes its choices under each stage's shape class; a later batch of
+    the same shapes takes them from the file without tuning runs (ms_tune 0)
+    and gives the same results."""
+    path = tmp_path / "tune.json"
+    monkeypatch.setenv("RT_TUNE_CACHE", str(path))
+    probs = problems()
+    outs = []
+    for attempt in range(2):
+        rts = [make_ctx(p) for p in probs]
+        with rotran.Batch(rts) as b:
+            b.run()
+            st = b.stats()
+            outs.append([rt.result() for rt in rts])
+        for rt in rts:
+            rt.close()
+        if attempt == 0:
+            assert st.ms_tune > 0.0
+            text = path.read_text()
+            assert text.count(":") >= 2 * (st.tile64 + st.tile128)
+        else:
+            assert st.ms_tune == 0.0
+    for a, b_ in zip(*outs):
+        for x, y in zip(a, b_):
+            assert np.array_equal(x, y)
