@@ -2129,15 +2129,20 @@ extern "C" int rt_copy_result(rt_ctx* ctx, int* hdr, int* idx, double* val) {
     API_TRY
     if (!ctx->transformed) throw Error(RT_ERR_USER, "no transform result");
     Work& w = W(ctx);
-    long long r0 = 0, z0 = 0;
-    std::vector<int> cnt;
+    // every class stream's copies first, one synchronisation
+    std::vector<int> cnt[4];
+    long long z0 = 0;
     for (int c = 0; c < 4; ++c) {
         const long long nr = ctx->out_nrec[c], nz = ctx->out_nz[c];
-        cnt.resize(std::max(1LL, nr));
-        if (nr) RT_CUDA(cudaMemcpyAsync(cnt.data(), ctx->d_hdr[c], nr * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        cnt[c].resize(std::max(1LL, nr));
+        if (nr) RT_CUDA(cudaMemcpyAsync(cnt[c].data(), ctx->d_hdr[c], nr * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         if (nz && idx) RT_CUDA(cudaMemcpyAsync(idx + 2 * z0, ctx->d_oidx[c], 2 * nz * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         if (nz && val) RT_CUDA(cudaMemcpyAsync(val + 2 * z0, ctx->d_oval[c], 2 * nz * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        RT_CUDA(cudaStreamSynchronize(ctx->stream));
+        z0 += nz;
+    }
+    RT_CUDA(cudaStreamSynchronize(ctx->stream));
+    long long r0 = 0;
+    for (int c = 0; c < 4; ++c) {
         if (hdr) {
             long long k = 0;
             for (const EmitRec& r : w.recs) {
@@ -2145,12 +2150,11 @@ extern "C" int rt_copy_result(rt_ctx* ctx, int* hdr, int* idx, double* val) {
                 int is = -1, js = (c == 0) ? -1 : 1;   // rotran.F:306-328
                 hdr[3 * (r0 + k)] = r.ikr * is;
                 hdr[3 * (r0 + k) + 1] = r.jkr * js;
-                hdr[3 * (r0 + k) + 2] = cnt[k];
+                hdr[3 * (r0 + k) + 2] = cnt[c][k];
                 ++k;
             }
         }
-        r0 += nr;
-        z0 += nz;
+        r0 += ctx->out_nrec[c];
     }
     API_CATCH
 }
