@@ -51,6 +51,19 @@ def test_noalloc_matches_allocating_entry_point_twice():
         results.append((dc, got))
     # the first output is untouched by the second call
     assert np.array_equal(results[0][0].cpu().numpy(), results[0][1])
+    # repeated calls take no device memory: the free memory the driver
+    # reports is the same right before and right after each call
+    for (m, n, k, s, seed) in [(300, 257, 800, 6, 1), (77, 513, 1000, 5, 2)] * 2:
+        a, b = operands(m, n, k, seed)
+        da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        dc = torch.empty((m, n), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        before = torch.cuda.mem_get_info()[0]
+        rotran.split_dgemm_noalloc(m, n, k, da.data_ptr(), db.data_ptr(), dc.data_ptr(),
+                                   slices=s, stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == before
+        del da, db, dc
 
 
 def test_noalloc_rejects_sizes_beyond_scratch():
