@@ -482,6 +482,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="leave out the 48-instance batched leg of the default line")
+    ap.add_argument("--half-buckets", action="store_true",
+                    help="rotran's own half-transformed intermediate (rt_config.half_buckets = 1)")
     ap.add_argument("--per-class", action="store_true",
                     help="also split vs FP64 per AO integral class (3 + 3 extra transforms)")
     args = ap.parse_args()
@@ -542,7 +544,7 @@ def main():
     assert nint == config["integrals"], "generator and workload count disagree"
 
     def make_ctx(p, slices):
-        rt = rotran.Rotran.for_problem(prob, precision=p, slices=slices)
+        rt = rotran.Rotran.for_problem(prob, precision=p, slices=slices, half_buckets=args.half_buckets)
         rt.set_problem_coefficients(prob)
         return rt
 
@@ -745,7 +747,8 @@ def main():
             "vs_baseline": None, "dtype": "bf16-slices/f32-acc (split)" if prec_name == "split" else "f64",
             "data": "synthetic",
             "config": config,
-            "precision": {"path": prec_name, "slices": args.slices if prec_name == "split" else None},
+            "precision": {"path": prec_name, "slices": args.slices if prec_name == "split" else None,
+                          "half_buckets": bool(args.half_buckets)},
             "tflops_dense_equivalent": config["flops_dense_equivalent"] * world / main["sec"] / 1e12,
             "oracle_check": ocheck,
             "batched": batched,

@@ -109,6 +109,25 @@ def test_half_buckets_are_rotrans_intermediate(thrgen, throut, precision):
         assert list(st.nfinal) == [int(x) for x in img.nfinal]
 
 
+@pytest.mark.parametrize("precision", [FP64, SPLIT], ids=["fp64", "split"])
+def test_half_buckets_irrep_blocks_and_shuffled_spinors(precision):
+    """rotran's intermediate over the 4-irrep AO block structure and with the
+    spinors in a shuffled order, at a coarse THRGEN (FP64) and the default
+    (split)."""
+    thrgen = 1e-5 if precision == FP64 else 1e-16
+    tol = TOL_FP64 if precision == FP64 else 1e-10
+    p = synth.make_problem(10, 14, 5, seed=13, n_irrep=4)
+    img, ref = ref_stream(p, thrgen=thrgen)
+    got, st = run_gpu(p, precision=precision, thrgen=thrgen, half_buckets=True)
+    assert compare_streams(got, ref, tol) <= tol
+    q = permute_spinors(synth.make_problem(6, 10, 5, seed=12), np.random.default_rng(1).permutation(10))
+    img_q, ref_q = ref_stream(q, thrgen=thrgen)
+    got_q, st_q = run_gpu(q, precision=precision, thrgen=thrgen, half_buckets=True)
+    assert compare_streams(got_q, ref_q, tol) <= tol
+    if precision == FP64:
+        assert st.nhalft == img.nhalft and st_q.nhalft == img_q.nhalft
+
+
 def test_per_record_calls_and_srt_files_match_bulk(tmp_path):
     p = synth.make_problem(6, 8, 4, seed=15)
     bulk, _ = run_gpu(p, bulk=True)
