@@ -226,6 +226,17 @@ int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz);
  * (ppsym.F:89-91), idx[2*nz] = (INDK, INDL), val[2*nz] = (re, im). */
 int rt_copy_result(rt_ctx* ctx, int* hdr, int* idx, double* val);
 
+/* Stream the elements of the following rt_transform calls into caller-owned
+ * host buffers, one per record class c = 0..3 (MDCINT classes 1..4):
+ * idx[c] holds 2*cap[c] ints, val[c] 2*cap[c] doubles, in the order
+ * rt_copy_result gives that class's elements.  Each item chunk's elements
+ * are copied as soon as the chunk is done, overlapping the remaining work
+ * (pinned buffers copy asynchronously); rt_transform returns with all of
+ * them in place, and rt_copy_result(ctx, hdr, NULL, NULL) then gives the
+ * headers.  A class with more elements than cap[c] fails the transform with
+ * class 3.  NULL idx or val unregisters. */
+int rt_set_result_host(rt_ctx* ctx, int* const* idx, double* const* val, const long long* cap);
+
 /* Write MDCINT (inittwoe.F:1-25, ppsym.F:89-91, exittwoe.F:1-10) as
  * a gfortran sequential unformatted file. */
 int rt_write_mdcint(rt_ctx* ctx, const char* path, const char* datex10, const char* timex8);

@@ -1191,7 +1191,10 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     const bool split = ps.split;
     auto gemm_begin = [&]() { if (!split) kt.begin(); };
     auto gemm_end = [&](double fl) { if (!split) kt.end(fl, fl); };
-    const int item_chunk = ps.item_chunk;
+    // with result buffers on the host, stage B runs in at least four item
+    // chunks so that each chunk's copy overlaps the following chunks' work
+    const bool to_host = ctx->host_on;
+    const int item_chunk = to_host ? std::min(ps.item_chunk, std::max(1, (KK1 + 3) / 4)) : ps.item_chunk;
     long long* d_total = ps.alloc<long long>(4);
     RT_CUDA(cudaMemsetAsync(d_total, 0, 4 * sizeof(long long), st));
     long long* d_off[4];
@@ -1222,6 +1225,30 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     }
     os.total = d_total;
     std::vector<EmitRec> chunk_recs;
+    // the elements of finished chunks to the caller's host buffers, on a copy
+    // stream, while the next chunks run (the host has synchronised st)
+    long long streamed[4] = {0, 0, 0, 0};
+    if (to_host && !ctx->cstream[0]) RT_CUDA(cudaStreamCreateWithFlags(&ctx->cstream[0], cudaStreamNonBlocking));
+    auto stream_out = [&]() {
+        if (!to_host) return;
+        long long tot[4];
+        RT_CUDA(cudaMemcpy(tot, d_total, sizeof(tot), cudaMemcpyDeviceToHost));
+        for (int c = 0; c < 4; ++c)
+            if (tot[c] > ctx->host_cap[c]) {
+                cudaStreamSynchronize(ctx->cstream[0]);   // no copy left in flight
+                throw Error(RT_ERR_DIM, "rt_set_result_host: class " + std::to_string(c + 1) + " needs " +
+                                            std::to_string(tot[c]) + " elements");
+            }
+        for (int c = 0; c < 4; ++c) {
+            const long long a = streamed[c], nz = tot[c] - a;
+            if (nz <= 0) continue;
+            RT_CUDA(cudaMemcpyAsync(ctx->host_idx[c] + 2 * a, ctx->d_oidx[c] + 2 * a, 2 * nz * sizeof(int),
+                                    cudaMemcpyDeviceToHost, ctx->cstream[0]));
+            RT_CUDA(cudaMemcpyAsync(ctx->host_val[c] + 2 * a, ctx->d_oval[c] + 2 * a, 2 * nz * sizeof(double),
+                                    cudaMemcpyDeviceToHost, ctx->cstream[0]));
+            streamed[c] = tot[c];
+        }
+    };
     for (int i0 = 0; i0 < KK1; i0 += item_chunk) {
         const int nij = std::min(item_chunk, KK1 - i0);
         const long long rkplane = (long long)n * nij * m;
@@ -1306,6 +1333,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         // the host copy of chunk_recs must outlive the async copy
         RT_CUDA(cudaStreamSynchronize(st));
         tr.mark("B: MDCINT selection");
+        stream_out();
     }
     // rotran's halves: the records from the RL of all items (PPSYM)
     for (int i0 = 0; halves && i0 < KK1; i0 += item_chunk) {
@@ -1320,6 +1348,11 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         ps.launches += 3;
         RT_CUDA(cudaStreamSynchronize(st));
         tr.mark("B: records from both halves");
+        stream_out();
+    }
+    if (to_host) {
+        RT_CUDA(cudaStreamSynchronize(ctx->cstream[0]));
+        tr.mark("B: last result copies");
     }
     RT_CUDA(cudaGetLastError());
     RT_CUDA(cudaEventRecord(ctx->ev[4], st));
@@ -2121,6 +2154,23 @@ extern "C" int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz) {
     for (int c = 0; c < 4; ++c) { a += ctx->out_nrec[c]; b += ctx->out_nz[c]; }
     if (nrec) *nrec = a;
     if (nz) *nz = b;
+    API_CATCH
+}
+
+extern "C" int rt_set_result_host(rt_ctx* ctx, int* const* idx, double* const* val, const long long* cap) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    ctx->host_on = false;
+    const bool on = idx && val;
+    for (int c = 0; on && c < 4; ++c)
+        if (!cap || cap[c] < 0 || (cap[c] > 0 && (!idx[c] || !val[c])))
+            throw Error(RT_ERR_USER, "rt_set_result_host: each class needs buffers for a capacity >= 0");
+    for (int c = 0; c < 4; ++c) {
+        ctx->host_idx[c] = on ? idx[c] : nullptr;
+        ctx->host_val[c] = on ? val[c] : nullptr;
+        ctx->host_cap[c] = on ? cap[c] : 0;
+    }
+    ctx->host_on = on;
     API_CATCH
 }
 

@@ -295,6 +295,12 @@ struct rt_ctx {
     int* d_oidx[4] = {};
     double* d_oval[4] = {};
     long long out_nrec[4] = {}, out_nz[4] = {}, out_cap[4] = {};
+    // caller's host buffers the next transform streams each class into
+    // (rt_set_result_host): elements copied as their item chunk completes
+    bool host_on = false;
+    int* host_idx[4] = {};
+    double* host_val[4] = {};
+    long long host_cap[4] = {};
     unsigned long long* d_stat = nullptr;
     rt_stats stats{};
     size_t dev_bytes = 0, dev_peak = 0;

@@ -86,7 +86,7 @@ EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm",
            "rt_split_dgemm_noalloc", "rt_adjoint", "rt_batch_create", "rt_batch_run",
            "rt_batch_get_stats", "rt_batch_last_error", "rt_batch_destroy", "rt_srtpq_scan",
-           "rt_read_srtpq_files"]
+           "rt_read_srtpq_files", "rt_set_result_host"]
 
 _lib = None
 
@@ -138,6 +138,7 @@ def load(build: bool = True):
                                   P(C.c_longlong), P(C.c_longlong), P(C.c_int), P(C.c_int),
                                   P(C.c_longlong), P(C.c_double), P(C.c_int), P(C.c_int)]
     lib.rt_read_srtpq_files.argtypes = [vp, C.c_char_p, C.c_int]
+    lib.rt_set_result_host.argtypes = [vp, P(P(C.c_int)), P(P(C.c_double)), P(C.c_longlong)]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy", "rt_batch_last_error", "rt_batch_destroy"):
@@ -322,6 +323,38 @@ class Rotran:
         self._check(self.lib.rt_copy_result(self.h, _p(hdr, C.c_int), _p(idx, C.c_int),
                                             val.ctypes.data_as(C.POINTER(C.c_double))))
         return hdr, idx, val
+
+    def headers(self):
+        """The MDCINT record headers (nrec, 3) alone (``rt_copy_result`` with no element buffers)."""
+        nr, _ = self.result_sizes()
+        hdr = np.empty((nr, 3), np.int32)
+        self._check(self.lib.rt_copy_result(self.h, _p(hdr, C.c_int), None, None))
+        return hdr
+
+    def set_result_host(self, idx=None, val=None):
+        """Stream the following transforms' elements into host arrays (``rt_set_result_host``).
+
+        ``idx[c]``: int32 array of shape (cap_c, 2), ``val[c]``: complex128 array of
+        shape (cap_c,) for record class c = 0..3, C-contiguous; pinned memory (for
+        instance numpy views of pinned torch tensors) lets the copies overlap the
+        transform.  Class c's elements land in ``idx[c][:n_c]``, ``val[c][:n_c]``
+        with n_c = ``stats().nfinal[c]``.  No arguments unregisters.  The arrays
+        must stay alive while registered."""
+        if idx is None or val is None:
+            self._host = None
+            self._check(self.lib.rt_set_result_host(self.h, None, None, None))
+            return
+        assert len(idx) == 4 and len(val) == 4
+        caps = []
+        for a, v in zip(idx, val):
+            assert a.dtype == np.int32 and a.ndim == 2 and a.shape[1] == 2 and a.flags.c_contiguous
+            assert v.dtype == np.complex128 and v.ndim == 1 and v.flags.c_contiguous
+            caps.append(min(a.shape[0], v.shape[0]))
+        ip = (C.POINTER(C.c_int) * 4)(*[_p(a, C.c_int) for a in idx])
+        dp = (C.POINTER(C.c_double) * 4)(*[v.ctypes.data_as(C.POINTER(C.c_double)) for v in val])
+        cp = (C.c_longlong * 4)(*caps)
+        self._host = (list(idx), list(val))
+        self._check(self.lib.rt_set_result_host(self.h, ip, dp, cp))
 
     def write_mdcint(self, path, datex="", timex=""):
         self._check(self.lib.rt_write_mdcint(self.h, os.fsencode(path), datex.encode()[:10],
