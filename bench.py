@@ -288,6 +288,86 @@ def run_breit_case(args, rank):
     print(json.dumps(out))
 
 
+def run_fock_case(args, rank, hbm_peak, peak_kind):
+    """tmoone's skeleton Fock build (MFDFOCK/FOCK, rt_fock_skeleton) over the
+    precision-study workload's 8.7e8 resident integral records (n = 400,
+    14 GB, larger than L2): closed shell (one density set) and closed plus
+    open shell (two), kernel time by CUDA events over the steps after the
+    warm-ups.  Checks: GPU vs the oracle on the first records (about 3e7
+    integrals, 1e-12 of max|F|), linearity F(D1 + D2) = F(D1) + F(D2) at full
+    size, and the two-set call equal to two one-set calls.  The CPU baseline
+    is the oracle (one thread, as FOCK runs) on the same sample."""
+    import torch
+    from molfdir_gb300 import rotran, synth
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    if rank != 0:
+        return
+    work = WORKLOAD
+    prob = synth.make_spinor_problem(work["n_l"], work["n_s"], work["nkr"], seed=work["seed"])
+    cls, its, nts, dv, dl2, dl1 = synth.device_records(prob, 3, device="cuda")
+    torch.cuda.synchronize()
+    nint = int(nts.sum())
+    n = prob.n
+    ntri = n * (n + 1) // 2
+    g = torch.Generator(device="cuda").manual_seed(0)
+    d1 = torch.randn((1, 4, ntri), device="cuda", dtype=torch.float64, generator=g)
+    d2 = torch.randn((1, 4, ntri), device="cuda", dtype=torch.float64, generator=g)
+    out = {"workload": "fock_skeleton_n400", "n": n, "integrals": nint, "records": int(cls.size),
+           "steps": args.steps, "warmup": args.warmup}
+    with rotran.Rotran.for_problem(prob) as rt:
+        rt.add_records_bulk_device(cls, nts, its, dv, dl2, dl1)
+        legs = {}
+        for name, dens in (("closed", d1), ("closed_open", torch.cat([d1, d2]))):
+            for _ in range(args.warmup):
+                rt.fock_skeleton(dens)
+            ms = []
+            t0 = time.perf_counter()
+            for _ in range(max(1, args.steps)):
+                f, k = rt.fock_skeleton(dens)
+                ms.append(k)
+            wall = (time.perf_counter() - t0) / max(1, args.steps)
+            legs[name] = {"ms_kernel": statistics.mean(ms), "ms_call": wall * 1e3, "fock": f}
+        f1 = legs["closed"]["fock"]
+        f2, _ = rt.fock_skeleton(d2)
+        f12, _ = rt.fock_skeleton(d1 + d2)
+        scale = float(f12.abs().max())
+        lin = float((f12 - f1 - f2).abs().max()) / scale
+        pair = legs["closed_open"]["fock"]
+        two = float(max((pair[0] - f1[0]).abs().max(), (pair[1] - f2[0]).abs().max())) / scale
+    # the first records on the host: oracle vs GPU
+    nts_h = np.asarray(nts)
+    cum = np.cumsum(nts_h)
+    nr = int(np.searchsorted(cum, 30_000_000)) + 1
+    ns = int(cum[nr - 1])
+    sample = (np.asarray(cls)[:nr], np.asarray(its)[:nr], nts_h[:nr], dv[:ns].cpu().numpy(),
+              dl2[:ns].cpu().numpy(), dl1[:ns].cpu().numpy())
+    dh = d1.cpu().numpy()
+    t0 = time.perf_counter()
+    want = pyoracle.fock_skeleton(sample, n, dh, mfil=3)
+    cpu_sec = time.perf_counter() - t0
+    with rotran.Rotran.for_problem(prob) as rt:
+        rt.add_records_bulk(*(sample[0], sample[2], sample[1], sample[3], sample[4], sample[5]))
+        got, _ = rt.fock_skeleton(dh)
+    err = float(np.abs(got - want).max() / max(1.0, np.abs(want).max()))
+    ms = legs["closed"]["ms_kernel"]
+    achieved = 16.0 * nint / (ms / 1e3) / 1e9
+    out.update({
+        "metric": "skeleton Fock integrals/s", "value": nint / (ms / 1e3), "unit": "integrals/s",
+        "ms_kernel": ms, "ms_call": legs["closed"]["ms_call"],
+        "closed_open": {"ms_kernel": legs["closed_open"]["ms_kernel"],
+                        "value": nint / (legs["closed_open"]["ms_kernel"] / 1e3)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "bytes_per_integral": 16,
+                     "peak_source": f"hbm_gbs of {peak_kind}"},
+        "checks": {"oracle_sample_integrals": ns, "oracle_max_rel_err": err,
+                   "linearity_rel_err": lin, "two_sets_vs_one_rel_err": two},
+        "cpu_baseline": {"value": ns / cpu_sec, "unit": "integrals/s", "cores": 1, "kind": "port",
+                         "sample": f"first {nr} records ({ns} integrals), one density set"},
+    })
+    print(json.dumps(out))
+
+
 def run_files_case(args, rank):
     """Integral input from files at n = 160 (64 L + 96 S AOs), 40 Kramers
     pairs, 2.27e7 integrals: the serial SRTTW/SRTLB files (SORT1's input)
@@ -479,7 +559,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", default="precision",
                     choices=["precision", "c1", "profile", "profile2", "large", "batched", "gemm", "files",
-                             "breit"])
+                             "breit", "fock"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
@@ -499,6 +579,8 @@ def main():
         return run_files_case(args, rank)
     if args.workload == "breit":
         return run_breit_case(args, rank)
+    if args.workload == "fock":
+        return run_fock_case(args, rank, hbm_peak, peak_kind)
     work = {"precision": WORKLOAD, "c1": SMALL, "profile": PROFILE, "profile2": PROFILE2,
             "large": LARGE}[args.workload]
 

@@ -183,6 +183,23 @@ int rt_transform(rt_ctx* ctx);
  * density (16 NSP^4 bytes) plus the arrays of rt_transform. */
 int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double* energy);
 
+/* tmoone's skeleton Fock matrices (MFDFOCK, source/tmoone/mfdfock.F:53-140,
+ * with FOCK, source/tmoone/fock.F:1-656) from the context's integral
+ * records of files 1..MFIL, on the GPU.  dens holds nmat (1: closed shell,
+ * COMMON /DMT/; 2: closed then open shell, /DMT/ and /DOMT/) sets of four
+ * lower-triangle arrays DAAR, DBAR, DAAI, DBAI of NSC(NSC+1)/2 elements each,
+ * element (x,y), x >= y, at x(x-1)/2 + y - 1 (densfock.inc:4-5; the
+ * reference's arrays are dimensioned N21 and use this leading part); fock
+ * receives FAAR, FBAR, FAAI, FBAI (/FMT/, /FOMT/) in the same layout,
+ * overwritten.  Host or device pointers.  The records are the ones rotran
+ * transforms (rt_add_ao_records*, rt_read_srt_files; LABEL2 gives I, J and
+ * LABEL1 K, L as in mfdfock.F:103-114); coefficients are not needed.  The
+ * additions run in a different order than the reference's (FP64 atomics),
+ * so the sums agree to rounding.  *ms_kernel (may be NULL) receives the
+ * kernel's device milliseconds.  A label outside 1..NSC or a type outside
+ * 1..14 fails with RT_ERR_USER. */
+int rt_fock_skeleton(rt_ctx* ctx, int nmat, const double* dens, double* fock, double* ms_kernel);
+
 /* Batched transforms (no counterpart in the reference, which runs one
  * transformation per process).  rt_batch_create plans every context as a
  * single chunk (all pair groups and Kramers items resident at once; fails

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "librotran_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["rt_api.cu", "rt_kernels.cu", "rt_split.cu", "rt_io.cpp"]
+SOURCES = ["rt_api.cu", "rt_kernels.cu", "rt_split.cu", "rt_fock.cu", "rt_io.cpp"]
 
 
 def nvcc() -> str:

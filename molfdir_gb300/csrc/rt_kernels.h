@@ -174,4 +174,16 @@ void launch_gamma_hat_t(cudaStream_t st, const double* gamma, int m, const int4*
 void launch_partial_sum(cudaStream_t st, bool ff, const double* part, int nb, long long len,
                         double* acc);
 
+// ---- tmoone's skeleton Fock build (rt_fock.cu) ----
+struct FockRec {       // a chunk of one integral record of files 1..MFIL
+    long long off, nt; // first integral in the resident arrays, count
+    int it, pad;       // integral type 1..14
+};
+// fock[s][x][T] += terms of every integral of recs (nmat density sets of
+// four arrays AAR, BAR, AAI, BAI of nsc(nsc+1)/2 elements); fock must be
+// zeroed first.  A label outside 1..nsc sets *bad and the integral is skipped.
+void launch_fock_skeleton(cudaStream_t st, const double* rint, const int* l2, const int* l1,
+                          const FockRec* recs, int nrec, int nsc, int nmat, const double* dens,
+                          double* fock, unsigned long long* bad);
+
 }  // namespace rt

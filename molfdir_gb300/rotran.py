@@ -86,7 +86,7 @@ EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm",
            "rt_split_dgemm_noalloc", "rt_adjoint", "rt_batch_create", "rt_batch_run",
            "rt_batch_get_stats", "rt_batch_last_error", "rt_batch_destroy", "rt_srtpq_scan",
-           "rt_read_srtpq_files", "rt_set_result_host"]
+           "rt_read_srtpq_files", "rt_set_result_host", "rt_fock_skeleton"]
 
 _lib = None
 
@@ -139,6 +139,7 @@ def load(build: bool = True):
                                   P(C.c_longlong), P(C.c_double), P(C.c_int), P(C.c_int)]
     lib.rt_read_srtpq_files.argtypes = [vp, C.c_char_p, C.c_int]
     lib.rt_set_result_host.argtypes = [vp, P(P(C.c_int)), P(P(C.c_double)), P(C.c_longlong)]
+    lib.rt_fock_skeleton.argtypes = [vp, C.c_int, vp, vp, P(C.c_double)]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy", "rt_batch_last_error", "rt_batch_destroy"):
@@ -323,6 +324,22 @@ class Rotran:
         self._check(self.lib.rt_copy_result(self.h, _p(hdr, C.c_int), _p(idx, C.c_int),
                                             val.ctypes.data_as(C.POINTER(C.c_double))))
         return hdr, idx, val
+
+    def fock_skeleton(self, dens, out=None):
+        """tmoone's skeleton Fock sets from the context's records (``rt_fock_skeleton``).
+
+        ``dens``: float64 array (nmat, 4, NSC(NSC+1)/2), sets of DAAR, DBAR, DAAI,
+        DBAI (numpy, or a torch tensor on the host or the device).  Returns the
+        Fock sets in the same shape and kind (``out`` if given) and the kernel's
+        device milliseconds."""
+        nmat = dens.shape[0]
+        if out is None:
+            out = dens.new_empty(dens.shape) if hasattr(dens, "data_ptr") else np.empty_like(dens)
+        pd = dens.data_ptr() if hasattr(dens, "data_ptr") else dens.ctypes.data
+        pf = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+        ms = C.c_double()
+        self._check(self.lib.rt_fock_skeleton(self.h, nmat, C.c_void_p(pd), C.c_void_p(pf), C.byref(ms)))
+        return out, ms.value
 
     def headers(self):
         """The MDCINT record headers (nrec, 3) alone (``rt_copy_result`` with no element buffers)."""

@@ -2,7 +2,8 @@
 
 Imported by the tests, by the smoke check and by bench.py's CPU-baseline
 leg; never by the product package.  ``build()`` compiles
-``oracle/rotran_oracle.c`` into ``oracle/_build/liborotran.so``.
+``oracle/rotran_oracle.c`` (rotran) and ``oracle/tmoone_fock_oracle.c``
+(tmoone's skeleton Fock build) into ``oracle/_build/liborotran.so``.
 """
 
 from __future__ import annotations
@@ -19,11 +20,12 @@ LIB = os.path.join(HERE, "_build", "liborotran.so")
 
 
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "rotran_oracle.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("rotran_oracle.c", "tmoone_fock_oracle.c", "rotran_oracle.h")]
+    if force or not os.path.exists(LIB) or \
+            os.path.getmtime(LIB) < max(os.path.getmtime(f) for f in srcs):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
         subprocess.check_call(["gcc", "-O2", "-fPIC", "-fopenmp", "-std=c11", "-shared",
-                               "-o", LIB, src, "-lm"], cwd=HERE)
+                               "-o", LIB, srcs[0], srcs[1], "-lm"], cwd=HERE)
     return LIB
 
 
@@ -116,6 +118,27 @@ def run(problem, thrgen=1e-16, throut=1e-16, nthreads=0, limit_pq=0, limit_ij=0,
     finally:
         lib.orc_free(C.byref(res))
     return img
+
+
+def fock_skeleton(records, nsc, dens, mfil=3):
+    """tmoone's skeleton Fock sets (MFDFOCK/FOCK) of flat records
+    ``(cls, its, nts, v, l2, l1)``; ``dens`` is (nmat, 4, nsc(nsc+1)/2) in the
+    order AAR, BAR, AAI, BAI.  Returns the Fock sets in the same shape."""
+    lib = _load()
+    cls, its, l2, l1 = (np.ascontiguousarray(x, np.int32) for x in
+                        (records[0], records[1], records[4], records[5]))
+    nts = np.ascontiguousarray(records[2], np.int64)
+    v = np.ascontiguousarray(records[3], np.float64)
+    d = np.ascontiguousarray(dens, np.float64)
+    assert d.ndim == 3 and d.shape[1] == 4 and d.shape[2] == nsc * (nsc + 1) // 2
+    f = np.empty_like(d)
+    rc = lib.orc_fock_skeleton(C.c_long(cls.size), _ptr(cls, C.c_int), _ptr(its, C.c_int),
+                               _ptr(nts, C.c_long), _ptr(v, C.c_double), _ptr(l2, C.c_int),
+                               _ptr(l1, C.c_int), mfil, nsc, d.shape[0], _ptr(d, C.c_double),
+                               _ptr(f, C.c_double))
+    if rc != 0:
+        raise ValueError("integral label outside 1..NSC")
+    return f
 
 
 def inttyp(a, b, c, d):

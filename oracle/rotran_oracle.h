@@ -48,6 +48,11 @@ int orc_run(const orc_params* prm, const double* qa, const int* itrmo, const int
             orc_result* out);
 void orc_free(orc_result* r);
 
+/* tmoone's skeleton Fock build (tmoone_fock_oracle.c) */
+int orc_fock_skeleton(long nrec, const int* rec_file, const int* rec_it, const long* rec_nt,
+                      const double* rint, const int* label2, const int* label1, int mfil, int nsc,
+                      int nmat, const double* dens, double* fock);
+
 #ifdef __cplusplus
 }
 #endif
