@@ -291,7 +291,8 @@ def run_breit_case(args, rank):
 def run_fock_case(args, rank, hbm_peak, peak_kind):
     """tmoone's skeleton Fock build (MFDFOCK/FOCK, rt_fock_skeleton) over the
     precision-study workload's 8.7e8 resident integral records (n = 400,
-    14 GB, larger than L2): closed shell (one density set) and closed plus
+    14 GB, larger than L2; ``fock_small``: the n = 200 profiling case, 5.5e7
+    integrals, 0.9 GB): closed shell (one density set) and closed plus
     open shell (two), kernel time by CUDA events over the steps after the
     warm-ups.  Checks: GPU vs the oracle on the first records (about 3e7
     integrals, 1e-12 of max|F|), linearity F(D1 + D2) = F(D1) + F(D2) at full
@@ -303,7 +304,7 @@ def run_fock_case(args, rank, hbm_peak, peak_kind):
     import pyoracle
     if rank != 0:
         return
-    work = WORKLOAD
+    work = PROFILE2 if args.workload == "fock_small" else WORKLOAD
     prob = synth.make_spinor_problem(work["n_l"], work["n_s"], work["nkr"], seed=work["seed"])
     cls, its, nts, dv, dl2, dl1 = synth.device_records(prob, 3, device="cuda")
     torch.cuda.synchronize()
@@ -313,7 +314,7 @@ def run_fock_case(args, rank, hbm_peak, peak_kind):
     g = torch.Generator(device="cuda").manual_seed(0)
     d1 = torch.randn((1, 4, ntri), device="cuda", dtype=torch.float64, generator=g)
     d2 = torch.randn((1, 4, ntri), device="cuda", dtype=torch.float64, generator=g)
-    out = {"workload": "fock_skeleton_n400", "n": n, "integrals": nint, "records": int(cls.size),
+    out = {"workload": f"fock_skeleton_n{n}", "n": n, "integrals": nint, "records": int(cls.size),
            "steps": args.steps, "warmup": args.warmup}
     with rotran.Rotran.for_problem(prob) as rt:
         rt.add_records_bulk_device(cls, nts, its, dv, dl2, dl1)
@@ -559,7 +560,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", default="precision",
                     choices=["precision", "c1", "profile", "profile2", "large", "batched", "gemm", "files",
-                             "breit", "fock"])
+                             "breit", "fock", "fock_small"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
@@ -579,7 +580,7 @@ def main():
         return run_files_case(args, rank)
     if args.workload == "breit":
         return run_breit_case(args, rank)
-    if args.workload == "fock":
+    if args.workload in ("fock", "fock_small"):
         return run_fock_case(args, rank, hbm_peak, peak_kind)
     work = {"precision": WORKLOAD, "c1": SMALL, "profile": PROFILE, "profile2": PROFILE2,
             "large": LARGE}[args.workload]

@@ -7,7 +7,7 @@
 // AAR, BAR, AAI, BAI, in up to two density sets (closed and open shell).
 // FOCK spells the fourteen types out one by one; here each type is a short
 // table of terms -- target pair, source pair (positions in (I,J,K,L)) and one
-// integer factor per array -- read from constant memory:
+// integer factor per array:
 //
 //   F_x(target) += (integral * D_x(source)) * factor_x      x = AAR..BAI
 //
@@ -15,9 +15,11 @@
 // a persistent grid walks the records in chunks of up to 4096 integrals, one
 // chunk per block at a time (a record has one type, so the term table is
 // uniform across the block).  The additions are FP64 atomics into
-// the Fock arrays (a few MB, resident in L2).  Where a whole warp adds to
-// the same element -- records list many integrals of one (I,J) pair in a
-// row -- the warp sums its contributions first and adds once.
+// the Fock arrays (a few MB, resident in L2).  The term lists are expanded at
+// compile time per type (the kernel is bound by instruction issue, not by
+// the atomics).  Where a whole warp adds to the same element -- records list
+// many integrals of one label pair in a row -- the warp sums first and adds
+// once.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -29,122 +31,157 @@ namespace rt {
 namespace {
 
 struct FockTerm {
-    int8_t tx, ty, sx, sy;  // target pair and source pair, positions 0..3 of (I,J,K,L)
-    int8_t c[4];            // factor per array: AAR, BAR, AAI, BAI
-};
-struct FockType {
-    int nterm;
-    FockTerm t[6];
+    int tx, ty, sx, sy;  // target pair and source pair, positions 0..3 of (I,J,K,L)
+    int c[4];            // factor per array: AAR, BAR, AAI, BAI
 };
 
-// I = 0, J = 1, K = 2, L = 3; the fock.F lines each row restates
-#define FT_(tx, ty, sx, sy, a, b, c, d) {tx, ty, sx, sy, {a, b, c, d}}
+// The terms of type `it` (1..14), I = 0, J = 1, K = 2, L = 3, with the
+// fock.F lines each row restates; evaluated at compile time.
+__host__ __device__ constexpr int fock_nterm(int it) {
+    return it == 1 ? 1 : it == 2 || it == 3 ? 3 : it == 4 || it == 6 ? 2 : it >= 12 ? 6 : 4;
+}
+__host__ __device__ constexpr FockTerm fock_term(int it, int q) {
+#define FT_(tx, ty, sx, sy, a, b, c, d) FockTerm{tx, ty, sx, sy, {a, b, c, d}}
 #define FT(...) FT_(__VA_ARGS__)
 #define ALL(v) v, v, v, v
-__constant__ FockType c_fock_types[15] = {
-    {0, {}},
-    // 1 (fock.F:52-65): (II|II)
-    {1, {FT(0, 1, 0, 1, 1, -1, -1, -1)}},
-    // 2 (fock.F:72-107)
-    {3, {FT(0, 1, 0, 1, 3, 1, 1, 1), FT(1, 3, 0, 2, ALL(-1)), FT(0, 2, 1, 3, ALL(-1))}},
-    // 3 (fock.F:115-138)
-    {3, {FT(0, 1, 2, 3, 2, 0, 0, 0), FT(2, 3, 0, 1, 2, 0, 0, 0), FT(0, 2, 0, 2, ALL(-1))}},
-    // 4 (fock.F:146-164)
-    {2, {FT(0, 1, 2, 3, 2, 0, 0, 0), FT(2, 3, 0, 1, 1, -1, -1, -1)}},
-    // 5 (fock.F:172-206)
-    {4, {FT(0, 1, 2, 3, 4, 0, 0, 0), FT(2, 3, 0, 1, 2, 0, 0, 0), FT(0, 3, 1, 2, ALL(-1)),
-         FT(1, 2, 0, 3, ALL(-1))}},
-    // 6 (fock.F:214-232)
-    {2, {FT(2, 3, 0, 1, 2, 0, 0, 0), FT(0, 1, 2, 3, 1, -1, -1, -1)}},
-    // 7 (fock.F:240-274)
-    {4, {FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 1, 2, 3, 2, 0, 0, 0), FT(0, 2, 1, 3, ALL(-1)),
-         FT(1, 3, 0, 2, ALL(-1))}},
-    // 8 (fock.F:282-316)
-    {4, {FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 1, 2, 3, 2, 0, 0, 0), FT(0, 2, 3, 1, -1, 1, 1, 1),
-         FT(3, 1, 0, 2, -1, 1, 1, 1)}},
-    // 9 (fock.F:324-364)
-    {4, {FT(0, 1, 2, 3, 3, -1, -1, -1), FT(2, 3, 0, 1, 3, -1, -1, -1), FT(0, 3, 1, 2, -1, -1, 1, -1),
-         FT(1, 2, 0, 3, -2, 0, 0, 0)}},
-    // 10 (fock.F:372-412)
-    {4, {FT(0, 1, 2, 3, 3, 1, 1, 1), FT(2, 3, 0, 1, 3, 1, 1, 1), FT(0, 2, 1, 3, -2, 0, 0, 0),
-         FT(1, 3, 0, 2, ALL(-1))}},
-    // 11 (fock.F:420-460)
-    {4, {FT(0, 1, 2, 3, 3, 1, 1, 1), FT(2, 3, 0, 1, 3, 1, 1, 1), FT(0, 2, 1, 3, ALL(-1)),
-         FT(1, 3, 0, 2, -2, 0, 0, 0)}},
-    // 12 (fock.F:468-522)
-    {6, {FT(0, 1, 2, 3, 4, 0, 0, 0), FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 3, 1, 2, ALL(-1)),
-         FT(1, 2, 0, 3, ALL(-1)), FT(0, 2, 1, 3, ALL(-1)), FT(1, 3, 0, 2, ALL(-1))}},
-    // 13 (fock.F:530-584)
-    {6, {FT(0, 1, 2, 3, 4, 0, 0, 0), FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 3, 2, 1, -1, 1, 1, 1),
-         FT(2, 1, 0, 3, -1, 1, 1, 1), FT(0, 2, 1, 3, ALL(-1)), FT(1, 3, 0, 2, ALL(-1))}},
-    // 14 (fock.F:593-647)
-    {6, {FT(0, 1, 2, 3, 4, 0, 0, 0), FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 3, 2, 1, -1, 1, 1, 1),
-         FT(2, 1, 0, 3, -1, 1, 1, 1), FT(0, 2, 3, 1, -1, 1, 1, 1), FT(3, 1, 0, 2, -1, 1, 1, 1)}},
-};
+    const FockTerm t[15][6] = {
+        {},
+        // 1 (fock.F:52-65)
+        {FT(0, 1, 0, 1, 1, -1, -1, -1)},
+        // 2 (fock.F:72-107)
+        {FT(0, 1, 0, 1, 3, 1, 1, 1), FT(1, 3, 0, 2, ALL(-1)), FT(0, 2, 1, 3, ALL(-1))},
+        // 3 (fock.F:115-138)
+        {FT(0, 1, 2, 3, 2, 0, 0, 0), FT(2, 3, 0, 1, 2, 0, 0, 0), FT(0, 2, 0, 2, ALL(-1))},
+        // 4 (fock.F:146-164)
+        {FT(0, 1, 2, 3, 2, 0, 0, 0), FT(2, 3, 0, 1, 1, -1, -1, -1)},
+        // 5 (fock.F:172-206)
+        {FT(0, 1, 2, 3, 4, 0, 0, 0), FT(2, 3, 0, 1, 2, 0, 0, 0), FT(0, 3, 1, 2, ALL(-1)),
+         FT(1, 2, 0, 3, ALL(-1))},
+        // 6 (fock.F:214-232)
+        {FT(2, 3, 0, 1, 2, 0, 0, 0), FT(0, 1, 2, 3, 1, -1, -1, -1)},
+        // 7 (fock.F:240-274)
+        {FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 1, 2, 3, 2, 0, 0, 0), FT(0, 2, 1, 3, ALL(-1)),
+         FT(1, 3, 0, 2, ALL(-1))},
+        // 8 (fock.F:282-316)
+        {FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 1, 2, 3, 2, 0, 0, 0), FT(0, 2, 3, 1, -1, 1, 1, 1),
+         FT(3, 1, 0, 2, -1, 1, 1, 1)},
+        // 9 (fock.F:324-364)
+        {FT(0, 1, 2, 3, 3, -1, -1, -1), FT(2, 3, 0, 1, 3, -1, -1, -1), FT(0, 3, 1, 2, -1, -1, 1, -1),
+         FT(1, 2, 0, 3, -2, 0, 0, 0)},
+        // 10 (fock.F:372-412)
+        {FT(0, 1, 2, 3, 3, 1, 1, 1), FT(2, 3, 0, 1, 3, 1, 1, 1), FT(0, 2, 1, 3, -2, 0, 0, 0),
+         FT(1, 3, 0, 2, ALL(-1))},
+        // 11 (fock.F:420-460)
+        {FT(0, 1, 2, 3, 3, 1, 1, 1), FT(2, 3, 0, 1, 3, 1, 1, 1), FT(0, 2, 1, 3, ALL(-1)),
+         FT(1, 3, 0, 2, -2, 0, 0, 0)},
+        // 12 (fock.F:468-522)
+        {FT(0, 1, 2, 3, 4, 0, 0, 0), FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 3, 1, 2, ALL(-1)),
+         FT(1, 2, 0, 3, ALL(-1)), FT(0, 2, 1, 3, ALL(-1)), FT(1, 3, 0, 2, ALL(-1))},
+        // 13 (fock.F:530-584)
+        {FT(0, 1, 2, 3, 4, 0, 0, 0), FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 3, 2, 1, -1, 1, 1, 1),
+         FT(2, 1, 0, 3, -1, 1, 1, 1), FT(0, 2, 1, 3, ALL(-1)), FT(1, 3, 0, 2, ALL(-1))},
+        // 14 (fock.F:593-647)
+        {FT(0, 1, 2, 3, 4, 0, 0, 0), FT(2, 3, 0, 1, 4, 0, 0, 0), FT(0, 3, 2, 1, -1, 1, 1, 1),
+         FT(2, 1, 0, 3, -1, 1, 1, 1), FT(0, 2, 3, 1, -1, 1, 1, 1), FT(3, 1, 0, 2, -1, 1, 1, 1)},
+    };
 #undef ALL
 #undef FT
 #undef FT_
-
-__device__ __forceinline__ int pick(int i, int j, int k, int l, int pos) {
-    return pos == 0 ? i : pos == 1 ? j : pos == 2 ? k : l;
+    return t[it][q];
 }
 
-__device__ __forceinline__ long long tri0(int x, int y) { return (long long)x * (x - 1) / 2 + y - 1; }
+template <int P>
+__device__ __forceinline__ unsigned pick(unsigned i, unsigned j, unsigned k, unsigned l) {
+    if constexpr (P == 0) return i;
+    else if constexpr (P == 1) return j;
+    else if constexpr (P == 2) return k;
+    else return l;
+}
+
+// 0-based lower-triangle position x(x-1)/2 + y - 1 (fits 32 bits for x, y <= 65535)
+__device__ __forceinline__ unsigned tri0(unsigned x, unsigned y) { return x * (x - 1) / 2 + y - 1; }
+
+// Term Q onwards of type IT for one integral per lane (lanes with on = false
+// add nothing but take part in the warp votes).  When the whole warp adds to
+// one element, one lane adds the warp's sum.
+template <int IT, int Q>
+__device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsigned k, unsigned l, double v,
+                                           int lane, int leader, int nmat, unsigned ntri,
+                                           const double* __restrict__ dens, double* __restrict__ fock) {
+    if constexpr (Q < fock_nterm(IT)) {
+        constexpr FockTerm m = fock_term(IT, Q);
+        const unsigned tg = tri0(pick<m.tx>(i, j, k, l), pick<m.ty>(i, j, k, l));
+        const unsigned sr = tri0(pick<m.sx>(i, j, k, l), pick<m.sy>(i, j, k, l));
+        const unsigned tg0 = __shfl_sync(0xffffffffu, tg, leader);
+        const bool uniform = __all_sync(0xffffffffu, !on || tg == tg0);
+        for (int s = 0; s < nmat; ++s) {
+            const double* d = dens + (size_t)s * 4 * ntri;
+            double* f = fock + (size_t)s * 4 * ntri;
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+                if (m.c[x] == 0) continue;
+                double c = on ? (v * d[(size_t)x * ntri + sr]) * (double)m.c[x] : 0.0;
+                if (uniform) {
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+                    if (lane == leader) atomicAdd(f + (size_t)x * ntri + tg0, c);
+                } else if (on) {
+                    atomicAdd(f + (size_t)x * ntri + tg, c);
+                }
+            }
+        }
+        fock_terms<IT, Q + 1>(on, i, j, k, l, v, lane, leader, nmat, ntri, dens, fock);
+    }
+}
+
+// the integrals of one record chunk, all of type IT
+template <int IT>
+__device__ __forceinline__ void fock_chunk(const FockRec& R, const double* __restrict__ rint,
+                                           const int* __restrict__ l2, const int* __restrict__ l1,
+                                           unsigned nsc, unsigned ntri, int nmat,
+                                           const double* __restrict__ dens, double* __restrict__ fock,
+                                           unsigned long long* __restrict__ bad) {
+    const int lane = threadIdx.x & 31;
+    for (long long base = 0; base < R.nt; base += blockDim.x) {
+        const long long t = base + threadIdx.x;
+        bool on = t < R.nt;
+        unsigned i = 1, j = 1, k = 1, l = 1;
+        double v = 0.0;
+        if (on) {
+            const unsigned u2 = (unsigned)l2[R.off + t], u1 = (unsigned)l1[R.off + t];
+            i = u2 >> 16, j = u2 & 0xFFFFu, k = u1 >> 16, l = u1 & 0xFFFFu;
+            if (i - 1 >= nsc || j - 1 >= nsc || k - 1 >= nsc || l - 1 >= nsc) {  // outside 1..nsc
+                atomicOr(bad, 1ull);
+                on = false;
+                i = j = k = l = 1;
+            } else {
+                v = rint[R.off + t];
+            }
+        }
+        const unsigned on_mask = __ballot_sync(0xffffffffu, on);
+        if (on_mask == 0) continue;
+        fock_terms<IT, 0>(on, i, j, k, l, v, lane, __ffs(on_mask) - 1, nmat, ntri, dens, fock);
+    }
+}
 
 __global__ void __launch_bounds__(256) k_fock_skeleton(const double* __restrict__ rint,
                                                        const int* __restrict__ l2,
                                                        const int* __restrict__ l1,
                                                        const FockRec* __restrict__ recs, int nrec,
-                                                       int nsc, long long ntri, int nmat,
+                                                       unsigned nsc, unsigned ntri, int nmat,
                                                        const double* __restrict__ dens,
                                                        double* __restrict__ fock,
                                                        unsigned long long* __restrict__ bad) {
-    const int lane = threadIdx.x & 31;
     for (int r = blockIdx.x; r < nrec; r += gridDim.x) {
         const FockRec R = recs[r];
-        const FockType& T = c_fock_types[R.it];
-        for (long long base = 0; base < R.nt; base += blockDim.x) {
-            const long long t = base + threadIdx.x;
-            bool on = t < R.nt;
-            int i = 1, j = 1, k = 1, l = 1;
-            double v = 0.0;
-            if (on) {
-                const unsigned u2 = (unsigned)l2[R.off + t], u1 = (unsigned)l1[R.off + t];
-                i = (int)(u2 >> 16), j = (int)(u2 & 0xFFFFu), k = (int)(u1 >> 16), l = (int)(u1 & 0xFFFFu);
-                if (i < 1 || i > nsc || j < 1 || j > nsc || k < 1 || k > nsc || l < 1 || l > nsc) {
-                    atomicOr(bad, 1ull);
-                    on = false;
-                    i = j = k = l = 1;
-                } else {
-                    v = rint[R.off + t];
-                }
-            }
-            const unsigned on_mask = __ballot_sync(0xffffffffu, on);
-            if (on_mask == 0) continue;
-            const int leader = __ffs(on_mask) - 1;
-            for (int q = 0; q < T.nterm; ++q) {
-                const FockTerm m = T.t[q];
-                const long long tg = tri0(pick(i, j, k, l, m.tx), pick(i, j, k, l, m.ty));
-                const long long sr = tri0(pick(i, j, k, l, m.sx), pick(i, j, k, l, m.sy));
-                const long long tg0 = __shfl_sync(0xffffffffu, tg, leader);
-                const bool uniform = __all_sync(0xffffffffu, !on || tg == tg0);
-                for (int s = 0; s < nmat; ++s) {
-                    const double* d = dens + (long long)s * 4 * ntri;
-                    double* f = fock + (long long)s * 4 * ntri;
-#pragma unroll
-                    for (int x = 0; x < 4; ++x) {
-                        if (m.c[x] == 0) continue;
-                        double c = on ? (v * d[x * ntri + sr]) * (double)m.c[x] : 0.0;
-                        if (uniform) {
-#pragma unroll
-                            for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-                            if (lane == leader) atomicAdd(f + x * ntri + tg0, c);
-                        } else if (on) {
-                            atomicAdd(f + x * ntri + tg, c);
-                        }
-                    }
-                }
-            }
+        switch (R.it) {  // uniform across the block
+#define RT_FOCK_CASE(T) \
+    case T: fock_chunk<T>(R, rint, l2, l1, nsc, ntri, nmat, dens, fock, bad); break;
+            RT_FOCK_CASE(1) RT_FOCK_CASE(2) RT_FOCK_CASE(3) RT_FOCK_CASE(4) RT_FOCK_CASE(5)
+            RT_FOCK_CASE(6) RT_FOCK_CASE(7) RT_FOCK_CASE(8) RT_FOCK_CASE(9) RT_FOCK_CASE(10)
+            RT_FOCK_CASE(11) RT_FOCK_CASE(12) RT_FOCK_CASE(13) RT_FOCK_CASE(14)
+#undef RT_FOCK_CASE
+            default: break;
         }
     }
 }
@@ -155,9 +192,9 @@ void launch_fock_skeleton(cudaStream_t st, const double* rint, const int* l2, co
                           const FockRec* recs, int nrec, int nsc, int nmat, const double* dens,
                           double* fock, unsigned long long* bad) {
     if (nrec <= 0) return;
-    const long long ntri = (long long)nsc * (nsc + 1) / 2;
+    const unsigned ntri = (unsigned)((long long)nsc * (nsc + 1) / 2);
     const int grid = nrec < 152 * 8 ? nrec : 152 * 8;
-    k_fock_skeleton<<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, nsc, ntri, nmat, dens, fock, bad);
+    k_fock_skeleton<<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, (unsigned)nsc, ntri, nmat, dens, fock, bad);
 }
 
 }  // namespace rt
