@@ -101,12 +101,75 @@ __device__ __forceinline__ unsigned pick(unsigned i, unsigned j, unsigned k, uns
 // 0-based lower-triangle position x(x-1)/2 + y - 1 (fits 32 bits for x, y <= 65535)
 __device__ __forceinline__ unsigned tri0(unsigned x, unsigned y) { return x * (x - 1) / 2 + y - 1; }
 
+// Products in the integer units.  GB300 issues FP64 arithmetic at a small
+// fraction of its integer rate, and each term and array needs one product
+// integral x density element, so the products are formed from the binary64
+// fields directly: the 53-bit significands multiplied into the high 64 bits
+// of their 106-bit product (one 64x64 high multiply), renormalised by one
+// bit where the product is 2 or more, rounded to nearest on the first
+// dropped bit, and given the summed exponent plus log2 of the term's
+// power-of-two factor.  The result is within one unit in the last place of
+// the exact product (the discarded low 64 bits only decide ties), which the
+// tolerance of the sums (1e-12 of the largest element) does not see.  Zero
+// and subnormal operands give zero; the integrals and densities are normal
+// numbers far from overflow.
+__device__ __forceinline__ double mul_pow2(double a, double b, int log2f, unsigned long long flip) {
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+    const int ea = (int)((ua >> 52) & 0x7FF), eb = (int)((ub >> 52) & 0x7FF);
+    if (ea == 0 || eb == 0) return 0.0;
+    constexpr unsigned long long MANT = (1ull << 52) - 1, HIDDEN = 1ull << 52;
+    const unsigned long long hi = __umul64hi(((ua & MANT) | HIDDEN) << 11, ((ub & MANT) | HIDDEN) << 11);
+    const int two = (int)(hi >> 63);           // product of the significands >= 2
+    const int sh = 10 + two;
+    unsigned long long m = (hi >> sh) + ((hi >> (sh - 1)) & 1ull);
+    int e = ea + eb - 1023 + two + log2f;
+    if (m >> 53) {                             // rounding carried into bit 53
+        m >>= 1;
+        ++e;
+    }
+    if (e <= 0) return 0.0;
+    const unsigned long long sign = ((ua ^ ub) & (1ull << 63)) ^ flip;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)e << 52) | (m & MANT)));
+}
+
+// The integral's multiples for the factors 3 (one FP64 multiply, made only
+// for the types that use it); 1, 2 and 4 enter through the exponent.
+struct Multiples {
+    double v1, v3;
+};
+// (C v) * dv for a term factor C in -4..4, C != 0
+template <int C>
+__device__ __forceinline__ double times(const Multiples& w, double dv) {
+    constexpr int a = C < 0 ? -C : C;
+    constexpr unsigned long long flip = C < 0 ? (1ull << 63) : 0ull;
+    if constexpr (a == 3) return mul_pow2(w.v3, dv, 0, flip);
+    else return mul_pow2(w.v1, dv, a == 1 ? 0 : a == 2 ? 1 : 2, flip);
+}
+
 // Term Q onwards of type IT for one integral per lane (lanes with on = false
 // add nothing but take part in the warp votes).  When the whole warp adds to
 // one element, one lane adds the warp's sum.
+// F_x(tg) += (C v) D_x(sr) for array x of one density set
+template <int C>
+__device__ __forceinline__ void add_term(int x, bool on, bool uniform, int lane, int leader, const Multiples& w,
+                                         const double* __restrict__ d, double* __restrict__ f, unsigned ntri,
+                                         unsigned sr, unsigned tg, unsigned tg0) {
+    if constexpr (C != 0) {
+        double c = on ? times<C>(w, d[(size_t)x * ntri + sr]) : 0.0;
+        if (uniform) {
+#pragma unroll
+            for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+            if (lane == leader) atomicAdd(f + (size_t)x * ntri + tg0, c);
+        } else if (on) {
+            atomicAdd(f + (size_t)x * ntri + tg, c);
+        }
+    }
+}
+
 template <int IT, int Q>
-__device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsigned k, unsigned l, double v,
-                                           int lane, int leader, int nmat, unsigned ntri,
+__device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsigned k, unsigned l,
+                                           const Multiples& w, int lane, int leader, int nmat, unsigned ntri,
                                            const double* __restrict__ dens, double* __restrict__ fock) {
     if constexpr (Q < fock_nterm(IT)) {
         constexpr FockTerm m = fock_term(IT, Q);
@@ -117,20 +180,12 @@ __device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsi
         for (int s = 0; s < nmat; ++s) {
             const double* d = dens + (size_t)s * 4 * ntri;
             double* f = fock + (size_t)s * 4 * ntri;
-#pragma unroll
-            for (int x = 0; x < 4; ++x) {
-                if (m.c[x] == 0) continue;
-                double c = on ? (v * d[(size_t)x * ntri + sr]) * (double)m.c[x] : 0.0;
-                if (uniform) {
-#pragma unroll
-                    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-                    if (lane == leader) atomicAdd(f + (size_t)x * ntri + tg0, c);
-                } else if (on) {
-                    atomicAdd(f + (size_t)x * ntri + tg, c);
-                }
-            }
+            add_term<m.c[0]>(0, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
+            add_term<m.c[1]>(1, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
+            add_term<m.c[2]>(2, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
+            add_term<m.c[3]>(3, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
         }
-        fock_terms<IT, Q + 1>(on, i, j, k, l, v, lane, leader, nmat, ntri, dens, fock);
+        fock_terms<IT, Q + 1>(on, i, j, k, l, w, lane, leader, nmat, ntri, dens, fock);
     }
 }
 
@@ -160,7 +215,8 @@ __device__ __forceinline__ void fock_chunk(const FockRec& R, const double* __res
         }
         const unsigned on_mask = __ballot_sync(0xffffffffu, on);
         if (on_mask == 0) continue;
-        fock_terms<IT, 0>(on, i, j, k, l, v, lane, __ffs(on_mask) - 1, nmat, ntri, dens, fock);
+        const Multiples w{v, 3.0 * v};   // 3v is made only where a type uses it
+        fock_terms<IT, 0>(on, i, j, k, l, w, lane, __ffs(on_mask) - 1, nmat, ntri, dens, fock);
     }
 }
 
