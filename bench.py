@@ -360,7 +360,12 @@ def run_fock_case(args, rank, hbm_peak, peak_kind):
                         "value": nint / (legs["closed_open"]["ms_kernel"] / 1e3)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "bytes_per_integral": 16,
-                     "peak_source": f"hbm_gbs of {peak_kind}"},
+                     "traffic": 16.09 * nint,
+                     "traffic_source": "ncu capture of the n = 200 case (profiles/k_fock_skeleton_n200.md): "
+                                       "16.09 DRAM bytes per integral, scaled by the integrals",
+                     "peak_source": f"hbm_gbs of {peak_kind}",
+                     "limiter": "work per integral (18 atomics and gathers for the generic types), "
+                                "not HBM"},
         "checks": {"oracle_sample_integrals": ns, "oracle_max_rel_err": err,
                    "linearity_rel_err": lin, "two_sets_vs_one_rel_err": two},
         "cpu_baseline": {"value": ns / cpu_sec, "unit": "integrals/s", "cores": 1, "kind": "port",
