@@ -350,7 +350,38 @@ def run_fock_case(args, rank, hbm_peak, peak_kind):
     with rotran.Rotran.for_problem(prob) as rt:
         rt.add_records_bulk(*(sample[0], sample[2], sample[1], sample[3], sample[4], sample[5]))
         got, _ = rt.fock_skeleton(dh)
-    err = float(np.abs(got - want).max() / max(1.0, np.abs(want).max()))
+    err = float(np.abs(got - want).max() / np.abs(want).max())
+    gaunt = None
+    if args.workload == "fock":
+        # tmoone's Gaunt contributions (MFDBREIT/GAUNT) over the Gaunt file of
+        # the n = 200, 60 Kramers pair case (4.6e7 (SL|SL) integrals)
+        bp = synth.make_problem(80, 120, 60, seed=0, breit=True, mfil=1)
+        brecs = bp.flat_records()
+        keep = brecs[0] == 4
+        boff = np.concatenate([[0], np.cumsum(brecs[2])])
+        bsel = np.concatenate([np.arange(boff[r], boff[r + 1]) for r in np.nonzero(keep)[0]])
+        b6 = (brecs[0][keep], brecs[1][keep], brecs[2][keep], brecs[3][bsel], brecs[4][bsel], brecs[5][bsel])
+        bn = bp.n
+        bd = np.random.default_rng(1).standard_normal((1, 4, bn * (bn + 1) // 2))
+        bcfg, bkeep = rotran.make_config(bn, bp.nsc1, bp.nkr, mfil=3)
+        with rotran.Rotran(bcfg, bkeep) as rt:
+            rt.add_records_bulk(b6[0], b6[2], b6[1], b6[3], b6[4], b6[5])
+            for _ in range(args.warmup):
+                rt.fock_gaunt(bd)
+            gms = []
+            for _ in range(max(1, args.steps)):
+                gf, k = rt.fock_gaunt(bd)
+                gms.append(k)
+        t0 = time.perf_counter()
+        gw = pyoracle.fock_gaunt(b6, bn, bd)
+        gcpu = time.perf_counter() - t0
+        gint = int(b6[3].size)
+        gaunt = {"integrals": gint, "ms_kernel": statistics.mean(gms),
+                 "value": gint / (statistics.mean(gms) / 1e3), "unit": "integrals/s",
+                 "oracle_max_rel_err": float(np.abs(gf - gw).max() / np.abs(gw).max()),
+                 "max_abs_element": float(np.abs(gw).max()),
+                 "cpu_baseline": {"value": gint / gcpu, "unit": "integrals/s", "cores": 1, "kind": "port",
+                                  "sample": "all Gaunt integrals of the case"}}
     ms = legs["closed"]["ms_kernel"]
     achieved = 16.0 * nint / (ms / 1e3) / 1e9
     out.update({
@@ -370,6 +401,7 @@ def run_fock_case(args, rank, hbm_peak, peak_kind):
                    "linearity_rel_err": lin, "two_sets_vs_one_rel_err": two},
         "cpu_baseline": {"value": ns / cpu_sec, "unit": "integrals/s", "cores": 1, "kind": "port",
                          "sample": f"first {nr} records ({ns} integrals), one density set"},
+        "gaunt": gaunt,
     })
     print(json.dumps(out))
 

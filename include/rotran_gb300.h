@@ -200,6 +200,18 @@ int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double* energy);
  * 1..14 fails with RT_ERR_USER. */
 int rt_fock_skeleton(rt_ctx* ctx, int nmat, const double* dens, double* fock, double* ms_kernel);
 
+/* tmoone's Gaunt contributions to the same Fock sets (MFDBREIT,
+ * source/tmoone/mfdbreit.F:50-138, with GAUNT, source/tmoone/gaunt.F) from
+ * the context's file-4 records (SRTBREI/SRTBREL, class 4 of
+ * rt_add_ao_records*; rt_read_srt_files reads them for contexts created with
+ * BREIT = 1).  Layouts as rt_fock_skeleton.  accumulate = 1 adds them to the
+ * sets passed in fock (BREIT: after MFDFOCK, mfddriv.F:46); accumulate = 0
+ * overwrites (ONLYBRT, mfddriv.F:42, where MFDBREIT clears the sets).  A
+ * record type GAUNT does not accept (other than 2, 10, 11, 13, 14) fails
+ * with RT_ERR_PROGRAM, as GAUNT's Q2JOB(6) does. */
+int rt_fock_gaunt(rt_ctx* ctx, int nmat, const double* dens, double* fock, int accumulate,
+                  double* ms_kernel);
+
 /* Batched transforms (no counterpart in the reference, which runs one
  * transformation per process).  rt_batch_create plans every context as a
  * single chunk (all pair groups and Kramers items resident at once; fails

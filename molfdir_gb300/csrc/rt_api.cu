@@ -2157,39 +2157,57 @@ extern "C" int rt_result_sizes(rt_ctx* ctx, long long* nrec, long long* nz) {
     API_CATCH
 }
 
-extern "C" int rt_fock_skeleton(rt_ctx* ctx, int nmat, const double* dens, double* fock, double* ms_kernel) {
-    if (!ctx) return RT_ERR_USER;
-    API_TRY
-    if (nmat < 1 || nmat > 2) throw Error(RT_ERR_USER, "rt_fock_skeleton: nmat must be 1 or 2");
-    if (!dens || !fock) throw Error(RT_ERR_USER, "rt_fock_skeleton: null density or Fock arrays");
+namespace {
+
+// One pass of tmoone's Fock build over the context's records: MFDFOCK's
+// files 1..MFIL with FOCK's terms, or MFDBREIT's file 4 with GAUNT's.  The
+// chunk list (records cut into <= 4096 integrals, one block each) is kept
+// while the records are unchanged.
+void fock_pass(rt_ctx* ctx, bool gaunt, int nmat, const double* dens, double* fock, bool accumulate,
+               double* ms_kernel) {
+    if (nmat < 1 || nmat > 2) throw Error(RT_ERR_USER, "Fock build: nmat must be 1 or 2");
+    if (!dens || !fock) throw Error(RT_ERR_USER, "Fock build: null density or Fock arrays");
     if (ctx->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
     cudaStream_t st = ctx->stream;
     flush_staged(ctx);
-    if (ctx->fock_gen != ctx->gen) {
-        // MFDFOCK reads files 1..MFIL (mfdfock.F:68); the Gaunt file is
-        // MFDBREIT's.  Records are cut into chunks of at most 4096 integrals
-        // (one block each), whatever their length.
+    const int w = gaunt ? 1 : 0;
+    if (ctx->fock_gen[w] != ctx->gen) {
         constexpr long long CHUNK = 4096;
         std::vector<FockRec> chunks;
-        for (int file = 1; file <= std::min(ctx->cfg.mfil, 3); ++file)
+        auto add = [&](size_t r) {
+            for (long long o = 0; o < ctx->rec_nt[r]; o += CHUNK)
+                chunks.push_back(FockRec{ctx->rec_off[r] + o, std::min(CHUNK, ctx->rec_nt[r] - o), ctx->rec_it[r], 0});
+        };
+        if (!gaunt) {
+            // MFDFOCK reads files 1..MFIL in order (mfdfock.F:68)
+            for (int file = 1; file <= std::min(ctx->cfg.mfil, 3); ++file)
+                for (size_t r = 0; r < ctx->rec_file.size(); ++r) {
+                    if (ctx->rec_file[r] != file || ctx->rec_nt[r] == 0) continue;
+                    if (ctx->rec_it[r] < 1 || ctx->rec_it[r] > 14)
+                        throw Error(RT_ERR_USER, "integral type outside 1..14 (fock.F:37)");
+                    add(r);
+                }
+        } else {
+            // MFDBREIT reads SRTBREI/SRTBREL (mfdbreit.F:66-138)
             for (size_t r = 0; r < ctx->rec_file.size(); ++r) {
-                if (ctx->rec_file[r] != file || ctx->rec_nt[r] == 0) continue;
-                if (ctx->rec_it[r] < 1 || ctx->rec_it[r] > 14)
-                    throw Error(RT_ERR_USER, "integral type outside 1..14 (fock.F:37)");
-                for (long long o = 0; o < ctx->rec_nt[r]; o += CHUNK)
-                    chunks.push_back(FockRec{ctx->rec_off[r] + o, std::min(CHUNK, ctx->rec_nt[r] - o),
-                                             ctx->rec_it[r], 0});
+                if (ctx->rec_file[r] != 4 || ctx->rec_nt[r] == 0) continue;
+                const int it = ctx->rec_it[r];
+                if (it != 2 && it != 10 && it != 11 && it != 13 && it != 14)
+                    throw Error(RT_ERR_PROGRAM, "INVALID TYPE IN BREIT: type " + std::to_string(it) +
+                                                    " (gaunt.F:25-28)");
+                add(r);
             }
+        }
         if ((long long)chunks.size() >= (1LL << 31)) throw Error(RT_ERR_DIM, "more than 2^31 record chunks");
-        dfree(ctx, ctx->d_fock_chunks);
-        ctx->d_fock_chunks = nullptr;
-        ctx->fock_gen = ~0ull;
-        ctx->d_fock_chunks = dalloc<FockRec>(ctx, std::max<size_t>(1, chunks.size()));
+        dfree(ctx, ctx->d_fock_chunks[w]);
+        ctx->d_fock_chunks[w] = nullptr;
+        ctx->fock_gen[w] = ~0ull;
+        ctx->d_fock_chunks[w] = dalloc<FockRec>(ctx, std::max<size_t>(1, chunks.size()));
         if (!chunks.empty())
-            RT_CUDA(cudaMemcpy(ctx->d_fock_chunks, chunks.data(), chunks.size() * sizeof(FockRec),
+            RT_CUDA(cudaMemcpy(ctx->d_fock_chunks[w], chunks.data(), chunks.size() * sizeof(FockRec),
                                cudaMemcpyHostToDevice));
-        ctx->n_fock_chunks = (long long)chunks.size();
-        ctx->fock_gen = ctx->gen;
+        ctx->n_fock_chunks[w] = (long long)chunks.size();
+        ctx->fock_gen[w] = ctx->gen;
     }
     const long long ntri = (long long)ctx->cfg.nsc * (ctx->cfg.nsc + 1) / 2;
     const size_t mat_bytes = (size_t)nmat * 4 * ntri * sizeof(double);
@@ -2201,11 +2219,12 @@ extern "C" int rt_fock_skeleton(rt_ctx* ctx, int nmat, const double* dens, doubl
     auto* d_bad = (unsigned long long*)tmp_alloc(ctx, sizeof(unsigned long long));
     tmp.push_back(d_bad);
     RT_CUDA(cudaMemcpyAsync(d_dens, dens, mat_bytes, cudaMemcpyDefault, st));
-    RT_CUDA(cudaMemsetAsync(d_fock, 0, mat_bytes, st));
+    if (accumulate) RT_CUDA(cudaMemcpyAsync(d_fock, fock, mat_bytes, cudaMemcpyDefault, st));
+    else RT_CUDA(cudaMemsetAsync(d_fock, 0, mat_bytes, st));
     RT_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(unsigned long long), st));
     RT_CUDA(cudaEventRecord(ctx->ev[0], st));
-    launch_fock_skeleton(st, ctx->d_rint, ctx->d_l2, ctx->d_l1, (const FockRec*)ctx->d_fock_chunks,
-                         (int)ctx->n_fock_chunks, ctx->cfg.nsc, nmat, d_dens, d_fock, d_bad);
+    launch_fock_skeleton(st, gaunt, ctx->d_rint, ctx->d_l2, ctx->d_l1, (const FockRec*)ctx->d_fock_chunks[w],
+                         (int)ctx->n_fock_chunks[w], ctx->cfg.nsc, nmat, d_dens, d_fock, d_bad);
     RT_CUDA(cudaGetLastError());
     RT_CUDA(cudaEventRecord(ctx->ev[1], st));
     unsigned long long bad = 0;
@@ -2217,6 +2236,22 @@ extern "C" int rt_fock_skeleton(rt_ctx* ctx, int nmat, const double* dens, doubl
     if (ms_kernel) *ms_kernel = ms;
     tmp_release(ctx, tmp, true);
     if (bad) throw Error(RT_ERR_USER, "integral label outside 1..NSC");
+}
+
+}  // namespace
+
+extern "C" int rt_fock_skeleton(rt_ctx* ctx, int nmat, const double* dens, double* fock, double* ms_kernel) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    fock_pass(ctx, false, nmat, dens, fock, false, ms_kernel);
+    API_CATCH
+}
+
+extern "C" int rt_fock_gaunt(rt_ctx* ctx, int nmat, const double* dens, double* fock, int accumulate,
+                             double* ms_kernel) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    fock_pass(ctx, true, nmat, dens, fock, accumulate != 0, ms_kernel);
     API_CATCH
 }
 

@@ -1,5 +1,7 @@
 // rt_fock.cu -- tmoone's skeleton Fock build on the GPU (replaces MFDFOCK,
-// source/tmoone/mfdfock.F:53-140, and FOCK, source/tmoone/fock.F:1-656).
+// source/tmoone/mfdfock.F:53-140, with FOCK, source/tmoone/fock.F:1-656,
+// and MFDBREIT, source/tmoone/mfdbreit.F:50-138, with GAUNT,
+// source/tmoone/gaunt.F).
 //
 // Every unique integral (IJ|KL) of a record of type IT (the index-coincidence
 // type of INTTYP) adds products "integral x density element x small factor"
@@ -90,6 +92,37 @@ __host__ __device__ constexpr FockTerm fock_term(int it, int q) {
     return t[it][q];
 }
 
+// The terms of tmoone's GAUNT (source/tmoone/gaunt.F) for the types it
+// accepts (2, 10, 11, 13, 14; the others stop it with Q2JOB class 6,
+// gaunt.F:25-28, and are refused on the host).
+__host__ __device__ constexpr int gaunt_nterm(int it) { return it == 2 ? 3 : 4; }
+__host__ __device__ constexpr FockTerm gaunt_term(int it, int q) {
+#define FT_(tx, ty, sx, sy, a, b, c, d) FockTerm{tx, ty, sx, sy, {a, b, c, d}}
+#define FT(...) FT_(__VA_ARGS__)
+    const FockTerm t2[3] = {  // gaunt.F:41-76, I = K > J = L
+        FT(0, 1, 0, 1, 3, 1, 1, 1), FT(1, 3, 0, 2, 3, -1, -1, -1), FT(0, 2, 1, 3, 3, -1, -1, -1)};
+    const FockTerm t10[4] = {  // gaunt.F:84-124, I = K > J > L
+        FT(0, 1, 2, 3, 3, 1, 1, 1), FT(2, 3, 0, 1, 3, 1, 1, 1), FT(0, 2, 1, 3, 6, 0, 0, 0),
+        FT(1, 3, 0, 2, 3, 1, -1, 1)};
+    const FockTerm t11[4] = {  // gaunt.F:132-172, I > K > J = L
+        FT(0, 1, 2, 3, 3, 1, 1, 1), FT(2, 3, 0, 1, 3, 1, 1, 1), FT(0, 2, 1, 3, 3, -1, -1, -1),
+        FT(1, 3, 0, 2, 6, 0, 0, 0)};
+    const FockTerm t13[4] = {  // gaunt.F:180-228, I > K > J > L
+        FT(0, 3, 2, 1, 3, 1, 1, 1), FT(2, 1, 0, 3, 3, 1, 1, 1), FT(0, 2, 1, 3, 3, -1, -1, -1),
+        FT(1, 3, 0, 2, 3, -1, -1, -1)};
+    const FockTerm t14[4] = {  // gaunt.F:236-284, I > K > L > J
+        FT(0, 3, 2, 1, 3, 1, 1, 1), FT(2, 1, 0, 3, 3, 1, 1, 1), FT(0, 2, 3, 1, 3, 1, 1, 1),
+        FT(3, 1, 0, 2, 3, 1, 1, 1)};
+#undef FT
+#undef FT_
+    return it == 2 ? t2[q] : it == 10 ? t10[q] : it == 11 ? t11[q] : it == 13 ? t13[q] : t14[q];
+}
+
+template <bool G>
+__host__ __device__ constexpr int nterm_of(int it) { return G ? gaunt_nterm(it) : fock_nterm(it); }
+template <bool G>
+__host__ __device__ constexpr FockTerm term_of(int it, int q) { return G ? gaunt_term(it, q) : fock_term(it, q); }
+
 template <int P>
 __device__ __forceinline__ unsigned pick(unsigned i, unsigned j, unsigned k, unsigned l) {
     if constexpr (P == 0) return i;
@@ -133,17 +166,18 @@ __device__ __forceinline__ double mul_pow2(double a, double b, int log2f, unsign
     return __longlong_as_double((long long)(sign | ((unsigned long long)e << 52) | (m & MANT)));
 }
 
-// The integral's multiples for the factors 3 (one FP64 multiply, made only
-// for the types that use it); 1, 2 and 4 enter through the exponent.
+// The integral's multiple 3v (one FP64 multiply, made only for the types
+// that use it); the factors 1, 2, 4 and the 2 of 6 enter through the exponent.
 struct Multiples {
     double v1, v3;
 };
-// (C v) * dv for a term factor C in -4..4, C != 0
+// (C v) * dv for a term factor C in {1, 2, 3, 4, 6} up to sign
 template <int C>
 __device__ __forceinline__ double times(const Multiples& w, double dv) {
     constexpr int a = C < 0 ? -C : C;
+    static_assert(a == 1 || a == 2 || a == 3 || a == 4 || a == 6, "term factor");
     constexpr unsigned long long flip = C < 0 ? (1ull << 63) : 0ull;
-    if constexpr (a == 3) return mul_pow2(w.v3, dv, 0, flip);
+    if constexpr (a == 3 || a == 6) return mul_pow2(w.v3, dv, a == 6 ? 1 : 0, flip);
     else return mul_pow2(w.v1, dv, a == 1 ? 0 : a == 2 ? 1 : 2, flip);
 }
 
@@ -167,12 +201,12 @@ __device__ __forceinline__ void add_term(int x, bool on, bool uniform, int lane,
     }
 }
 
-template <int IT, int Q>
+template <bool G, int IT, int Q>
 __device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsigned k, unsigned l,
                                            const Multiples& w, int lane, int leader, int nmat, unsigned ntri,
                                            const double* __restrict__ dens, double* __restrict__ fock) {
-    if constexpr (Q < fock_nterm(IT)) {
-        constexpr FockTerm m = fock_term(IT, Q);
+    if constexpr (Q < nterm_of<G>(IT)) {
+        constexpr FockTerm m = term_of<G>(IT, Q);
         const unsigned tg = tri0(pick<m.tx>(i, j, k, l), pick<m.ty>(i, j, k, l));
         const unsigned sr = tri0(pick<m.sx>(i, j, k, l), pick<m.sy>(i, j, k, l));
         const unsigned tg0 = __shfl_sync(0xffffffffu, tg, leader);
@@ -185,12 +219,12 @@ __device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsi
             add_term<m.c[2]>(2, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
             add_term<m.c[3]>(3, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
         }
-        fock_terms<IT, Q + 1>(on, i, j, k, l, w, lane, leader, nmat, ntri, dens, fock);
+        fock_terms<G, IT, Q + 1>(on, i, j, k, l, w, lane, leader, nmat, ntri, dens, fock);
     }
 }
 
-// the integrals of one record chunk, all of type IT
-template <int IT>
+// the integrals of one record chunk, all of type IT (G: GAUNT's terms)
+template <bool G, int IT>
 __device__ __forceinline__ void fock_chunk(const FockRec& R, const double* __restrict__ rint,
                                            const int* __restrict__ l2, const int* __restrict__ l1,
                                            unsigned nsc, unsigned ntri, int nmat,
@@ -216,10 +250,11 @@ __device__ __forceinline__ void fock_chunk(const FockRec& R, const double* __res
         const unsigned on_mask = __ballot_sync(0xffffffffu, on);
         if (on_mask == 0) continue;
         const Multiples w{v, 3.0 * v};   // 3v is made only where a type uses it
-        fock_terms<IT, 0>(on, i, j, k, l, w, lane, __ffs(on_mask) - 1, nmat, ntri, dens, fock);
+        fock_terms<G, IT, 0>(on, i, j, k, l, w, lane, __ffs(on_mask) - 1, nmat, ntri, dens, fock);
     }
 }
 
+template <bool G>
 __global__ void __launch_bounds__(256) k_fock_skeleton(const double* __restrict__ rint,
                                                        const int* __restrict__ l2,
                                                        const int* __restrict__ l1,
@@ -230,27 +265,39 @@ __global__ void __launch_bounds__(256) k_fock_skeleton(const double* __restrict_
                                                        unsigned long long* __restrict__ bad) {
     for (int r = blockIdx.x; r < nrec; r += gridDim.x) {
         const FockRec R = recs[r];
-        switch (R.it) {  // uniform across the block
 #define RT_FOCK_CASE(T) \
-    case T: fock_chunk<T>(R, rint, l2, l1, nsc, ntri, nmat, dens, fock, bad); break;
-            RT_FOCK_CASE(1) RT_FOCK_CASE(2) RT_FOCK_CASE(3) RT_FOCK_CASE(4) RT_FOCK_CASE(5)
-            RT_FOCK_CASE(6) RT_FOCK_CASE(7) RT_FOCK_CASE(8) RT_FOCK_CASE(9) RT_FOCK_CASE(10)
-            RT_FOCK_CASE(11) RT_FOCK_CASE(12) RT_FOCK_CASE(13) RT_FOCK_CASE(14)
-#undef RT_FOCK_CASE
-            default: break;
+    case T: fock_chunk<G, T>(R, rint, l2, l1, nsc, ntri, nmat, dens, fock, bad); break;
+        if constexpr (G) {
+            switch (R.it) {  // uniform across the block
+                RT_FOCK_CASE(2) RT_FOCK_CASE(10) RT_FOCK_CASE(11) RT_FOCK_CASE(13) RT_FOCK_CASE(14)
+                default: break;
+            }
+        } else {
+            switch (R.it) {
+                RT_FOCK_CASE(1) RT_FOCK_CASE(2) RT_FOCK_CASE(3) RT_FOCK_CASE(4) RT_FOCK_CASE(5)
+                RT_FOCK_CASE(6) RT_FOCK_CASE(7) RT_FOCK_CASE(8) RT_FOCK_CASE(9) RT_FOCK_CASE(10)
+                RT_FOCK_CASE(11) RT_FOCK_CASE(12) RT_FOCK_CASE(13) RT_FOCK_CASE(14)
+                default: break;
+            }
         }
+#undef RT_FOCK_CASE
     }
 }
 
 }  // namespace
 
-void launch_fock_skeleton(cudaStream_t st, const double* rint, const int* l2, const int* l1,
+void launch_fock_skeleton(cudaStream_t st, bool gaunt, const double* rint, const int* l2, const int* l1,
                           const FockRec* recs, int nrec, int nsc, int nmat, const double* dens,
                           double* fock, unsigned long long* bad) {
     if (nrec <= 0) return;
     const unsigned ntri = (unsigned)((long long)nsc * (nsc + 1) / 2);
     const int grid = nrec < 152 * 8 ? nrec : 152 * 8;
-    k_fock_skeleton<<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, (unsigned)nsc, ntri, nmat, dens, fock, bad);
+    if (gaunt)
+        k_fock_skeleton<true><<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, (unsigned)nsc, ntri, nmat, dens,
+                                                    fock, bad);
+    else
+        k_fock_skeleton<false><<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, (unsigned)nsc, ntri, nmat, dens,
+                                                     fock, bad);
 }
 
 }  // namespace rt

@@ -297,11 +297,12 @@ struct rt_ctx {
     long long out_nrec[4] = {}, out_nz[4] = {}, out_cap[4] = {};
     // caller's host buffers the next transform streams each class into
     // (rt_set_result_host): elements copied as their item chunk completes
-    // rt_fock_skeleton's work list (records of files 1..MFIL in chunks),
-    // kept while the records are unchanged (fock_gen == gen)
-    void* d_fock_chunks = nullptr;
-    long long n_fock_chunks = 0;
-    unsigned long long fock_gen = ~0ull;
+    // the Fock builds' work lists (records in chunks; [0] files 1..MFIL for
+    // rt_fock_skeleton, [1] file 4 for rt_fock_gaunt), kept while the
+    // records are unchanged (fock_gen == gen)
+    void* d_fock_chunks[2] = {nullptr, nullptr};
+    long long n_fock_chunks[2] = {0, 0};
+    unsigned long long fock_gen[2] = {~0ull, ~0ull};
     bool host_on = false;
     int* host_idx[4] = {};
     double* host_val[4] = {};

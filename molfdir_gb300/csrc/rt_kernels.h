@@ -180,9 +180,10 @@ struct FockRec {       // a chunk of one integral record of files 1..MFIL
     int it, pad;       // integral type 1..14
 };
 // fock[s][x][T] += terms of every integral of recs (nmat density sets of
-// four arrays AAR, BAR, AAI, BAI of nsc(nsc+1)/2 elements); fock must be
-// zeroed first.  A label outside 1..nsc sets *bad and the integral is skipped.
-void launch_fock_skeleton(cudaStream_t st, const double* rint, const int* l2, const int* l1,
+// four arrays AAR, BAR, AAI, BAI of nsc(nsc+1)/2 elements): FOCK's terms, or
+// with gaunt GAUNT's (types 2, 10, 11, 13, 14 only).  A label outside
+// 1..nsc sets *bad and the integral is skipped.
+void launch_fock_skeleton(cudaStream_t st, bool gaunt, const double* rint, const int* l2, const int* l1,
                           const FockRec* recs, int nrec, int nsc, int nmat, const double* dens,
                           double* fock, unsigned long long* bad);
 

@@ -86,7 +86,7 @@ EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm",
            "rt_split_dgemm_noalloc", "rt_adjoint", "rt_batch_create", "rt_batch_run",
            "rt_batch_get_stats", "rt_batch_last_error", "rt_batch_destroy", "rt_srtpq_scan",
-           "rt_read_srtpq_files", "rt_set_result_host", "rt_fock_skeleton"]
+           "rt_read_srtpq_files", "rt_set_result_host", "rt_fock_skeleton", "rt_fock_gaunt"]
 
 _lib = None
 
@@ -140,6 +140,7 @@ def load(build: bool = True):
     lib.rt_read_srtpq_files.argtypes = [vp, C.c_char_p, C.c_int]
     lib.rt_set_result_host.argtypes = [vp, P(P(C.c_int)), P(P(C.c_double)), P(C.c_longlong)]
     lib.rt_fock_skeleton.argtypes = [vp, C.c_int, vp, vp, P(C.c_double)]
+    lib.rt_fock_gaunt.argtypes = [vp, C.c_int, vp, vp, C.c_int, P(C.c_double)]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy", "rt_batch_last_error", "rt_batch_destroy"):
@@ -340,6 +341,21 @@ class Rotran:
         ms = C.c_double()
         self._check(self.lib.rt_fock_skeleton(self.h, nmat, C.c_void_p(pd), C.c_void_p(pf), C.byref(ms)))
         return out, ms.value
+
+    def fock_gaunt(self, dens, fock=None):
+        """tmoone's Gaunt contributions from the context's file-4 records
+        (``rt_fock_gaunt``), added to ``fock`` (modified in place; as MFDBREIT
+        after MFDFOCK) or, with ``fock`` None, into new zeroed sets.  Returns
+        the sets and the kernel's device milliseconds."""
+        acc = fock is not None
+        if fock is None:
+            fock = dens.new_empty(dens.shape) if hasattr(dens, "data_ptr") else np.empty_like(dens)
+        pd = dens.data_ptr() if hasattr(dens, "data_ptr") else dens.ctypes.data
+        pf = fock.data_ptr() if hasattr(fock, "data_ptr") else fock.ctypes.data
+        ms = C.c_double()
+        self._check(self.lib.rt_fock_gaunt(self.h, dens.shape[0], C.c_void_p(pd), C.c_void_p(pf),
+                                           1 if acc else 0, C.byref(ms)))
+        return fock, ms.value
 
     def headers(self):
         """The MDCINT record headers (nrec, 3) alone (``rt_copy_result`` with no element buffers)."""

@@ -141,6 +141,28 @@ def fock_skeleton(records, nsc, dens, mfil=3):
     return f
 
 
+def fock_gaunt(records, nsc, dens, fock=None):
+    """tmoone's Gaunt contributions (MFDBREIT/GAUNT) of the file-4 records,
+    added to ``fock`` (a copy; zero when None) as MFDBREIT does after MFDFOCK."""
+    lib = _load()
+    cls, its, l2, l1 = (np.ascontiguousarray(x, np.int32) for x in
+                        (records[0], records[1], records[4], records[5]))
+    nts = np.ascontiguousarray(records[2], np.int64)
+    v = np.ascontiguousarray(records[3], np.float64)
+    d = np.ascontiguousarray(dens, np.float64)
+    assert d.ndim == 3 and d.shape[1] == 4 and d.shape[2] == nsc * (nsc + 1) // 2
+    f = np.zeros_like(d) if fock is None else np.array(fock, np.float64, copy=True, order="C")
+    rc = lib.orc_fock_gaunt(C.c_long(cls.size), _ptr(cls, C.c_int), _ptr(its, C.c_int),
+                            _ptr(nts, C.c_long), _ptr(v, C.c_double), _ptr(l2, C.c_int),
+                            _ptr(l1, C.c_int), nsc, d.shape[0], 0 if fock is None else 1,
+                            _ptr(d, C.c_double), _ptr(f, C.c_double))
+    if rc == 1:
+        raise ValueError("integral label outside 1..NSC")
+    if rc == 2:
+        raise ValueError("invalid integral type for GAUNT")
+    return f
+
+
 def inttyp(a, b, c, d):
     return _load().orc_inttyp(a, b, c, d)
 

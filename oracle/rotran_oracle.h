@@ -52,6 +52,9 @@ void orc_free(orc_result* r);
 int orc_fock_skeleton(long nrec, const int* rec_file, const int* rec_it, const long* rec_nt,
                       const double* rint, const int* label2, const int* label1, int mfil, int nsc,
                       int nmat, const double* dens, double* fock);
+int orc_fock_gaunt(long nrec, const int* rec_file, const int* rec_it, const long* rec_nt,
+                   const double* rint, const int* label2, const int* label1, int nsc, int nmat,
+                   int accumulate, const double* dens, double* fock);
 
 #ifdef __cplusplus
 }

@@ -215,3 +215,96 @@ int orc_fock_skeleton(long nrec, const int* rec_file, const int* rec_it, const l
     }
     return 0;
 }
+
+/* One Gaunt integral of type it (GAUNT, source/tmoone/gaunt.F): returns 1
+ * for a type GAUNT rejects (gaunt.F:25-28, Q2JOB class 6). */
+static int gaunt_one(int it, long i, long j, long k, long l, double r, const double* d, double* f,
+                     long n) {
+    const double *daar = d, *dbar = d + n, *daai = d + 2 * n, *dbai = d + 3 * n;
+    double *faar = f, *fbar = f + n, *faai = f + 2 * n, *fbai = f + 3 * n;
+    long a, b, c, e;
+    double c1, c2, c3, c4;
+    switch (it) {
+    case 2: /* gaunt.F:41-76, I = K > J = L */
+        a = tri(i, j), b = tri(i, k), c = tri(j, l);
+        c1 = -r * daar[a] * 3.0, c2 = -r * daai[a], c3 = -r * dbar[a], c4 = -r * dbai[a];
+        faar[a] -= c1, faai[a] -= c2, fbar[a] -= c3, fbai[a] -= c4;
+        c1 = -r * daar[b] * 3.0, c2 = r * daai[b], c3 = r * dbar[b], c4 = r * dbai[b];
+        faar[c] -= c1, faai[c] -= c2, fbar[c] -= c3, fbai[c] -= c4;
+        c1 = -r * daar[c] * 3.0, c2 = r * daai[c], c3 = r * dbar[c], c4 = r * dbai[c];
+        faar[b] -= c1, faai[b] -= c2, fbar[b] -= c3, fbai[b] -= c4;
+        return 0;
+    case 10: /* gaunt.F:84-124, I = K > J > L */
+    case 11: /* gaunt.F:132-172, I > K > J = L */
+        a = tri(k, l), b = tri(i, j), c = tri(i, k), e = tri(j, l);
+        c1 = -r * daar[a] * 3.0, c2 = -r * daai[a], c3 = -r * dbar[a], c4 = -r * dbai[a];
+        faar[b] -= c1, faai[b] -= c2, fbar[b] -= c3, fbai[b] -= c4;
+        c1 = -r * daar[b] * 3.0, c2 = -r * daai[b], c3 = -r * dbar[b], c4 = -r * dbai[b];
+        faar[a] -= c1, faai[a] -= c2, fbar[a] -= c3, fbai[a] -= c4;
+        if (it == 10) {
+            faar[c] -= -r * daar[e] * 6.0;
+            /* FCABR, FCABI: FBAR -= FCABR, FBAI += FCABI */
+            c1 = -r * daar[c] * 3.0, c2 = r * daai[c], c3 = -r * dbar[c], c4 = r * dbai[c];
+            faar[e] -= c1, faai[e] -= c2, fbar[e] -= c3, fbai[e] += c4;
+        } else {
+            c1 = -r * daar[e] * 3.0, c2 = r * daai[e], c3 = r * dbar[e], c4 = -r * dbai[e];
+            faar[c] -= c1, faai[c] -= c2, fbar[c] -= c3, fbai[c] += c4;
+            faar[e] -= -r * daar[c] * 6.0;
+        }
+        return 0;
+    case 13: /* gaunt.F:180-228, I > K > J > L */
+        a = tri(i, l), b = tri(k, j), c = tri(i, k), e = tri(j, l);
+        c1 = -r * daar[b] * 3.0, c2 = -r * daai[b], c3 = -r * dbar[b], c4 = -r * dbai[b];
+        faar[a] -= c1, faai[a] -= c2, fbar[a] -= c3, fbai[a] -= c4;
+        c1 = -r * daar[a] * 3.0, c2 = -r * daai[a], c3 = -r * dbar[a], c4 = -r * dbai[a];
+        faar[b] -= c1, faai[b] -= c2, fbar[b] -= c3, fbai[b] -= c4;
+        c1 = -r * daar[e] * 3.0, c2 = r * daai[e], c3 = r * dbar[e], c4 = r * dbai[e];
+        faar[c] -= c1, faai[c] -= c2, fbar[c] -= c3, fbai[c] -= c4;
+        c1 = -r * daar[c] * 3.0, c2 = r * daai[c], c3 = r * dbar[c], c4 = r * dbai[c];
+        faar[e] -= c1, faai[e] -= c2, fbar[e] -= c3, fbai[e] -= c4;
+        return 0;
+    case 14: /* gaunt.F:236-284, I > K > L > J */
+        a = tri(i, l), b = tri(k, j), c = tri(i, k), e = tri(l, j);
+        c1 = r * daar[b] * 3.0, c2 = r * daai[b], c3 = r * dbar[b], c4 = r * dbai[b];
+        faar[a] += c1, faai[a] += c2, fbar[a] += c3, fbai[a] += c4;
+        c1 = r * daar[a] * 3.0, c2 = r * daai[a], c3 = r * dbar[a], c4 = r * dbai[a];
+        faar[b] += c1, faai[b] += c2, fbar[b] += c3, fbai[b] += c4;
+        c1 = -r * daar[e] * 3.0, c2 = -r * daai[e], c3 = -r * dbar[e], c4 = -r * dbai[e];
+        faar[c] -= c1, faai[c] -= c2, fbar[c] -= c3, fbai[c] -= c4;
+        c1 = r * daar[c] * 3.0, c2 = r * daai[c], c3 = r * dbar[c], c4 = r * dbai[c];
+        faar[e] += c1, faai[e] += c2, fbar[e] += c3, fbai[e] += c4;
+        return 0;
+    default:
+        return 1;
+    }
+}
+
+/* MFDBREIT (source/tmoone/mfdbreit.F:50-138): the Gaunt contributions of the
+ * file-4 records (SRTBREI/SRTBREL) added to the Fock sets, which are zeroed
+ * first unless accumulate (BREIT, after MFDFOCK; with ONLYBRT MFDBREIT clears
+ * them itself, mfdbreit.F:50-65).  Returns 0, 1 for a label outside 1..nsc, 2 for a type
+ * GAUNT rejects. */
+int orc_fock_gaunt(long nrec, const int* rec_file, const int* rec_it, const long* rec_nt,
+                   const double* rint, const int* label2, const int* label1, int nsc, int nmat,
+                   int accumulate, const double* dens, double* fock) {
+    const long n = (long)nsc * (nsc + 1) / 2;
+    if (!accumulate)
+        for (long x = 0; x < 4L * n * nmat; ++x) fock[x] = 0.0;
+    long off = 0;
+    for (long r = 0; r < nrec; ++r) {
+        const long nt = rec_nt[r];
+        if (rec_file[r] == 4) {
+            for (long t = 0; t < nt; ++t) {
+                const unsigned u2 = (unsigned)label2[off + t], u1 = (unsigned)label1[off + t];
+                const long i = u2 >> 16, j = u2 & 0xFFFF, k = u1 >> 16, l = u1 & 0xFFFF;
+                if (i < 1 || i > nsc || j < 1 || j > nsc || k < 1 || k > nsc || l < 1 || l > nsc)
+                    return 1;
+                for (int s = 0; s < nmat; ++s)
+                    if (gaunt_one(rec_it[r], i, j, k, l, rint[off + t], dens + 4 * n * s, fock + 4 * n * s, n))
+                        return 2;
+            }
+        }
+        off += nt;
+    }
+    return 0;
+}

@@ -105,3 +105,25 @@ def test_fock_oracle_rejects_bad_labels():
     n = p.n
     with pytest.raises(ValueError):
         pyoracle.fock_skeleton((cls, its, nts, v, l2, l1), n, np.zeros((1, 4, n * (n + 1) // 2)))
+
+
+def test_gaunt_oracle_reads_file_4_only_and_rejects_other_types():
+    p = synth.make_problem(4, 6, 3, seed=2, breit=True)
+    cls, its, nts, v, l2, l1 = p.flat_records()
+    n = p.n
+    dens, _ = densities(n, 1, 2)
+    f = pyoracle.fock_gaunt((cls, its, nts, v, l2, l1), n, dens)
+    assert np.abs(f).max() > 0
+    # without the file-4 records nothing is added
+    keep = cls != 4
+    off = np.concatenate([[0], np.cumsum(nts)])
+    sel = np.concatenate([np.arange(off[r], off[r + 1]) for r in np.nonzero(keep)[0]])
+    f0 = pyoracle.fock_gaunt((cls[keep], its[keep], nts[keep], v[sel], l2[sel], l1[sel]), n, dens)
+    assert not f0.any()
+    # linear in the integrals: scaling them scales the sets
+    f2 = pyoracle.fock_gaunt((cls, its, nts, 2.0 * v, l2, l1), n, dens)
+    assert np.allclose(f2, 2.0 * f, rtol=0, atol=1e-14 * np.abs(f).max())
+    its = its.copy()
+    its[np.nonzero(cls == 4)[0][0]] = 12
+    with pytest.raises(ValueError):
+        pyoracle.fock_gaunt((cls, its, nts, v, l2, l1), n, dens)

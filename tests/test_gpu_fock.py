@@ -27,9 +27,11 @@ def random_density(n, nmat, seed):
 
 
 def check(got, want):
+    """Per array: |got - want| <= 1e-12 of the array's largest element."""
     for s in range(want.shape[0]):
         for x in range(4):
-            scale = max(1.0, np.abs(want[s, x]).max())
+            scale = np.abs(want[s, x]).max()
+            assert scale > 0, (s, x)
             err = np.abs(got[s, x] - want[s, x]).max()
             assert err <= TOL * scale, (s, x, err, scale)
 
@@ -91,3 +93,39 @@ def test_label_outside_nsc_is_refused():
         with pytest.raises(rotran.RotranError) as e:
             rt.fock_skeleton(random_density(p.n, 1, 0))
         assert e.value.code == rotran.RT_ERR_USER and "label" in str(e.value)
+
+
+# ---- tmoone's Gaunt contributions (MFDBREIT/GAUNT) ----
+
+@pytest.mark.parametrize("nl,ns,nkr,seed,nmat", [(3, 4, 2, 0, 1), (6, 9, 3, 1, 2), (12, 20, 4, 2, 1),
+                                                 (24, 40, 4, 3, 2)])
+def test_gaunt_contributions_match_the_oracle(nl, ns, nkr, seed, nmat):
+    """ONLYBRT (zeroed sets) and BREIT (added to MFDFOCK's sets)."""
+    p = synth.make_problem(nl, ns, nkr, seed=seed, breit=True)
+    recs = p.flat_records()
+    dens = random_density(p.n, nmat, seed)
+    coul = pyoracle.fock_skeleton(recs, p.n, dens, mfil=p.mfil)
+    only = pyoracle.fock_gaunt(recs, p.n, dens)
+    both = pyoracle.fock_gaunt(recs, p.n, dens, fock=coul)
+    assert np.abs(only).max() > 0
+    with rotran.Rotran.for_problem(p) as rt:   # a Coulomb context also holds file 4
+        rt.add_problem_records(p)
+        got_only, ms = rt.fock_gaunt(dens)
+        f, _ = rt.fock_skeleton(dens)
+        got_both, _ = rt.fock_gaunt(dens, f)
+    assert ms > 0
+    check(got_only, only)
+    check(got_both, both)
+
+
+def test_gaunt_refuses_the_types_gaunt_rejects():
+    p = synth.make_problem(3, 4, 2, seed=0, breit=True)
+    cls, its, nts, v, l2, l1 = p.flat_records()
+    its = its.copy()
+    its[np.nonzero(cls == 4)[0][0]] = 12
+    with rotran.Rotran.for_problem(p) as rt:
+        rt.add_records_bulk(cls, nts, its, v, l2, l1)
+        with pytest.raises(rotran.RotranError) as e:
+            rt.fock_gaunt(random_density(p.n, 1, 0))
+        assert e.value.code == rotran.RT_ERR_PROGRAM and "INVALID TYPE IN BREIT" in str(e.value)
+        rt.fock_skeleton(random_density(p.n, 1, 0))   # FOCK takes type 12
