@@ -163,6 +163,22 @@ int rt_srtpq_scan(const char* dir, int nranks, int nsc, int nsc1, long long cap,
 /* Drop all records added so far (a new integral set, same sizes). */
 int rt_clear_ao_records(rt_ctx* ctx);
 
+/* Queue the next record set (arguments as rt_add_ao_records_bulk) so that
+ * its host->device copies overlap the next rt_transform: that call reads the
+ * current records during its bucketing, then copies the queued ones into
+ * the record arrays on streams of their own while its half-transformations
+ * run, and returns with the queued set as the context's records (whatever
+ * its outcome); its results are those of the records it started with.  The
+ * arrays are borrowed until that rt_transform returns (pinned host memory
+ * copies asynchronously).  Any other call that reads or changes the records
+ * (rt_add_*, rt_clear_ao_records, rt_read_*, rt_adjoint, rt_fock_*,
+ * rt_batch_create, a second rt_queue_ao_records_bulk) first makes the queued
+ * set current synchronously; rt_batch_run refuses a context with a set
+ * queued (RT_ERR_MISMATCH).  (No counterpart in the reference, which reads
+ * its integral files once per run.) */
+int rt_queue_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* file_class, const long long* nt,
+                             const int* itype, const double* rint, const int* label2, const int* label1);
+
 /* Run the transformation: first half (TRANS1), sort/transpose, second half
  * (TRANS2) and particle-particle completion (PPSYM); the MDCINT records stay
  * in device memory until copied or written. */

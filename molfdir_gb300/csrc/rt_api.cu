@@ -650,6 +650,68 @@ static void sync_pieces(rt_ctx* c) {
         if (s) RT_CUDA(cudaStreamSynchronize(s));
 }
 
+// ---- the queued next record set (rt_queue_ao_records_bulk) ----
+// Its copies go into the record arrays at offset 0 on the prefetch streams,
+// which only rt_transform issues while it runs (after its bucketing, the last
+// reader of the current records); every other call that touches the records
+// applies the queue first.
+static void rq_issue(rt_ctx* c) {
+    auto& q = c->rq;
+    if (!q.pending || q.issued) return;
+    const int ns = (int)(sizeof(c->pstream) / sizeof(c->pstream[0]));
+    if (!c->pstream[0])
+        for (int i = 0; i < ns; ++i) RT_CUDA(cudaStreamCreateWithFlags(&c->pstream[i], cudaStreamNonBlocking));
+    if (q.tot > c->cap_int) throw Error(RT_ERR_INTERNAL, "queued records exceed the record arrays");
+    auto pieces = [&](void* dst, const void* src, size_t bytes, int& k) {
+        const size_t piece = std::max<size_t>((size_t)64 << 20, (bytes + ns - 1) / ns);
+        for (size_t o = 0; o < bytes; o += piece, ++k)
+            RT_CUDA(cudaMemcpyAsync((char*)dst + o, (const char*)src + o, std::min(piece, bytes - o),
+                                    cudaMemcpyDefault, c->pstream[k % ns]));
+    };
+    int k = 0;
+    if (q.tot > 0) {
+        pieces(c->d_rint, q.rint, q.tot * sizeof(double), k);
+        pieces(c->d_l2, q.l2, q.tot * sizeof(int), k);
+        pieces(c->d_l1, q.l1, q.tot * sizeof(int), k);
+    }
+    q.issued = true;
+}
+
+// Wait for the queued copies and make the queued set the context's records.
+// Returns the first CUDA error of the wait (the records are then undefined).
+static cudaError_t rq_finish(rt_ctx* c) noexcept {
+    auto& q = c->rq;
+    if (!q.pending) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    for (auto s : c->pstream)
+        if (s) {
+            const cudaError_t x = cudaStreamSynchronize(s);
+            if (e == cudaSuccess) e = x;
+        }
+    c->rec_file = std::move(q.file);
+    c->rec_it = std::move(q.it);
+    c->rec_nt = std::move(q.nt);
+    c->rec_off.resize(c->rec_nt.size());
+    long long off = 0;
+    for (size_t r = 0; r < c->rec_nt.size(); ++r) {
+        c->rec_off[r] = off;
+        off += c->rec_nt[r];
+    }
+    c->n_int = q.tot;
+    q = rt_ctx::RecordQueue();
+    ++c->gen;
+    return e;
+}
+
+// Any call other than rt_transform that reads or changes the records
+// applies a queued set first, synchronously.
+static void rq_apply(rt_ctx* c) {
+    if (!c->rq.pending) return;
+    rq_issue(c);
+    const cudaError_t e = rq_finish(c);
+    if (e != cudaSuccess) throw Error(RT_ERR_PROGRAM, std::string("queued record copies: ") + cudaGetErrorString(e));
+}
+
 static void add_record_meta(rt_ctx* c, int file, int it, long long nt, long long off) {
     c->rec_file.push_back(file);
     c->rec_it.push_back(it);
@@ -664,6 +726,7 @@ extern "C" int rt_add_ao_records(rt_ctx* ctx, int file_class, int nt, int itype,
     if (nt < 0) throw Error(RT_ERR_USER, "negative record length");
     if (file_class < 1 || file_class > 4) throw Error(RT_ERR_USER, "file class must be 1..4");
     if (nt > 0 && (!rint || !label2 || !label1)) throw Error(RT_ERR_USER, "null record arrays");
+    rq_apply(ctx);
     long long off = ctx->n_int + (long long)ctx->st_v.size();
     add_record_meta(ctx, file_class, itype, nt, off);
     ctx->st_v.insert(ctx->st_v.end(), rint, rint + nt);
@@ -687,6 +750,7 @@ extern "C" int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* fi
         if (file_class[r] < 1 || file_class[r] > 4) throw Error(RT_ERR_USER, "file class must be 1..4");
         tot += nt[r];
     }
+    rq_apply(ctx);
     flush_staged(ctx);
     long long off = ctx->n_int;
     for (long long r = 0; r < nrec; ++r) {
@@ -707,9 +771,40 @@ extern "C" int rt_add_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* fi
     API_CATCH
 }
 
+extern "C" int rt_queue_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* file_class,
+                                       const long long* nt, const int* itype, const double* rint,
+                                       const int* label2, const int* label1) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    if (nrec < 0) throw Error(RT_ERR_USER, "negative record count");
+    if (nrec > 0 && (!file_class || !nt || !itype)) throw Error(RT_ERR_USER, "null record tables");
+    long long tot = 0;
+    for (long long r = 0; r < nrec; ++r) {
+        if (nt[r] < 0) throw Error(RT_ERR_USER, "negative record length");
+        if (file_class[r] < 1 || file_class[r] > 4) throw Error(RT_ERR_USER, "file class must be 1..4");
+        tot += nt[r];
+    }
+    if (tot > 0 && (!rint || !label2 || !label1)) throw Error(RT_ERR_USER, "null record arrays");
+    rq_apply(ctx);  // a set queued before and not yet transformed
+    flush_staged(ctx);
+    ensure_record_capacity(ctx, tot);  // keeps the current records
+    auto& q = ctx->rq;
+    q.file.assign(file_class, file_class + nrec);
+    q.it.assign(itype, itype + nrec);
+    q.nt.assign(nt, nt + nrec);
+    q.tot = tot;
+    q.rint = rint;
+    q.l2 = label2;
+    q.l1 = label1;
+    q.issued = false;
+    q.pending = true;
+    API_CATCH
+}
+
 extern "C" int rt_clear_ao_records(rt_ctx* ctx) {
     if (!ctx) return RT_ERR_USER;
     API_TRY
+    rq_apply(ctx);
     ctx->n_int = 0;
     ctx->st_v.clear();
     ctx->st_l2.clear();
@@ -1168,6 +1263,19 @@ double algorithmic_flops(const Plan& P, bool breit) { return algorithmic_flops(P
 
 extern "C" int rt_transform(rt_ctx* ctx) {
     if (!ctx) return RT_ERR_USER;
+    // a queued record set becomes the context's records when this call
+    // returns, whatever its outcome (its copies start after the bucketing)
+    struct QueueGuard {
+        rt_ctx* c;
+        ~QueueGuard() {
+            if (!c->rq.pending) return;
+            try {
+                rq_issue(c);
+            } catch (...) {
+            }
+            if (rq_finish(c) != cudaSuccess) c->unusable = true;
+        }
+    } queue_guard{ctx};
     API_TRY
     if (ctx->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
     if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
@@ -1202,6 +1310,10 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     // ---- sort the records into pq buckets (SORT1) ----
     pass_bucketing(ps, uses_halves(ctx));
     RT_CUDA(cudaEventRecord(ctx->ev[2], st));
+    if (ctx->rq.pending) {  // the raw records are read no more: the next set's copies overlap the rest
+        rq_issue(ctx);
+        tr.mark("next records queued");
+    }
     // ---- stage A: first half-transformation (TRANS1) per pair chunk ----
     pass_stage_a(ps, ctx->cfg.thrgen);
     RT_CUDA(cudaEventRecord(ctx->ev[3], st));
@@ -1439,6 +1551,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     if (ctx->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
     if (ctx->cfg.breit) throw Error(RT_ERR_USER, "the adjoint is built for the Coulomb transformation");
     if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
+    rq_apply(ctx);
     Plan& P = ctx->plan;
     cudaStream_t st = ctx->stream;
     const int n = P.n, m = P.m;
@@ -1832,6 +1945,7 @@ extern "C" int rt_batch_create(rt_batch** out, rt_ctx* const* ctxs, int count) {
             rt_ctx* c = ctxs[i];
             if (!c) throw Error(RT_ERR_USER, "null context in batch");
             if (c->device != B->device) throw Error(RT_ERR_USER, "batch contexts on different devices");
+            rq_apply(c);
             if (!c->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
             if (c->cfg.breit) throw Error(RT_ERR_USER, "batched transforms are Coulomb only");
             if (c->cfg.half_buckets)
@@ -1999,7 +2113,7 @@ extern "C" int rt_batch_run(rt_batch* b) {
     try {
         for (BatchInst& I : b->inst) {
             if (I.c->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
-            if (I.c->gen != I.gen)
+            if (I.c->gen != I.gen || I.c->rq.pending)
                 throw Error(RT_ERR_MISMATCH, "a context of the batch changed after rt_batch_create");
         }
         // tile widths from the cache when every stage's shape is in it
@@ -2169,6 +2283,7 @@ void fock_pass(rt_ctx* ctx, bool gaunt, int nmat, const double* dens, double* fo
     if (!dens || !fock) throw Error(RT_ERR_USER, "Fock build: null density or Fock arrays");
     if (ctx->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
     cudaStream_t st = ctx->stream;
+    rq_apply(ctx);
     flush_staged(ctx);
     const int w = gaunt ? 1 : 0;
     if (ctx->fock_gen[w] != ctx->gen) {
@@ -2321,6 +2436,11 @@ extern "C" const char* rt_last_error(rt_ctx* ctx) {
 extern "C" void rt_destroy(rt_ctx* ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto s : ctx->pstream)
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
     for (auto s : ctx->cstream)
         if (s) {
             cudaStreamSynchronize(s);

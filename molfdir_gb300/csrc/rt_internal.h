@@ -248,6 +248,18 @@ struct rt_ctx {
     double* d_rint = nullptr;
     int* d_l2 = nullptr;
     int* d_l1 = nullptr;
+    // the next record set queued by rt_queue_ao_records_bulk: host arrays
+    // borrowed until the rt_transform that copies them returns
+    struct RecordQueue {
+        bool pending = false, issued = false;
+        std::vector<int> file, it;
+        std::vector<long long> nt;
+        long long tot = 0;
+        const double* rint = nullptr;
+        const int* l2 = nullptr;
+        const int* l1 = nullptr;
+    } rq;
+    cudaStream_t pstream[4] = {};  // the queued records' copies
     // staging for per-record calls
     std::vector<double> st_v;
     std::vector<int> st_l2, st_l1;

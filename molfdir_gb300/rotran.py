@@ -86,7 +86,8 @@ EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_get_stats", "rt_last_error", "rt_destroy", "rt_kramers_check", "rt_split_dgemm",
            "rt_split_dgemm_noalloc", "rt_adjoint", "rt_batch_create", "rt_batch_run",
            "rt_batch_get_stats", "rt_batch_last_error", "rt_batch_destroy", "rt_srtpq_scan",
-           "rt_read_srtpq_files", "rt_set_result_host", "rt_fock_skeleton", "rt_fock_gaunt"]
+           "rt_read_srtpq_files", "rt_set_result_host", "rt_fock_skeleton", "rt_fock_gaunt",
+           "rt_queue_ao_records_bulk"]
 
 _lib = None
 
@@ -141,6 +142,7 @@ def load(build: bool = True):
     lib.rt_set_result_host.argtypes = [vp, P(P(C.c_int)), P(P(C.c_double)), P(C.c_longlong)]
     lib.rt_fock_skeleton.argtypes = [vp, C.c_int, vp, vp, P(C.c_double)]
     lib.rt_fock_gaunt.argtypes = [vp, C.c_int, vp, vp, C.c_int, P(C.c_double)]
+    lib.rt_queue_ao_records_bulk.argtypes = lib.rt_add_ao_records_bulk.argtypes
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy", "rt_batch_last_error", "rt_batch_destroy"):
@@ -279,6 +281,19 @@ class Rotran:
         n = np.ascontiguousarray(nt, np.int64)
         it = np.ascontiguousarray(itype, np.int32)
         self._check(self.lib.rt_add_ao_records_bulk(
+            self.h, int(fc.size), _p(fc, C.c_int), _p(n, C.c_longlong), _p(it, C.c_int),
+            C.cast(C.c_void_p(p_rint), C.POINTER(C.c_double)),
+            C.cast(C.c_void_p(p_label2), C.POINTER(C.c_int)),
+            C.cast(C.c_void_p(p_label1), C.POINTER(C.c_int))))
+
+    def queue_records_bulk_ptr(self, file_class, nt, itype, p_rint, p_label2, p_label1):
+        """Queue the next record set (``rt_queue_ao_records_bulk``): its copies
+        overlap the next ``transform()``, after which it is the context's
+        records.  The arrays behind the pointers must stay alive until then."""
+        fc = np.ascontiguousarray(file_class, np.int32)
+        n = np.ascontiguousarray(nt, np.int64)
+        it = np.ascontiguousarray(itype, np.int32)
+        self._check(self.lib.rt_queue_ao_records_bulk(
             self.h, int(fc.size), _p(fc, C.c_int), _p(n, C.c_longlong), _p(it, C.c_int),
             C.cast(C.c_void_p(p_rint), C.POINTER(C.c_double)),
             C.cast(C.c_void_p(p_label2), C.POINTER(C.c_int)),
