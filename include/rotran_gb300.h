@@ -181,7 +181,9 @@ int rt_queue_ao_records_bulk(rt_ctx* ctx, long long nrec, const int* file_class,
 
 /* Run the transformation: first half (TRANS1), sort/transpose, second half
  * (TRANS2) and particle-particle completion (PPSYM); the MDCINT records stay
- * in device memory until copied or written. */
+ * in device memory until copied or written.  The previous result is
+ * replaced: after a failed call there is none (rt_result_sizes,
+ * rt_copy_result and rt_write_mdcint fail with RT_ERR_USER). */
 int rt_transform(rt_ctx* ctx);
 
 /* Adjoint of the transformation (no counterpart in the reference, which

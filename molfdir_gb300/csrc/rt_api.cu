@@ -1279,6 +1279,9 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     API_TRY
     if (ctx->unusable) throw Error(RT_ERR_PROGRAM, UNUSABLE_MSG);
     if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
+    // the result arrays are rewritten from here on: an earlier result is
+    // gone, and a transform that fails leaves none
+    ctx->transformed = false;
     Plan& P = ctx->plan;
     Work& w = W(ctx);
     cudaStream_t st = ctx->stream;
@@ -2116,6 +2119,7 @@ extern "C" int rt_batch_run(rt_batch* b) {
             if (I.c->gen != I.gen || I.c->rq.pending)
                 throw Error(RT_ERR_MISMATCH, "a context of the batch changed after rt_batch_create");
         }
+        for (BatchInst& I : b->inst) I.c->transformed = false;  // rewritten from here on
         // tile widths from the cache when every stage's shape is in it
         const char* cache = std::getenv("RT_TUNE_CACHE");
         bool cached = false;

@@ -81,6 +81,8 @@ def test_too_small_class_buffer_fails_and_the_context_recovers():
         with pytest.raises(rotran.RotranError) as e:
             rt.transform()
         assert e.value.code == rotran.RT_ERR_DIM and f"class {big + 1}" in str(e.value)
+        with pytest.raises(rotran.RotranError):   # the failed transform left no result
+            rt.result()
         rt.set_result_host()
         rt.transform()
         again = rt.result()
