@@ -1269,6 +1269,9 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         rt_ctx* c;
         ~QueueGuard() {
             if (!c->rq.pending) return;
+            // a call that ended early may still have bucketing kernels
+            // reading the current records: they finish before the copies
+            if (!c->rq.issued && cudaStreamSynchronize(c->stream) != cudaSuccess) c->unusable = true;
             try {
                 rq_issue(c);
             } catch (...) {
