@@ -284,6 +284,16 @@ int rt_copy_result(rt_ctx* ctx, int* hdr, int* idx, double* val);
  * class 3.  NULL idx or val unregisters. */
 int rt_set_result_host(rt_ctx* ctx, int* const* idx, double* const* val, const long long* cap);
 
+/* With deferred = 1, rt_transform returns before the copies of its last
+ * item chunk into the registered buffers have landed; they finish while the
+ * caller (or the next rt_transform's first half, which never writes the
+ * results) runs.  rt_result_host_wait waits for them; so do rt_copy_result,
+ * rt_write_mdcint, rt_set_result_host, rt_set_result_host_deferred,
+ * rt_adjoint, rt_batch_run and the next rt_transform before it writes
+ * results again.  Default 0: rt_transform returns with every copy done. */
+int rt_set_result_host_deferred(rt_ctx* ctx, int deferred);
+int rt_result_host_wait(rt_ctx* ctx);
+
 /* Write MDCINT (inittwoe.F:1-25, ppsym.F:89-91, exittwoe.F:1-10) as
  * a gfortran sequential unformatted file. */
 int rt_write_mdcint(rt_ctx* ctx, const char* path, const char* datex10, const char* timex8);

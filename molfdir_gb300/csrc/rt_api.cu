@@ -712,6 +712,14 @@ static void rq_apply(rt_ctx* c) {
     if (e != cudaSuccess) throw Error(RT_ERR_PROGRAM, std::string("queued record copies: ") + cudaGetErrorString(e));
 }
 
+// The host copies of an earlier transform's elements (deferred mode)
+// complete before anything rewrites or hands out its results.
+static void host_result_wait(rt_ctx* c) {
+    if (!c->host_inflight) return;
+    c->host_inflight = false;
+    RT_CUDA(cudaStreamSynchronize(c->cstream[0]));
+}
+
 static void add_record_meta(rt_ctx* c, int file, int it, long long nt, long long off) {
     c->rec_file.push_back(file);
     c->rec_it.push_back(it);
@@ -1325,6 +1333,7 @@ extern "C" int rt_transform(rt_ctx* ctx) {
     RT_CUDA(cudaEventRecord(ctx->ev[3], st));
     tr.mark("stage A tail");
     // ---- stage B: second half-transformation (TRANS2) + PPSYM per item chunk ----
+    host_result_wait(ctx);  // the previous transform's copies (they overlapped stage A)
     double* m3 = ctx->d_ha;
     int ncmax = std::max(P.ncomp[0], P.ncomp[1]);
     const bool breit = ctx->cfg.breit != 0, halves = uses_halves(ctx);
@@ -1468,7 +1477,9 @@ extern "C" int rt_transform(rt_ctx* ctx) {
         tr.mark("B: records from both halves");
         stream_out();
     }
-    if (to_host) {
+    if (to_host && ctx->host_defer) {
+        ctx->host_inflight = true;  // completed by rt_result_host_wait or the next user of the results
+    } else if (to_host) {
         RT_CUDA(cudaStreamSynchronize(ctx->cstream[0]));
         tr.mark("B: last result copies");
     }
@@ -1558,6 +1569,7 @@ extern "C" int rt_adjoint(rt_ctx* ctx, const double* gamma, double* dedc, double
     if (ctx->cfg.breit) throw Error(RT_ERR_USER, "the adjoint is built for the Coulomb transformation");
     if (!ctx->have_coef) throw Error(RT_ERR_USER, "rt_set_coefficients has not been called");
     rq_apply(ctx);
+    host_result_wait(ctx);
     Plan& P = ctx->plan;
     cudaStream_t st = ctx->stream;
     const int n = P.n, m = P.m;
@@ -2122,7 +2134,10 @@ extern "C" int rt_batch_run(rt_batch* b) {
             if (I.c->gen != I.gen || I.c->rq.pending)
                 throw Error(RT_ERR_MISMATCH, "a context of the batch changed after rt_batch_create");
         }
-        for (BatchInst& I : b->inst) I.c->transformed = false;  // rewritten from here on
+        for (BatchInst& I : b->inst) {
+            host_result_wait(I.c);
+            I.c->transformed = false;  // rewritten from here on
+        }
         // tile widths from the cache when every stage's shape is in it
         const char* cache = std::getenv("RT_TUNE_CACHE");
         bool cached = false;
@@ -2377,9 +2392,25 @@ extern "C" int rt_fock_gaunt(rt_ctx* ctx, int nmat, const double* dens, double* 
     API_CATCH
 }
 
+extern "C" int rt_set_result_host_deferred(rt_ctx* ctx, int deferred) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    host_result_wait(ctx);
+    ctx->host_defer = deferred != 0;
+    API_CATCH
+}
+
+extern "C" int rt_result_host_wait(rt_ctx* ctx) {
+    if (!ctx) return RT_ERR_USER;
+    API_TRY
+    host_result_wait(ctx);
+    API_CATCH
+}
+
 extern "C" int rt_set_result_host(rt_ctx* ctx, int* const* idx, double* const* val, const long long* cap) {
     if (!ctx) return RT_ERR_USER;
     API_TRY
+    host_result_wait(ctx);
     ctx->host_on = false;
     const bool on = idx && val;
     for (int c = 0; on && c < 4; ++c)
@@ -2397,6 +2428,7 @@ extern "C" int rt_set_result_host(rt_ctx* ctx, int* const* idx, double* const* v
 extern "C" int rt_copy_result(rt_ctx* ctx, int* hdr, int* idx, double* val) {
     if (!ctx) return RT_ERR_USER;
     API_TRY
+    host_result_wait(ctx);
     if (!ctx->transformed) throw Error(RT_ERR_USER, "no transform result");
     Work& w = W(ctx);
     // every class stream's copies first, one synchronisation

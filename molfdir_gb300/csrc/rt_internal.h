@@ -316,6 +316,8 @@ struct rt_ctx {
     long long n_fock_chunks[2] = {0, 0};
     unsigned long long fock_gen[2] = {~0ull, ~0ull};
     bool host_on = false;
+    bool host_defer = false;     // rt_transform returns before its last copies land
+    bool host_inflight = false;  // copies of the last transform still on cstream[0]
     int* host_idx[4] = {};
     double* host_val[4] = {};
     long long host_cap[4] = {};

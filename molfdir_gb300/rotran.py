@@ -87,7 +87,7 @@ EXPORTS = ["rt_plan", "rt_create", "rt_set_coefficients", "rt_add_ao_records",
            "rt_split_dgemm_noalloc", "rt_adjoint", "rt_batch_create", "rt_batch_run",
            "rt_batch_get_stats", "rt_batch_last_error", "rt_batch_destroy", "rt_srtpq_scan",
            "rt_read_srtpq_files", "rt_set_result_host", "rt_fock_skeleton", "rt_fock_gaunt",
-           "rt_queue_ao_records_bulk"]
+           "rt_queue_ao_records_bulk", "rt_set_result_host_deferred", "rt_result_host_wait"]
 
 _lib = None
 
@@ -143,6 +143,8 @@ def load(build: bool = True):
     lib.rt_fock_skeleton.argtypes = [vp, C.c_int, vp, vp, P(C.c_double)]
     lib.rt_fock_gaunt.argtypes = [vp, C.c_int, vp, vp, C.c_int, P(C.c_double)]
     lib.rt_queue_ao_records_bulk.argtypes = lib.rt_add_ao_records_bulk.argtypes
+    lib.rt_set_result_host_deferred.argtypes = [vp, C.c_int]
+    lib.rt_result_host_wait.argtypes = [vp]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("rt_last_error", "rt_destroy", "rt_batch_last_error", "rt_batch_destroy"):
@@ -403,6 +405,14 @@ class Rotran:
         cp = (C.c_longlong * 4)(*caps)
         self._host = (list(idx), list(val))
         self._check(self.lib.rt_set_result_host(self.h, ip, dp, cp))
+
+    def set_result_host_deferred(self, deferred=True):
+        """``rt_set_result_host_deferred``: transform() returns before its last
+        host copies land; ``result_host_wait()`` (or any result read) completes them."""
+        self._check(self.lib.rt_set_result_host_deferred(self.h, 1 if deferred else 0))
+
+    def result_host_wait(self):
+        self._check(self.lib.rt_result_host_wait(self.h))
 
     def write_mdcint(self, path, datex="", timex=""):
         self._check(self.lib.rt_write_mdcint(self.h, os.fsencode(path), datex.encode()[:10],

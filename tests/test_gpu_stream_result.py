@@ -105,3 +105,34 @@ def test_pageable_buffers_stream_too():
         rt.transform()
         sidx, sval = streamed(hidx, hval, sizes)
         assert np.array_equal(sidx, idx) and np.array_equal(sval, val)
+
+
+def test_deferred_copies_complete_before_results_are_reused():
+    """Deferred mode: the last copies land by rt_result_host_wait, by a result
+    read, or before the next transform writes results again."""
+    p = synth.make_problem(12, 20, 10, seed=6)
+    with rotran.Rotran.for_problem(p, precision=SPLIT) as rt:
+        rt.set_problem_coefficients(p)
+        rt.add_problem_records(p)
+        rt.transform()
+        hdr, idx, val = rt.result()
+        sizes = [int(x) for x in rt.stats().nfinal]
+        keep, hidx, hval = pinned_class_buffers(sizes)
+        rt.set_result_host(hidx, hval)
+        rt.set_result_host_deferred(True)
+        for wait in ("explicit", "headers", "next transform"):
+            for x in hidx + hval:
+                x.fill(0)
+            rt.transform()
+            if wait == "explicit":
+                rt.result_host_wait()
+            elif wait == "headers":
+                assert np.array_equal(rt.headers(), hdr)
+            else:
+                rt.transform()   # waits before its second half, then streams again
+                rt.result_host_wait()
+            sidx, sval = streamed(hidx, hval, sizes)
+            assert np.array_equal(sidx, idx), wait
+            assert np.array_equal(sval.view(np.float64), val.view(np.float64)), wait
+        rt.set_result_host_deferred(False)
+        del keep
