@@ -111,3 +111,23 @@ def test_a_larger_set_and_a_failed_transform(problems):
         del keep
         rt.transform()
         assert compare_streams(rt.result(), (ib.hdr, ib.idx, ib.val), 1e-10) <= 1e-10
+
+
+def test_queued_gaunt_records():
+    """The Gaunt transform (file 4 only) with a queued set."""
+    pa = synth.make_problem(6, 9, 4, seed=11, breit=True)
+    pb = synth.make_problem(6, 9, 4, seed=12, breit=True)
+    ra, rb = pa.flat_records(), pb.flat_records()
+    ia = pyoracle.run(pa, breit=True)
+    ib = pyoracle.run(pa, records=rb, breit=True)
+    with rotran.Rotran.for_problem(pa, precision=SPLIT, breit=True) as rt:
+        rt.set_problem_coefficients(pa)
+        rt.add_records_bulk(ra[0], ra[2], ra[1], ra[3], ra[4], ra[5])
+        keep = queue(rt, rb)
+        rt.transform()
+        got_a = rt.result()
+        del keep
+        rt.transform()
+        got_b = rt.result()
+    assert compare_streams(got_a, (ia.hdr, ia.idx, ia.val), 1e-10) <= 1e-10
+    assert compare_streams(got_b, (ib.hdr, ib.idx, ib.val), 1e-10) <= 1e-10
