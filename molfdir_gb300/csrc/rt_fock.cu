@@ -291,7 +291,9 @@ void launch_fock_skeleton(cudaStream_t st, bool gaunt, const double* rint, const
                           double* fock, unsigned long long* bad) {
     if (nrec <= 0) return;
     const unsigned ntri = (unsigned)((long long)nsc * (nsc + 1) / 2);
-    const int grid = nrec < 152 * 8 ? nrec : 152 * 8;
+    // as many blocks as are resident (four per SM at 256 threads and 62-64
+    // registers): a second wave would leave SMs idle at the end
+    const int grid = nrec < 152 * 4 ? nrec : 152 * 4;
     if (gaunt)
         k_fock_skeleton<true><<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, (unsigned)nsc, ntri, nmat, dens,
                                                     fock, bad);
