@@ -220,12 +220,13 @@ def cpu_sample(work, steps=1, warmup=0, seconds=15.0):
 
 
 def run_gemm_case(args, rank):
-    """One split GEMM of the shape of the second and fourth quarter steps at
-    n = 400, 120 Kramers pairs (M = 2m = 480, K = 2n = 800), N = 32768, for
-    kernel profiling (float-float operands sliced on the device, 6 slices)."""
+    """One split GEMM of the shape of the second and fourth quarter steps, for
+    kernel profiling (float-float operands sliced on the device): by default
+    n = 400, 120 Kramers pairs (M = 2m = 480, K = 2n = 800), N = 32768;
+    ``--gemm-shape 800,960,32768`` gives the n = 480, 200 Kramers pair shape."""
     from molfdir_gb300 import rotran
     rng = np.random.default_rng(0)
-    m_, k_, n_ = 480, 800, 32768
+    m_, k_, n_ = (int(x) for x in args.gemm_shape.split(","))
     a = rng.standard_normal((m_, k_))
     b = rng.standard_normal((k_, n_))
     for _ in range(max(1, args.steps)):
@@ -233,7 +234,7 @@ def run_gemm_case(args, rank):
         rotran.split_dgemm(a, b, slices=args.slices, mode=1)
         dt = time.perf_counter() - t0
     if rank == 0:
-        print(json.dumps({"workload": "gemm_m480_k800_n32768", "slices": args.slices,
+        print(json.dumps({"workload": f"gemm_m{m_}_k{k_}_n{n_}", "slices": args.slices,
                           "seconds_per_call_with_host_work": dt}))
 
 
@@ -600,6 +601,8 @@ def main():
     ap.add_argument("--workload", default="precision",
                     choices=["precision", "c1", "profile", "profile2", "large", "batched", "gemm", "files",
                              "breit", "fock", "fock_small"])
+    ap.add_argument("--gemm-shape", default="480,800,32768",
+                    help="M,K,N of --workload gemm")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
