@@ -201,9 +201,9 @@ __device__ __forceinline__ void add_term(int x, bool on, bool uniform, int lane,
     }
 }
 
-template <bool G, int IT, int Q>
+template <bool G, int NM, int IT, int Q>
 __device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsigned k, unsigned l,
-                                           const Multiples& w, int lane, int leader, int nmat, unsigned ntri,
+                                           const Multiples& w, int lane, int leader, unsigned ntri,
                                            const double* __restrict__ dens, double* __restrict__ fock) {
     if constexpr (Q < nterm_of<G>(IT)) {
         constexpr FockTerm m = term_of<G>(IT, Q);
@@ -211,7 +211,8 @@ __device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsi
         const unsigned sr = tri0(pick<m.sx>(i, j, k, l), pick<m.sy>(i, j, k, l));
         const unsigned tg0 = __shfl_sync(0xffffffffu, tg, leader);
         const bool uniform = __all_sync(0xffffffffu, !on || tg == tg0);
-        for (int s = 0; s < nmat; ++s) {
+#pragma unroll
+        for (int s = 0; s < NM; ++s) {
             const double* d = dens + (size_t)s * 4 * ntri;
             double* f = fock + (size_t)s * 4 * ntri;
             add_term<m.c[0]>(0, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
@@ -219,15 +220,15 @@ __device__ __forceinline__ void fock_terms(bool on, unsigned i, unsigned j, unsi
             add_term<m.c[2]>(2, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
             add_term<m.c[3]>(3, on, uniform, lane, leader, w, d, f, ntri, sr, tg, tg0);
         }
-        fock_terms<G, IT, Q + 1>(on, i, j, k, l, w, lane, leader, nmat, ntri, dens, fock);
+        fock_terms<G, NM, IT, Q + 1>(on, i, j, k, l, w, lane, leader, ntri, dens, fock);
     }
 }
 
 // the integrals of one record chunk, all of type IT (G: GAUNT's terms)
-template <bool G, int IT>
+template <bool G, int NM, int IT>
 __device__ __forceinline__ void fock_chunk(const FockRec& R, const double* __restrict__ rint,
                                            const int* __restrict__ l2, const int* __restrict__ l1,
-                                           unsigned nsc, unsigned ntri, int nmat,
+                                           unsigned nsc, unsigned ntri,
                                            const double* __restrict__ dens, double* __restrict__ fock,
                                            unsigned long long* __restrict__ bad) {
     const int lane = threadIdx.x & 31;
@@ -250,23 +251,23 @@ __device__ __forceinline__ void fock_chunk(const FockRec& R, const double* __res
         const unsigned on_mask = __ballot_sync(0xffffffffu, on);
         if (on_mask == 0) continue;
         const Multiples w{v, 3.0 * v};   // 3v is made only where a type uses it
-        fock_terms<G, IT, 0>(on, i, j, k, l, w, lane, __ffs(on_mask) - 1, nmat, ntri, dens, fock);
+        fock_terms<G, NM, IT, 0>(on, i, j, k, l, w, lane, __ffs(on_mask) - 1, ntri, dens, fock);
     }
 }
 
-template <bool G>
+template <bool G, int NM>
 __global__ void __launch_bounds__(256) k_fock_skeleton(const double* __restrict__ rint,
                                                        const int* __restrict__ l2,
                                                        const int* __restrict__ l1,
                                                        const FockRec* __restrict__ recs, int nrec,
-                                                       unsigned nsc, unsigned ntri, int nmat,
+                                                       unsigned nsc, unsigned ntri,
                                                        const double* __restrict__ dens,
                                                        double* __restrict__ fock,
                                                        unsigned long long* __restrict__ bad) {
     for (int r = blockIdx.x; r < nrec; r += gridDim.x) {
         const FockRec R = recs[r];
 #define RT_FOCK_CASE(T) \
-    case T: fock_chunk<G, T>(R, rint, l2, l1, nsc, ntri, nmat, dens, fock, bad); break;
+    case T: fock_chunk<G, NM, T>(R, rint, l2, l1, nsc, ntri, dens, fock, bad); break;
         if constexpr (G) {
             switch (R.it) {  // uniform across the block
                 RT_FOCK_CASE(2) RT_FOCK_CASE(10) RT_FOCK_CASE(11) RT_FOCK_CASE(13) RT_FOCK_CASE(14)
@@ -291,15 +292,21 @@ void launch_fock_skeleton(cudaStream_t st, bool gaunt, const double* rint, const
                           double* fock, unsigned long long* bad) {
     if (nrec <= 0) return;
     const unsigned ntri = (unsigned)((long long)nsc * (nsc + 1) / 2);
-    // as many blocks as are resident (four per SM at 256 threads and 62-64
-    // registers): a second wave would leave SMs idle at the end
+    // four blocks per SM, as many as are resident at 256 threads and the
+    // two-set kernels' registers: a second wave would leave SMs idle at the
+    // end, and more blocks per SM (the one-set kernels would fit eight)
+    // measured slower
     const int grid = nrec < 152 * 4 ? nrec : 152 * 4;
-    if (gaunt)
-        k_fock_skeleton<true><<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, (unsigned)nsc, ntri, nmat, dens,
-                                                    fock, bad);
-    else
-        k_fock_skeleton<false><<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, (unsigned)nsc, ntri, nmat, dens,
-                                                     fock, bad);
+#define RT_FOCK_LAUNCH(GV, NMV)                                                                          \
+    k_fock_skeleton<GV, NMV><<<grid, 256, 0, st>>>(rint, l2, l1, recs, nrec, (unsigned)nsc, ntri, dens, fock, bad)
+    if (gaunt) {
+        if (nmat == 2) RT_FOCK_LAUNCH(true, 2);
+        else RT_FOCK_LAUNCH(true, 1);
+    } else {
+        if (nmat == 2) RT_FOCK_LAUNCH(false, 2);
+        else RT_FOCK_LAUNCH(false, 1);
+    }
+#undef RT_FOCK_LAUNCH
 }
 
 }  // namespace rt
