@@ -6,8 +6,9 @@
  *
  * Parity status: "parity unpinned" against reference-run outputs (Fortran 77,
  * no compiler here, no tmoone fixtures in the reference).  The restatement is
- * cross-checked against a dense Coulomb/exchange formulation of the same
- * integrals (tests/test_fock_oracle.py).
+ * cross-checked against dense formulations of the same integrals
+ * (tests/test_fock_oracle.py): FOCK against 2J - K / -K, GAUNT against
+ * 3K / -K for Kramers-restricted densities.
  *
  * MFDFOCK (source/tmoone/mfdfock.F:53-66) clears the closed- and open-shell
  * Fock arrays, then reads the integral records of files 1..MFIL

@@ -1,5 +1,5 @@
-"""The skeleton Fock oracle (tmoone's MFDFOCK/FOCK restated in
-oracle/tmoone_fock_oracle.c) against a dense formulation (CPU only).
+"""The skeleton Fock oracle (tmoone's MFDFOCK/FOCK and MFDBREIT/GAUNT restated
+in oracle/tmoone_fock_oracle.c) against dense formulations (CPU only).
 
 FOCK adds each unique integral (IJ|KL) of a record of type IT
 (source/tmoone/fock.F) to lower-triangle Fock elements.  For one set of
@@ -105,6 +105,48 @@ def test_fock_oracle_rejects_bad_labels():
     n = p.n
     with pytest.raises(ValueError):
         pyoracle.fock_skeleton((cls, its, nts, v, l2, l1), n, np.zeros((1, 4, n * (n + 1) // 2)))
+
+
+def gaunt_tensor(records, n):
+    """The full (SL|SL) tensor from the file-4 records (eight-fold permutation symmetry)."""
+    cls, its, nts, v, l2, l1 = records
+    off = np.concatenate([[0], np.cumsum(nts)])
+    keep = np.concatenate([np.arange(off[r], off[r + 1]) for r in range(cls.size) if cls[r] == 4])
+    a, b = (l2[keep] >> 16) - 1, (l2[keep] & 0xFFFF) - 1
+    c, d = (l1[keep] >> 16) - 1, (l1[keep] & 0xFFFF) - 1
+    g = np.zeros((n,) * 4)
+    for (p, q, r, s) in ((a, b, c, d), (b, a, c, d), (a, b, d, c), (b, a, d, c),
+                         (c, d, a, b), (d, c, a, b), (c, d, b, a), (d, c, b, a)):
+        g[p, q, r, s] = v[keep]
+    return g
+
+
+@pytest.mark.parametrize("nl,ns,nkr,seed", [(3, 4, 2, 0), (4, 6, 3, 2), (6, 9, 3, 5)])
+def test_gaunt_oracle_is_three_k_and_minus_k(nl, ns, nkr, seed):
+    """GAUNT (source/tmoone/gaunt.F) restated by the oracle against a dense
+    formulation: for a Kramers-restricted density (AAR symmetric; BAR, AAI,
+    BAI antisymmetric) the Gaunt skeleton is, element (i,j) with i >= j,
+    3 K[D](i,j) for AAR and -K[D](i,j) for the others (off the diagonal),
+    K[D](i,j) = sum_kl (ik|jl) D(k,l) over the (SL|SL) integrals -- the
+    scalar and vector parts of sigma . sigma."""
+    p = synth.make_problem(nl, ns, nkr, seed=seed, breit=True)
+    recs = p.flat_records()
+    n = p.n
+    g = gaunt_tensor(recs, n)
+    dens, full = densities(n, 2, seed)
+    f = pyoracle.fock_gaunt(recs, n, dens)
+    i, j = np.tril_indices(n)
+    order = np.argsort(i * (i + 1) // 2 + j)
+    i, j = i[order], j[order]
+    off = i != j
+    for s in range(2):
+        mats = full[s]   # AAR, BAR, AAI, BAI
+        k = [np.einsum("ikjl,kl->ij", g, x) for x in mats]
+        want = [3.0 * k[0], -k[1], -k[2], -k[3]]
+        scale = max(np.abs(w).max() for w in want)
+        assert np.allclose(f[s, 0], want[0][i, j], atol=1e-12 * scale, rtol=0)
+        for x in (1, 2, 3):
+            assert np.allclose(f[s, x][off], want[x][i, j][off], atol=1e-12 * scale, rtol=0), x
 
 
 def test_gaunt_oracle_reads_file_4_only_and_rejects_other_types():
