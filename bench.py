@@ -16,6 +16,9 @@ too); ``e2e.sequential`` copies each step's records before it, and
 (the reference is Fortran 77 and cannot be built here) on a bounded sample of
 the same workload with all host cores.
 
+The line also carries ``fock``: tmoone's skeleton Fock build over the same
+resident records (``--workload fock`` measures it with oracle checks).
+
 Multi-GPU: every rank runs an independent replica of the workload (no
 collective on the data path); value = all ranks' work / max rank time.
 """
@@ -605,6 +608,8 @@ def main():
                     help="M,K,N of --workload gemm")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fock", action="store_true",
+                    help="leave out the skeleton Fock build of the default line")
     ap.add_argument("--no-batched", action="store_true",
                     help="leave out the 48-instance batched leg of the default line")
     ap.add_argument("--half-buckets", action="store_true",
@@ -870,6 +875,30 @@ def main():
         cpu = {"value": res["tflops"], "unit": "TFLOP/s", "cores": cores, "kind": "port",
                "sample": res["sample"]}
 
+    # ---- tmoone's skeleton Fock build over the same resident records ----
+    fock = None
+    if work["name"] == WORKLOAD["name"] and not args.no_fock:
+        ntri = prob.n * (prob.n + 1) // 2
+        gen = torch.Generator(device="cuda").manual_seed(0)
+        d1 = torch.randn((1, 4, ntri), device="cuda", dtype=torch.float64, generator=gen)
+        d2 = torch.randn((1, 4, ntri), device="cuda", dtype=torch.float64, generator=gen)
+        with rotran.Rotran.for_problem(prob) as frt:
+            frt.add_records_bulk_device(cls, nts, its, dv, dl2, dl1)
+            for _ in range(2):
+                frt.fock_skeleton(d1)
+            fms = []
+            for _ in range(3):
+                f1, k = frt.fock_skeleton(d1)
+                fms.append(k)
+            f2, _ = frt.fock_skeleton(d2)
+            f12, _ = frt.fock_skeleton(d1 + d2)
+            lin = float((f12 - f1 - f2).abs().max() / f12.abs().max())
+        fmean = statistics.mean(fms)
+        fock = {"workload": "skeleton Fock build (MFDFOCK/FOCK) over these records, one density set",
+                "value": nint / (fmean / 1e3), "unit": "integrals/s", "ms_kernel": fmean,
+                "steps": 3, "warmup": 2, "linearity_rel_err": lin,
+                "hbm_frac": 16.0 * nint / (fmean / 1e3) / 1e9 / hbm_peak}
+
     # ---- the batched workload (48 instances, one CUDA graph) beside it ----
     batched = None
     if work["name"] == WORKLOAD["name"] and not args.no_batched and prec_name == "split":
@@ -926,7 +955,7 @@ def main():
                           "half_buckets": bool(args.half_buckets)},
             "tflops_dense_equivalent": config["flops_dense_equivalent"] * world / main["sec"] / 1e12,
             "oracle_check": ocheck,
-            "batched": batched,
+            "batched": batched, "fock": fock,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64,
             "gpu_launches": st.gpu_launches * args.steps, "clocks": main["clocks"],
             "stats": st.as_dict(), "mdcint": {"records": nrec, "elements": nz},
